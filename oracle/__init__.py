@@ -1,0 +1,257 @@
+"""CPU oracle for the PIS Lennard-Jones MD step - TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
+may import this package, and only as the checker. The product (``pis_gb300``) never
+imports, loads or executes anything from here.
+
+It wraps ``oracle/pis_oracle.cpp`` (a C++ restatement of the reference's FP64 arithmetic,
+built by ``oracle/Makefile`` into ``oracle/_build/liboracle.so``) and
+``oracle/data_file.py`` (a restatement of the reference's data-file reader).
+
+Parity status: "parity unpinned" against reference outputs - the reference is a Rust
+crate that cannot be built here and its tests pin no physics. The oracle is anchored on
+known-answer tests derived from the reference's example inputs instead.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from .data_file import read_data  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+
+OFFSET, ALLPAIRS, VERLET27, PARALLEL, FULLLIST = 0, 1, 2, 3, 4
+KB = 0.0083144621  # src/constants.rs:3
+
+
+def build() -> str:
+    """Compile the oracle library (idempotent)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+class _System(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64),
+        ("n_types", C.c_int32),
+        ("pbc", C.c_int32 * 3),
+        ("type_ids", C.POINTER(C.c_int32)),
+        ("masses", C.POINTER(C.c_double)),
+        ("pos", C.POINTER(C.c_double)),
+        ("vel", C.POINTER(C.c_double)),
+        ("force", C.POINTER(C.c_double)),
+        ("h", C.c_double * 9),
+        ("hinv", C.c_double * 9),
+        ("eps", C.POINTER(C.c_double)),
+        ("sigma", C.POINTER(C.c_double)),
+        ("rcut", C.POINTER(C.c_double)),
+        ("present", C.POINTER(C.c_int32)),
+        ("shift", C.c_int32),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = C.CDLL(_LIB_PATH)
+        P = C.POINTER
+        S = P(_System)
+        d = C.c_double
+        L.or_inverse3.argtypes = [P(d), P(d)]
+        L.or_determinant3.argtypes = [P(d)]
+        L.or_determinant3.restype = d
+        L.or_min_image.argtypes = [S, P(d)]
+        L.or_wrap.argtypes = [S, P(d)]
+        L.or_lj_pair.argtypes = [d, d, d, C.c_int32, P(d), P(d), P(d)]
+        L.or_max_rcut.argtypes = [S]
+        L.or_max_rcut.restype = d
+        L.or_divide_into_cells.argtypes = [S, d, P(C.c_int64)]
+        for name in ("or_compute_allpairs", "or_compute_verlet27", "or_compute_offset", "or_compute_full_list"):
+            getattr(L, name).argtypes = [S]
+            getattr(L, name).restype = d
+        L.or_compute_parallel.argtypes = [S, C.c_int32]
+        L.or_compute_parallel.restype = d
+        L.or_compute_potential.argtypes = [S, C.c_int32, C.c_int32]
+        L.or_compute_potential.restype = d
+        L.or_build_full_list.argtypes = [S, P(C.c_int64), P(C.c_int32), C.c_int64]
+        L.or_build_full_list.restype = C.c_int64
+        L.or_verlet_step_nve.argtypes = [S, d, C.c_int32, C.c_int32]
+        L.or_verlet_step_nve.restype = d
+        L.or_kinetic_energy.argtypes = [S]
+        L.or_kinetic_energy.restype = d
+        L.or_virial_tensor.argtypes = [S, P(d)]
+        L.or_pressure.argtypes = [S, d]
+        L.or_pressure.restype = d
+        L.or_temperature.argtypes = [S, d]
+        L.or_temperature.restype = d
+        L.or_run_nve.argtypes = [S, d, C.c_int64, C.c_int32, C.c_int32, P(d), P(d)]
+        L.or_fcc_lattice.argtypes = [d, C.c_int64, C.c_int64, C.c_int64, P(d)]
+        L.or_remove_drift_and_rescale.argtypes = [S, d]
+        L.or_num_threads_available.restype = C.c_int32
+        _lib = L
+    return _lib
+
+
+def _ptr(a, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def inverse3(h_rowmajor) -> np.ndarray:
+    h = np.ascontiguousarray(h_rowmajor, dtype=np.float64).reshape(9)
+    out = np.zeros(9)
+    lib().or_inverse3(_ptr(h, C.c_double), _ptr(out, C.c_double))
+    return out.reshape(3, 3)
+
+
+def lj_pair(eps, sigma, rcut, rij, shift=True):
+    r = np.ascontiguousarray(rij, dtype=np.float64)
+    u = np.zeros(1)
+    f = np.zeros(3)
+    lib().or_lj_pair(eps, sigma, rcut, int(shift), _ptr(r, C.c_double), _ptr(u, C.c_double), _ptr(f, C.c_double))
+    return float(u[0]), f
+
+
+def fcc_lattice(a, nx, ny, nz) -> np.ndarray:
+    pos = np.zeros((nx * ny * nz * 4, 3))
+    lib().or_fcc_lattice(a, nx, ny, nz, _ptr(pos, C.c_double))
+    return pos
+
+
+class System:
+    """Reference-layout state: positions/velocities/forces as (N,3) float64 (x,y,z per
+    atom), 1-based int32 type ids, masses per type, row-major box matrix h, and a dense
+    per-type-pair LJ table (key (min, max) as the reference's get_potential_ij)."""
+
+    def __init__(self, positions, type_ids, masses, h, table, velocities=None, pbc=(1, 1, 1), shift=True):
+        self.pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3).copy()
+        n = self.pos.shape[0]
+        self.vel = (np.zeros((n, 3)) if velocities is None
+                    else np.ascontiguousarray(velocities, dtype=np.float64).reshape(-1, 3).copy())
+        self.force = np.zeros((n, 3))
+        self.type_ids = np.ascontiguousarray(type_ids, dtype=np.int32).reshape(n).copy()
+        self.masses = np.ascontiguousarray(masses, dtype=np.float64).copy()
+        nt = len(self.masses)
+        self.eps = np.zeros(nt * nt)
+        self.sigma = np.zeros(nt * nt)
+        self.rcut = np.zeros(nt * nt)
+        self.present = np.zeros(nt * nt, dtype=np.int32)
+        for (ti, tj), (e, s, rc) in table.items():
+            a, b = min(ti, tj), max(ti, tj)
+            k = (a - 1) * nt + (b - 1)
+            self.eps[k], self.sigma[k], self.rcut[k], self.present[k] = e, s, rc, 1
+        self.h = np.ascontiguousarray(h, dtype=np.float64).reshape(3, 3).copy()
+        self.hinv = inverse3(self.h)
+        self._s = _System()
+        s = self._s
+        s.n = n
+        s.n_types = nt
+        s.pbc[:] = [int(p) for p in pbc]
+        s.shift = int(shift)
+        self._refresh()
+
+    def _refresh(self):
+        s = self._s
+        s.type_ids = _ptr(self.type_ids, C.c_int32)
+        s.masses = _ptr(self.masses, C.c_double)
+        s.pos = _ptr(self.pos, C.c_double)
+        s.vel = _ptr(self.vel, C.c_double)
+        s.force = _ptr(self.force, C.c_double)
+        s.h[:] = list(self.h.reshape(9))
+        s.hinv[:] = list(self.hinv.reshape(9))
+        s.eps = _ptr(self.eps, C.c_double)
+        s.sigma = _ptr(self.sigma, C.c_double)
+        s.rcut = _ptr(self.rcut, C.c_double)
+        s.present = _ptr(self.present, C.c_int32)
+
+    @property
+    def n(self):
+        return self.pos.shape[0]
+
+    def compute_potential(self, manager=OFFSET, nthreads=1) -> float:
+        self._refresh()
+        return lib().or_compute_potential(C.byref(self._s), manager, nthreads)
+
+    def verlet_step_nve(self, dt, manager=OFFSET, nthreads=1) -> float:
+        self._refresh()
+        return lib().or_verlet_step_nve(C.byref(self._s), dt, manager, nthreads)
+
+    def run_nve(self, dt, steps, manager=OFFSET, nthreads=1):
+        self._refresh()
+        pe = np.zeros(steps + 1)
+        ke = np.zeros(steps + 1)
+        lib().or_run_nve(C.byref(self._s), dt, steps, manager, nthreads, _ptr(pe, C.c_double), _ptr(ke, C.c_double))
+        return pe, ke
+
+    def full_list(self):
+        """Reference full neighbour list at rcut: list of sorted-as-built index arrays."""
+        self._refresh()
+        off = np.zeros(self.n + 1, dtype=np.int64)
+        total = lib().or_build_full_list(C.byref(self._s), _ptr(off, C.c_int64), None, 0)
+        idx = np.zeros(max(total, 1), dtype=np.int32)
+        lib().or_build_full_list(C.byref(self._s), _ptr(off, C.c_int64), _ptr(idx, C.c_int32), total)
+        return off, idx[:total]
+
+    def kinetic_energy(self) -> float:
+        self._refresh()
+        return lib().or_kinetic_energy(C.byref(self._s))
+
+    def virial_tensor(self) -> np.ndarray:
+        self._refresh()
+        w = np.zeros(9)
+        lib().or_virial_tensor(C.byref(self._s), _ptr(w, C.c_double))
+        return w.reshape(3, 3)
+
+    def pressure(self, ke) -> float:
+        self._refresh()
+        return lib().or_pressure(C.byref(self._s), ke)
+
+    def temperature(self, ke) -> float:
+        self._refresh()
+        return lib().or_temperature(C.byref(self._s), ke)
+
+    def min_image(self, r) -> np.ndarray:
+        self._refresh()
+        v = np.ascontiguousarray(r, dtype=np.float64).copy()
+        lib().or_min_image(C.byref(self._s), _ptr(v, C.c_double))
+        return v
+
+    def wrap(self, r) -> np.ndarray:
+        self._refresh()
+        v = np.ascontiguousarray(r, dtype=np.float64).copy()
+        lib().or_wrap(C.byref(self._s), _ptr(v, C.c_double))
+        return v
+
+    def max_rcut(self) -> float:
+        self._refresh()
+        return lib().or_max_rcut(C.byref(self._s))
+
+    def divide_into_cells(self, rcut):
+        self._refresh()
+        n = np.zeros(3, dtype=np.int64)
+        lib().or_divide_into_cells(C.byref(self._s), rcut, _ptr(n, C.c_int64))
+        return tuple(int(x) for x in n)
+
+    def remove_drift_and_rescale(self, temperature):
+        self._refresh()
+        lib().or_remove_drift_and_rescale(C.byref(self._s), temperature)
+
+    @staticmethod
+    def from_data(data, shift=True):
+        """Build from a parsed data file (oracle.read_data)."""
+        h = np.diag([data["xhi"] - data["xlo"], data["yhi"] - data["ylo"], data["zhi"] - data["zlo"]])
+        return System(data["positions"], data["type_ids"], data["masses"], h, data["table"],
+                      velocities=data["velocities"], shift=shift)
+
+
+def num_threads_available() -> int:
+    return int(lib().or_num_threads_available())

@@ -1,0 +1,89 @@
+"""ctypes binding of ``libpis_gpu.so`` (C ABI declared in include/pis_gpu.h).
+
+The library is built in-tree by ``pis_gb300.build``; importing this module without it fails
+loudly - there is no CPU fallback anywhere in the package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from .build import LIB
+
+PIS_OK = 0
+STATUS_NAMES = {
+    0: "PIS_OK", 1: "PIS_ERR_INVALID_ARGUMENT", 2: "PIS_ERR_NO_ATOMS", 3: "PIS_ERR_INVALID_ATOM_TYPE",
+    4: "PIS_ERR_MISSING_POTENTIAL", 5: "PIS_ERR_IO", 6: "PIS_ERR_PARSE", 7: "PIS_ERR_ATOM_COUNT",
+    8: "PIS_ERR_UNKNOWN_PAIR_STYLE", 20: "PIS_ERR_NAN_DETECTED", 21: "PIS_ERR_BOX_TOO_SMALL",
+    22: "PIS_ERR_NO_MEMORY", 23: "PIS_ERR_LIST_OVERFLOW", 24: "PIS_ERR_CUDA", 25: "PIS_ERR_STATE",
+    26: "PIS_ERR_UNSUPPORTED",
+}
+PRECISION = {"fp64": 0, "mixed": 1}
+LIST_KIND = {"default": 0, "half": 1, "full": 2}
+
+
+class PisError(RuntimeError):
+    """A non-zero pis_status from the library."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        self.name = STATUS_NAMES.get(status, f"status {status}")
+        super().__init__(f"{self.name}: {message}")
+
+
+class LJPair(C.Structure):
+    _fields_ = [("ti", C.c_int32), ("tj", C.c_int32), ("epsilon", C.c_double), ("sigma", C.c_double),
+                ("rcut", C.c_double), ("shift", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("n_atoms", C.c_int64), ("steps", C.c_int64), ("rebuilds", C.c_int64),
+                ("list_entries", C.c_int64), ("list_capacity", C.c_int32), ("cells", C.c_int32 * 3),
+                ("pe", C.c_double), ("ke", C.c_double), ("virial", C.c_double * 9)]
+
+
+_lib = None
+
+# (name, restype, argtypes) of every C-ABI entry point declared in include/pis_gpu.h
+_VP = C.c_void_p
+_DP = C.POINTER(C.c_double)
+SIGNATURES = [
+    ("pis_gpu_create", C.c_int, [C.POINTER(LJPair), C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(_VP)]),
+    ("pis_gpu_set_options", C.c_int, [_VP, C.c_int32, C.c_int32]),
+    ("pis_gpu_set_state", C.c_int, [_VP, C.c_int64, C.POINTER(C.c_int32), _DP, _DP, _DP, _DP, _DP,
+                                    C.POINTER(C.c_uint8)]),
+    ("pis_gpu_compute_potential", C.c_int, [_VP, _DP, _DP]),
+    ("pis_gpu_verlet_step_nve", C.c_int, [_VP, C.c_double, C.c_int64, _DP]),
+    ("pis_gpu_get_state", C.c_int, [_VP, _DP, _DP, _DP]),
+    ("pis_gpu_reductions", C.c_int, [_VP, _DP, _DP]),
+    ("pis_gpu_neighbour_list", C.c_int, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int64,
+                                         C.POINTER(C.c_int64)]),
+    ("pis_gpu_scale_velocities", C.c_int, [_VP, _DP]),
+    ("pis_gpu_scale_box", C.c_int, [_VP, _DP]),
+    ("pis_gpu_get_stats", C.c_int, [_VP, C.POINTER(Stats)]),
+    ("pis_gpu_last_error", C.c_char_p, [_VP]),
+    ("pis_gpu_destroy", None, [_VP]),
+    ("pis_gpu_run_timed", C.c_int, [_VP, C.c_double, C.c_int64, _DP, _DP]),
+    ("pis_gpu_kernel_launches", C.c_int64, []),
+    ("pis_gpu_version", C.c_char_p, []),
+]
+
+
+def lib() -> C.CDLL:
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise ImportError(f"{LIB} is missing: build it with `python -m pis_gb300.build` "
+                              "(pis_gb300 has no CPU fallback)")
+        L = C.CDLL(LIB)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def library_path() -> str:
+    return LIB

@@ -1,0 +1,1496 @@
+// engine.cu - kernels and pool management of the packed multi-system LJ MD engine.
+//
+// Per velocity-Verlet step every active slot goes through (one launch each, over the pool):
+//   k_integrate1   a_t = F/m; x += v dt + (a_t/2) dt^2; periodic wrap; skin-displacement test;
+//                  cell-relative FP32 coordinates for the mixed path
+//   k_bin .. k_build  neighbour-list rebuild, each kernel a no-op for slots whose rebuild flag
+//                  is clear: counting sort of atoms into cells (bin -> scan -> scatter), a
+//                  per-cell id sort + gather that physically reorders the atoms by cell, then
+//                  the list build at rcut + skin
+//   k_force_*      LJ forces and energy (FP64 half list with atomics, FP64 full list, or mixed
+//                  FP32 full list)
+//   k_integrate2   v += (a_t + a_tdt)/2 dt; chunk partial sums of KE (and virial on demand)
+//   k_step_end     per-slot deterministic reductions, history, counters
+// Everything a step needs lives in device memory, so chunks of steps are captured as one
+// CUDA graph and replayed without host round trips.
+//
+// Reference arithmetic (FP64 path): src/potentials/potential.rs:15-33 (NVE step),
+// src/simulation_box.rs:17-42 (min-image, wrap), src/potentials/lennard_jones.rs:33-55 (pair),
+// src/atoms/properties.rs:17-51 (a = F/m, KE, virial). Rounding is pinned with __d*_rn
+// intrinsics so no multiply-add is fused where the reference has two roundings.
+#include "engine.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+
+namespace pis {
+
+static std::atomic<int64_t> g_launches{0};
+int64_t Engine::launches() { return g_launches.load(); }
+
+constexpr int JBITS = 26;                  // atom-index bits of a neighbour entry
+constexpr uint32_t JMASK = (1u << JBITS) - 1u;
+constexpr int SCAN_THREADS = 1024;
+constexpr int END_THREADS = 256;
+
+struct Engine::DevPtrs {
+    double4* pos[2];
+    double4* vel[2];
+    double4* acc[2];
+    int32_t* id[2];
+    double4* frc;
+    double4* posb;
+    float4* prel;
+    int32_t* cellof;
+    int32_t* lcell;
+    int32_t* slotin;
+    int32_t* perm;
+    int32_t* nn;
+    uint32_t* nbr;
+    uint8_t* keep;
+    int32_t* cell_count;
+    int32_t* cell_start;
+    int32_t* cell_sys;
+    int32_t* blk_sys;
+    int32_t* blk_first;
+    SysParams* sp;
+    SysState* st;
+    LJDev* tab;
+    double* pe_part;
+    double* ke_part;
+    double* vir_part;
+    double* pe_hist;
+    int64_t npad;
+    int32_t cap;
+    int32_t hist;
+    int32_t max_slots;
+    int32_t zero_forces;  // half list: integrate1 clears F for the atomic scatter
+    int32_t full_list;
+};
+using DP = Engine::DevPtrs;
+
+// ---------------------------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ int type_of(double w) { return __double2hiint(w); }
+__device__ __forceinline__ double pack_type(int t) { return __hiloint2double(t, 0); }
+
+// One axis of SimulationBox::apply_boundary_conditions_dis for a diagonal box:
+// s = hinv*r; s -= round(s); r = h*s. rint replaces round: they differ only at |s - k| = 1/2,
+// i.e. |r| = L/2, which is beyond every cutoff because L > 2 (rcut + skin) is enforced.
+__device__ __forceinline__ double min_image_axis(double r, double h, double hinv) {
+    double s = __dmul_rn(hinv, r);
+    s = __dsub_rn(s, rint(s));
+    return __dmul_rn(h, s);
+}
+// One axis of SimulationBox::apply_boundary_conditions_pos: s = hinv*r; s -= floor(s); r = h*s.
+__device__ __forceinline__ double wrap_axis(double r, double h, double hinv) {
+    double s = __dmul_rn(hinv, r);
+    s = __dsub_rn(s, floor(s));
+    return __dmul_rn(h, s);
+}
+__device__ __forceinline__ double norm2_ref(double x, double y, double z) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+}
+
+// LennardJones::compute_potential (src/potentials/lennard_jones.rs:33-55) behind the
+// `|rij| > rcut => skip` test of the managers (:224-226). Returns false when skipped. The
+// cutoff is decided with the reference's own sqrt comparison inside a 1e-12 band around rcut^2.
+struct LJ64 {
+    double eps4, eps24, sigma2, rcut, rc2_lo, rc2_hi, ucut;
+};
+__device__ __forceinline__ LJ64 lj64_load(const LJDev& L) {
+    return LJ64{L.eps4, L.eps24, L.sigma2, L.rcut, L.rc2_lo, L.rc2_hi, L.ucut};
+}
+__device__ __forceinline__ bool lj_fp64(const LJ64& P, double r2, double& u, double& c) {
+    if (r2 > P.rc2_hi) return false;
+    if (r2 >= P.rc2_lo && sqrt(r2) > P.rcut) return false;
+    double inv = __ddiv_rn(1.0, r2);
+    double s2 = __dmul_rn(P.sigma2, inv);
+    double vdw = __dmul_rn(s2, __dmul_rn(s2, s2));
+    double rep = __dmul_rn(vdw, vdw);
+    u = __dsub_rn(__dmul_rn(P.eps4, __dsub_rn(rep, vdw)), P.ucut);
+    c = __dmul_rn(__dmul_rn(P.eps24, __dsub_rn(__dmul_rn(2.0, rep), vdw)), inv);
+    return true;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Deterministic block sum (fixed tree). All threads must call it; result valid in thread 0.
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    v = warp_sum(v);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (w == 0) {
+        r = (l < NT / 32) ? sh[l] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;
+}
+
+// Which atom this thread owns. Returns false for padding threads; s < 0 for unused chunks.
+__device__ __forceinline__ bool atom_of(const DP& P, int& s, int& i) {
+    s = P.blk_sys[blockIdx.x];
+    if (s < 0) return false;
+    i = P.blk_first[blockIdx.x] + (int)threadIdx.x;
+    const SysParams& sp = P.sp[s];
+    return i < (int)(sp.a0 + sp.n);
+}
+
+__device__ __forceinline__ bool slot_runs(const DP& P, int s, bool respect_steps) {
+    return !respect_steps || P.st[s].steps_left > 0;
+}
+
+__device__ __forceinline__ float4 cell_relative(const SysParams& sp, double4 p, int lc, int type) {
+    int cx = lc % sp.nc[0];
+    int cy = (lc / sp.nc[0]) % sp.nc[1];
+    int cz = lc / (sp.nc[0] * sp.nc[1]);
+    double dx = p.x - (cx + 0.5) * sp.cs[0];
+    double dy = p.y - (cy + 0.5) * sp.cs[1];
+    double dz = p.z - (cz + 0.5) * sp.cs[2];
+    dx -= sp.h[0] * rint(dx * sp.hinv[0]);
+    dy -= sp.h[1] * rint(dy * sp.hinv[1]);
+    dz -= sp.h[2] * rint(dz * sp.hinv[2]);
+    return make_float4((float)dx, (float)dy, (float)dz, __int_as_float(type));
+}
+
+// ---------------------------------------------------------------------------------------------
+// step kernels
+// ---------------------------------------------------------------------------------------------
+// First half of PotentialManager::verlet_step_nve (src/potentials/potential.rs:16-24).
+template <bool MIXED>
+__global__ void k_integrate1(const DP P) {
+    int s, i;
+    if (!atom_of(P, s, i)) return;
+    if (!slot_runs(P, s, true)) return;
+    const SysParams& sp = P.sp[s];
+    SysState& st = P.st[s];
+    const int cur = st.cur;
+    double4 p = P.pos[cur][i];
+    double4 v = P.vel[cur][i];
+    double4 f = P.frc[i];
+    const double m = v.w;
+    // Atoms::current_acceleration: a = 0 + F/m (src/atoms/properties.rs:32-39)
+    double ax = __dadd_rn(0.0, __ddiv_rn(f.x, m));
+    double ay = __dadd_rn(0.0, __ddiv_rn(f.y, m));
+    double az = __dadd_rn(0.0, __ddiv_rn(f.z, m));
+    // positions += v*dt + (a*0.5)*dt^2
+    double x = __dadd_rn(p.x, __dadd_rn(__dmul_rn(v.x, sp.dt), __dmul_rn(__dmul_rn(ax, 0.5), sp.dt2)));
+    double y = __dadd_rn(p.y, __dadd_rn(__dmul_rn(v.y, sp.dt), __dmul_rn(__dmul_rn(ay, 0.5), sp.dt2)));
+    double z = __dadd_rn(p.z, __dadd_rn(__dmul_rn(v.z, sp.dt), __dmul_rn(__dmul_rn(az, 0.5), sp.dt2)));
+    x = wrap_axis(x, sp.h[0], sp.hinv[0]);
+    y = wrap_axis(y, sp.h[1], sp.hinv[1]);
+    z = wrap_axis(z, sp.h[2], sp.hinv[2]);
+    P.pos[cur][i] = make_double4(x, y, z, p.w);
+    P.acc[cur][i] = make_double4(ax, ay, az, 0.0);
+    if (P.zero_forces) P.frc[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+    // skin test: rebuild when any atom moved more than skin/2 since the last build
+    double4 b = P.posb[i];
+    double dx = min_image_axis(x - b.x, sp.h[0], sp.hinv[0]);
+    double dy = min_image_axis(y - b.y, sp.h[1], sp.hinv[1]);
+    double dz = min_image_axis(z - b.z, sp.h[2], sp.hinv[2]);
+    double d2 = dx * dx + dy * dy + dz * dz;
+    if (!(d2 <= sp.half_skin2)) st.rebuild = 1;  // NaN also requests a rebuild
+    if (x != x || y != y || z != z) atomicOr(&st.flags, FLAG_NAN);
+    if (MIXED) P.prel[i] = cell_relative(sp, make_double4(x, y, z, 0.0), P.cellof[i], type_of(p.w));
+}
+
+// Counting sort, pass 1: cell of every atom (reference binning of src/atoms/neighbour_list.rs:
+// 9-42 at rcut + skin, with a Euclidean modulo so atoms outside the box fold back in) and its
+// slot inside the cell.
+__global__ void k_bin(const DP P, int respect_steps) {
+    int s, i;
+    if (!atom_of(P, s, i)) return;
+    if (!slot_runs(P, s, respect_steps)) return;
+    const SysParams& sp = P.sp[s];
+    const SysState& st = P.st[s];
+    if (!st.rebuild) return;
+    double4 p = P.pos[st.cur][i];
+    int c[3];
+    double q[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double t = floor(__dmul_rn(__dmul_rn(sp.hinv[d], q[d]), (double)sp.nc[d]));
+        long long k = (t == t) ? (long long)fmax(fmin(t, 4.0e18), -4.0e18) : 0;
+        k %= sp.nc[d];
+        if (k < 0) k += sp.nc[d];
+        c[d] = (int)k;
+    }
+    int lc = (c[2] * sp.nc[1] + c[1]) * sp.nc[0] + c[0];
+    P.lcell[i] = lc;
+    P.slotin[i] = atomicAdd(&P.cell_count[sp.c0 + lc], 1);
+}
+
+// Counting sort, pass 2: exclusive scan of the cell counts of one slot (one block per slot),
+// writing absolute atom indices; also flips the slot's buffer set.
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan(const DP P, int respect_steps) {
+    int s = blockIdx.x;
+    const SysParams& sp = P.sp[s];
+    if (!sp.active) return;
+    if (!slot_runs(P, s, respect_steps)) return;
+    SysState& st = P.st[s];
+    if (!st.rebuild) return;
+    __shared__ int warp_tot[SCAN_THREADS / 32];
+    __shared__ int carry_sh;
+    const int ncell = sp.nc[0] * sp.nc[1] * sp.nc[2];
+    int carry = (int)sp.a0;
+    const int t = threadIdx.x, l = t & 31, w = t >> 5;
+    for (int base = 0; base < ncell; base += SCAN_THREADS * 4) {
+        int v[4], sum = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            int c = base + t * 4 + k;
+            v[k] = 0;
+            if (c < ncell) {
+                v[k] = P.cell_count[sp.c0 + c];
+                P.cell_count[sp.c0 + c] = 0;
+            }
+            sum += v[k];
+        }
+        int incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (l >= o) incl += y;
+        }
+        if (l == 31) warp_tot[w] = incl;
+        __syncthreads();
+        if (w == 0) {
+            int x = warp_tot[l];
+            int xi = x;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, xi, o);
+                if (l >= o) xi += y;
+            }
+            warp_tot[l] = xi - x;  // exclusive warp offsets
+            if (l == 31) carry_sh = xi;
+        }
+        __syncthreads();
+        int run = carry + warp_tot[w] + incl - sum;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            int c = base + t * 4 + k;
+            if (c < ncell) P.cell_start[sp.c0 + c] = run;
+            run += v[k];
+        }
+        carry += carry_sh;
+        __syncthreads();
+    }
+    if (t == 0) {
+        P.cell_start[sp.c0 + ncell] = carry;
+        st.cur ^= 1;
+    }
+}
+
+// Counting sort, pass 3: destination of every atom.
+__global__ void k_scatter(const DP P, int respect_steps) {
+    int s, i;
+    if (!atom_of(P, s, i)) return;
+    if (!slot_runs(P, s, respect_steps)) return;
+    if (!P.st[s].rebuild) return;
+    const SysParams& sp = P.sp[s];
+    int dst = P.cell_start[sp.c0 + P.lcell[i]] + P.slotin[i];
+    P.perm[dst] = i;
+}
+
+// One warp per cell: order the cell's atoms by original id (so the layout depends only on the
+// physical state, not on atomics), then move every per-atom array into the new buffer set and
+// record the build snapshot and cell-relative coordinates.
+__global__ void k_gather(const DP P, int64_t max_cells, int respect_steps) {
+    int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (g >= max_cells) return;
+    int s = P.cell_sys[g];
+    if (s < 0) return;
+    if (!slot_runs(P, s, respect_steps)) return;
+    const SysParams& sp = P.sp[s];
+    const SysState& st = P.st[s];
+    if (!st.rebuild) return;
+    int lc = (int)(g - sp.c0);
+    if (lc >= sp.nc[0] * sp.nc[1] * sp.nc[2]) return;  // sentinel entry
+    const int dst_set = st.cur, src_set = st.cur ^ 1;
+    const int beg = P.cell_start[g], end = P.cell_start[g + 1];
+    const int cnt = end - beg;
+    for (int k = lane; k < cnt; k += 32) {
+        int src = P.perm[beg + k];
+        int myid = P.id[src_set][src];
+        int rank = 0;
+        for (int q = 0; q < cnt; ++q) rank += P.id[src_set][P.perm[beg + q]] < myid;
+        int dst = beg + rank;
+        double4 p = P.pos[src_set][src];
+        P.pos[dst_set][dst] = p;
+        P.vel[dst_set][dst] = P.vel[src_set][src];
+        P.acc[dst_set][dst] = P.acc[src_set][src];
+        P.id[dst_set][dst] = myid;
+        P.posb[dst] = p;
+        P.cellof[dst] = lc;
+        P.prel[dst] = cell_relative(sp, p, lc, type_of(p.w));
+    }
+}
+
+// Neighbour-list build at rcut + skin, one thread per atom in cell order. The distance test runs
+// in FP32 on cell-relative coordinates with a radius padded by 1e-5, so the list is a superset
+// of the exact FP64 list; the force kernels apply the exact cutoff. Entry = j | image code << 26,
+// the code giving the cell offset (0, +1, -1 per axis, 2 bits each) that makes the displacement
+// minimum-image at build time.
+template <bool HALF>
+__global__ void k_build(const DP P, int respect_steps) {
+    int s, i;
+    if (!atom_of(P, s, i)) return;
+    if (!slot_runs(P, s, respect_steps)) return;
+    const SysParams& sp = P.sp[s];
+    SysState& st = P.st[s];
+    if (!st.rebuild) return;
+    const int nx = sp.nc[0], ny = sp.nc[1], nz = sp.nc[2];
+    const int lc = P.cellof[i];
+    const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
+    const float4 pi = P.prel[i];
+    const float csx = sp.fcs[0], csy = sp.fcs[1], csz = sp.fcs[2];
+    const float rl2 = sp.frlist2;
+    const int64_t npad = P.npad;
+    const int cap = P.cap;
+    int cnt = 0;
+    const int zlo = nz >= 3 ? -1 : 0, ylo = ny >= 3 ? -1 : 0, xlo = nx >= 3 ? -1 : 0;
+    for (int oz = zlo; oz <= 1; ++oz) {
+        int z2 = cz + oz;
+        z2 += (z2 < 0) ? nz : 0;
+        z2 -= (z2 >= nz) ? nz : 0;
+        for (int oy = ylo; oy <= 1; ++oy) {
+            int y2 = cy + oy;
+            y2 += (y2 < 0) ? ny : 0;
+            y2 -= (y2 >= ny) ? ny : 0;
+            for (int ox = xlo; ox <= 1; ++ox) {
+                int x2 = cx + ox;
+                x2 += (x2 < 0) ? nx : 0;
+                x2 -= (x2 >= nx) ? nx : 0;
+                const int nb = (z2 * ny + y2) * nx + x2;
+                const int b0 = P.cell_start[sp.c0 + nb], b1 = P.cell_start[sp.c0 + nb + 1];
+                for (int j = b0; j < b1; ++j) {
+                    if (HALF ? (j <= i) : (j == i)) continue;
+                    const float4 pj = P.prel[j];
+                    float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                    uint32_t code = 0;
+                    // axis x
+                    if (ox != 0) {
+                        float a = dx + csx, b = dx - csx;
+                        bool usep = (nx == 2) ? (fabsf(a) <= fabsf(b)) : (ox > 0);
+                        dx = usep ? a : b;
+                        code |= usep ? 1u : 2u;
+                    }
+                    if (oy != 0) {
+                        float a = dy + csy, b = dy - csy;
+                        bool usep = (ny == 2) ? (fabsf(a) <= fabsf(b)) : (oy > 0);
+                        dy = usep ? a : b;
+                        code |= (usep ? 1u : 2u) << 2;
+                    }
+                    if (oz != 0) {
+                        float a = dz + csz, b = dz - csz;
+                        bool usep = (nz == 2) ? (fabsf(a) <= fabsf(b)) : (oz > 0);
+                        dz = usep ? a : b;
+                        code |= (usep ? 1u : 2u) << 4;
+                    }
+                    float r2 = dx * dx + dy * dy + dz * dz;
+                    if (r2 <= rl2) {
+                        if (cnt < cap) P.nbr[(int64_t)cnt * npad + i] = (uint32_t)j | (code << JBITS);
+                        ++cnt;
+                    }
+                }
+            }
+        }
+    }
+    if (cnt > cap) {
+        atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
+        cnt = cap;
+    }
+    P.nn[i] = cnt;
+}
+
+// FP64 forces, Newton-3 half list: the pair evaluation of LJVOffsetManager
+// (src/potentials/lennard_jones.rs:214-235) - F_i -= f, F_j += f (j's share by FP64 atomics),
+// PE += u. Forces must be zero on entry.
+template <bool FULL>
+__global__ void k_force_fp64(const DP P, int respect_steps) {
+    __shared__ double sh[32];
+    int s, i;
+    bool live = atom_of(P, s, i);
+    if (s < 0) return;
+    if (!slot_runs(P, s, respect_steps)) return;  // uniform per block (one slot per chunk)
+    double e = 0.0;
+    if (live) {
+        const SysParams& sp = P.sp[s];
+        const int cur = P.st[s].cur;
+        const double4* __restrict__ pos = P.pos[cur];
+        const double4 pi = pos[i];
+        const int ti = type_of(pi.w);
+        const LJDev* tab = P.tab + sp.tab0 + ti * sp.nt;
+        const bool one_type = sp.nt == 1;
+        const LJ64 P0 = lj64_load(tab[0]);
+        const double hx = sp.h[0], hy = sp.h[1], hz = sp.h[2];
+        const double ix = sp.hinv[0], iy = sp.hinv[1], iz = sp.hinv[2];
+        double fx = 0.0, fy = 0.0, fz = 0.0;
+        const int nn = P.nn[i];
+        const int64_t npad = P.npad;
+        for (int k = 0; k < nn; ++k) {
+            const int j = (int)(P.nbr[(int64_t)k * npad + i] & JMASK);
+            const double4 pj = pos[j];
+            double rx = min_image_axis(__dsub_rn(pj.x, pi.x), hx, ix);
+            double ry = min_image_axis(__dsub_rn(pj.y, pi.y), hy, iy);
+            double rz = min_image_axis(__dsub_rn(pj.z, pi.z), hz, iz);
+            double r2 = norm2_ref(rx, ry, rz);
+            LJ64 L = P0;
+            if (!one_type) {
+                const LJDev& T = tab[type_of(pj.w)];
+                if (!T.present) continue;
+                L = lj64_load(T);
+            }
+            double u, c;
+            if (!lj_fp64(L, r2, u, c)) continue;
+            double gx = __dmul_rn(c, rx), gy = __dmul_rn(c, ry), gz = __dmul_rn(c, rz);
+            fx = __dsub_rn(fx, gx);
+            fy = __dsub_rn(fy, gy);
+            fz = __dsub_rn(fz, gz);
+            e = __dadd_rn(e, u);
+            if (!FULL) {
+                atomicAdd(&P.frc[j].x, gx);
+                atomicAdd(&P.frc[j].y, gy);
+                atomicAdd(&P.frc[j].z, gz);
+            }
+        }
+        if (FULL) {
+            P.frc[i] = make_double4(fx, fy, fz, 0.0);
+        } else {
+            atomicAdd(&P.frc[i].x, fx);
+            atomicAdd(&P.frc[i].y, fy);
+            atomicAdd(&P.frc[i].z, fz);
+        }
+    }
+    double tot = block_sum<256>(e, sh);
+    if (threadIdx.x == 0) P.pe_part[blockIdx.x] = tot;
+}
+
+// Mixed precision forces, full list: FP32 pair arithmetic on cell-relative coordinates
+// (displacement = prel_j - prel_i + image shift), FP32 partial sums over runs of 32 neighbours
+// folded into FP64 accumulators. PE is sum_i sum_j u_ij, halved at the reduction.
+__global__ void k_force_mixed(const DP P, int respect_steps) {
+    __shared__ double sh[32];
+    int s, i;
+    bool live = atom_of(P, s, i);
+    if (s < 0) return;
+    if (!slot_runs(P, s, respect_steps)) return;
+    double e = 0.0;
+    if (live) {
+        const SysParams& sp = P.sp[s];
+        const float4* __restrict__ prel = P.prel;
+        const float4 pi = prel[i];
+        const int ti = __float_as_int(pi.w);
+        const LJDev* tab = P.tab + sp.tab0 + ti * sp.nt;
+        const bool one_type = sp.nt == 1;
+        const LJDev P0 = tab[0];
+        const float csx = sp.fcs[0], csy = sp.fcs[1], csz = sp.fcs[2];
+        double fx = 0.0, fy = 0.0, fz = 0.0;
+        const int nn = P.nn[i];
+        const int64_t npad = P.npad;
+        const uint32_t* __restrict__ nb = P.nbr + i;
+        for (int k0 = 0; k0 < nn; k0 += 32) {
+            const int k1 = min(nn, k0 + 32);
+            float px = 0.f, py = 0.f, pz = 0.f, pe = 0.f;
+#pragma unroll 4
+            for (int k = k0; k < k1; ++k) {
+                const uint32_t ent = __ldg(nb + (int64_t)k * npad);
+                const int j = (int)(ent & JMASK);
+                const uint32_t code = ent >> JBITS;
+                const float4 pj = __ldg(prel + j);
+                float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                dx += (code & 1u) ? csx : ((code & 2u) ? -csx : 0.f);
+                dy += (code & 4u) ? csy : ((code & 8u) ? -csy : 0.f);
+                dz += (code & 16u) ? csz : ((code & 32u) ? -csz : 0.f);
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                float frc2 = P0.frc2, fs2 = P0.fsigma2, fe24 = P0.feps24, fe4 = P0.feps4, fuc = P0.fucut;
+                if (!one_type) {
+                    const LJDev& L = tab[__float_as_int(pj.w)];
+                    frc2 = L.present ? L.frc2 : -1.f;
+                    fs2 = L.fsigma2;
+                    fe24 = L.feps24;
+                    fe4 = L.feps4;
+                    fuc = L.fucut;
+                }
+                if (r2 <= frc2) {
+                    const float inv = __fdividef(1.0f, r2);
+                    const float s2 = fs2 * inv;
+                    const float s6 = s2 * s2 * s2;
+                    const float c = fe24 * s6 * fmaf(2.0f, s6, -1.0f) * inv;
+                    px = fmaf(-c, dx, px);
+                    py = fmaf(-c, dy, py);
+                    pz = fmaf(-c, dz, pz);
+                    pe += fmaf(fe4 * s6, s6 - 1.0f, -fuc);
+                }
+            }
+            fx += (double)px;
+            fy += (double)py;
+            fz += (double)pz;
+            e += (double)pe;
+        }
+        P.frc[i] = make_double4(fx, fy, fz, 0.0);
+    }
+    double tot = block_sum<256>(e, sh);
+    if (threadIdx.x == 0) P.pe_part[blockIdx.x] = tot;
+}
+
+// Second half of verlet_step_nve (src/potentials/potential.rs:28-30):
+// v += ((a_t + a_tdt) * 0.5) * dt, then chunk partials of KE = sum 0.5 m |v|^2
+// (src/atoms/properties.rs:17-24) and, on request, W = sum r_i F_i^T (:49-51).
+template <bool UPDATE>
+__global__ void k_integrate2(const DP P, int respect_steps) {
+    __shared__ double sh[32];
+    int s, i;
+    bool live = atom_of(P, s, i);
+    if (s < 0) return;
+    if (!slot_runs(P, s, respect_steps)) return;
+    const SysParams& sp = P.sp[s];
+    const SysState& st = P.st[s];
+    const int cur = st.cur;
+    double ke = 0.0;
+    double w[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double4 p = make_double4(0, 0, 0, 0), f = p;
+    if (live) {
+        double4 v = P.vel[cur][i];
+        f = P.frc[i];
+        const double m = v.w;
+        if (UPDATE) {
+            double4 a = P.acc[cur][i];
+            double bx = __dadd_rn(0.0, __ddiv_rn(f.x, m));
+            double by = __dadd_rn(0.0, __ddiv_rn(f.y, m));
+            double bz = __dadd_rn(0.0, __ddiv_rn(f.z, m));
+            v.x = __dadd_rn(v.x, __dmul_rn(__dmul_rn(__dadd_rn(a.x, bx), 0.5), sp.dt));
+            v.y = __dadd_rn(v.y, __dmul_rn(__dmul_rn(__dadd_rn(a.y, by), 0.5), sp.dt));
+            v.z = __dadd_rn(v.z, __dmul_rn(__dmul_rn(__dadd_rn(a.z, bz), 0.5), sp.dt));
+            P.vel[cur][i] = v;
+        }
+        ke = __dmul_rn(__dmul_rn(0.5, m), norm2_ref(v.x, v.y, v.z));
+        if (st.want_virial) p = P.pos[cur][i];
+    }
+    double tot = block_sum<256>(ke, sh);
+    if (threadIdx.x == 0) P.ke_part[blockIdx.x] = tot;
+    if (st.want_virial) {
+        double r[3] = {p.x, p.y, p.z}, g[3] = {f.x, f.y, f.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                double t = block_sum<256>(live ? r[a] * g[b] : 0.0, sh);
+                if (threadIdx.x == 0) P.vir_part[(int64_t)blockIdx.x * 9 + a * 3 + b] = t;
+            }
+    }
+    (void)w;
+}
+
+// Per-slot end of a step (or of a force evaluation): deterministic sums of the chunk partials,
+// energy history, NaN check (PisError::NaNEnergy, src/errors.rs:87-88), counters.
+// mode 0: step; mode 1: force evaluation only (PE); mode 2: KE/virial only.
+__global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) {
+    __shared__ double sh[32];
+    int s = blockIdx.x;
+    const SysParams& sp = P.sp[s];
+    if (!sp.active) return;
+    SysState& st = P.st[s];
+    if (mode == 0 && st.steps_left <= 0) return;
+    double pe = 0.0, ke = 0.0;
+    for (int c = threadIdx.x; c < sp.nch; c += END_THREADS) {
+        if (mode != 2) pe += P.pe_part[sp.ch0 + c];
+        if (mode != 1) ke += P.ke_part[sp.ch0 + c];
+    }
+    pe = block_sum<END_THREADS>(pe, sh);
+    ke = block_sum<END_THREADS>(ke, sh);
+    double w[9];
+    const bool vir = st.want_virial && mode != 1;
+    if (vir) {
+        for (int q = 0; q < 9; ++q) {
+            double a = 0.0;
+            for (int c = threadIdx.x; c < sp.nch; c += END_THREADS) a += P.vir_part[(int64_t)(sp.ch0 + c) * 9 + q];
+            w[q] = block_sum<END_THREADS>(a, sh);
+        }
+    }
+    if (threadIdx.x == 0) {
+        if (mode != 2) {
+            if (P.full_list) pe *= 0.5;
+            st.pe = pe;
+        }
+        if (mode != 1) st.ke = ke;
+        if (vir)
+            for (int q = 0; q < 9; ++q) st.virial[q] = w[q];
+        if ((mode != 2 && pe != pe) || (mode != 1 && ke != ke)) st.flags |= FLAG_NAN;
+        if (mode != 2 && st.rebuild) {
+            st.rebuilds += 1;
+            st.rebuild = 0;
+        }
+        if (mode == 0) {
+            P.pe_hist[(int64_t)s * P.hist + (st.steps_done % P.hist)] = pe;
+            st.steps_done += 1;
+            st.steps_left -= 1;
+        }
+    }
+}
+
+// Host request for a rebuild of every active slot (force evaluation after new positions).
+__global__ void k_mark_rebuild(const DP P) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= P.max_slots || !P.sp[s].active) return;
+    P.st[s].rebuild = 1;
+}
+
+__global__ void k_zero_forces(const DP P) {
+    int s, i;
+    if (!atom_of(P, s, i)) return;
+    P.frc[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+}
+
+// Exact cutoff test of every list entry of one slot with the reference arithmetic (min-image,
+// Vector3::norm, `> rcut`), for neighbour-set export.
+__global__ void k_keep(const DP P, int slot) {
+    int s, i;
+    if (!atom_of(P, s, i) || s != slot) return;
+    const SysParams& sp = P.sp[s];
+    const int cur = P.st[s].cur;
+    const double4 pi = P.pos[cur][i];
+    const LJDev* tab = P.tab + sp.tab0 + type_of(pi.w) * sp.nt;
+    for (int k = 0; k < P.nn[i]; ++k) {
+        int64_t q = (int64_t)k * P.npad + i;
+        int j = (int)(P.nbr[q] & JMASK);
+        double4 pj = P.pos[cur][j];
+        double rx = min_image_axis(__dsub_rn(pj.x, pi.x), sp.h[0], sp.hinv[0]);
+        double ry = min_image_axis(__dsub_rn(pj.y, pi.y), sp.h[1], sp.hinv[1]);
+        double rz = min_image_axis(__dsub_rn(pj.z, pi.z), sp.h[2], sp.hinv[2]);
+        const LJDev& L = tab[type_of(pj.w)];
+        P.keep[q] = (uint8_t)(L.present && !(sqrt(norm2_ref(rx, ry, rz)) > L.rcut));
+    }
+}
+
+// v <- M v (row-major M) for one slot (ensemble velocity scaling).
+__global__ void k_scale_vel(const DP P, int slot, double m0, double m1, double m2, double m3, double m4,
+                            double m5, double m6, double m7, double m8) {
+    int s, i;
+    if (!atom_of(P, s, i) || s != slot) return;
+    const int cur = P.st[s].cur;
+    double4 v = P.vel[cur][i];
+    double x = m0 * v.x + m1 * v.y + m2 * v.z;
+    double y = m3 * v.x + m4 * v.y + m5 * v.z;
+    double z = m6 * v.x + m7 * v.y + m8 * v.z;
+    P.vel[cur][i] = make_double4(x, y, z, v.w);
+}
+
+// Atoms::scale_box (src/atoms/transformations.rs:5-16) for a diagonal box and diagonal M:
+// s = h^-1 r (old box), r = h' s (new box).
+__global__ void k_scale_pos(const DP P, int slot, double oh0, double oh1, double oh2, double nh0, double nh1,
+                            double nh2) {
+    int s, i;
+    if (!atom_of(P, s, i) || s != slot) return;
+    const int cur = P.st[s].cur;
+    double4 p = P.pos[cur][i];
+    p.x = nh0 * (oh0 * p.x);
+    p.y = nh1 * (oh1 * p.y);
+    p.z = nh2 * (oh2 * p.z);
+    P.pos[cur][i] = p;
+}
+
+// ---------------------------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------------------------
+#define LAUNCH(kern, grid, block, ...)                                \
+    do {                                                               \
+        kern<<<(grid), (block), 0, stream_>>>(__VA_ARGS__);           \
+        g_launches.fetch_add(1);                                       \
+    } while (0)
+
+Engine::Engine() {}
+
+Engine::~Engine() {
+    for (auto& kv : graphs_) {
+        cudaGraphExecDestroy(kv.second.exec);
+        for (auto e : kv.second.ev) cudaEventDestroy(e);
+    }
+    if (d_ && d_->keep) cudaFree(d_->keep);
+    if (mem_) cudaFree(mem_);
+    if (stream_) cudaStreamDestroy(stream_);
+    delete d_;
+}
+
+pis_status Engine::check(cudaError_t e, const char* what, std::string& err) {
+    if (e == cudaSuccess) return PIS_OK;
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return PIS_ERR_NO_MEMORY;
+    return PIS_ERR_CUDA;
+}
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+pis_status Engine::init(const PoolOptions& opt, std::string& err) {
+    opt_ = opt;
+    if (opt.max_atoms <= 0 || opt.max_slots <= 0) {
+        err = "pool needs atoms and slots";
+        return PIS_ERR_INVALID_ARGUMENT;
+    }
+    if (opt.blk != 256) {
+        err = "chunk size must be 256";
+        return PIS_ERR_INVALID_ARGUMENT;
+    }
+    half_ = opt.list_kind == PIS_LIST_HALF ||
+            (opt.list_kind == PIS_LIST_DEFAULT && opt.precision == PIS_PRECISION_FP64);
+    if (opt.precision == PIS_PRECISION_MIXED && half_) {
+        err = "the mixed-precision path uses a full list";
+        return PIS_ERR_UNSUPPORTED;
+    }
+    if (opt.max_atoms >= (int64_t)JMASK) {
+        err = "a pool holds at most 2^26 - 1 atoms (neighbour entries carry a 26-bit index)";
+        return PIS_ERR_UNSUPPORTED;
+    }
+    cap_ = opt.list_cap > 0 ? opt.list_cap : 192;
+    npad_ = (int64_t)align_up((size_t)opt.max_atoms, 32);
+    max_chunks_ = (opt.max_atoms + opt.blk - 1) / opt.blk + opt.max_slots;
+    int64_t max_cells = opt.max_cells > 0 ? opt.max_cells : opt.max_atoms + opt.max_slots;
+    opt_.max_cells = max_cells;
+    pis_status st = check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream", err);
+    if (st) return st;
+
+    const size_t NA = (size_t)opt.max_atoms, NC = (size_t)max_cells, NCH = (size_t)max_chunks_,
+                 NS = (size_t)opt.max_slots;
+    struct Item {
+        void** p;
+        size_t bytes;
+    };
+    d_ = new DevPtrs();
+    std::memset(d_, 0, sizeof(DevPtrs));
+    std::vector<Item> items = {
+        {(void**)&d_->pos[0], 32 * NA}, {(void**)&d_->pos[1], 32 * NA}, {(void**)&d_->vel[0], 32 * NA},
+        {(void**)&d_->vel[1], 32 * NA}, {(void**)&d_->acc[0], 32 * NA}, {(void**)&d_->acc[1], 32 * NA},
+        {(void**)&d_->id[0], 4 * NA},   {(void**)&d_->id[1], 4 * NA},   {(void**)&d_->frc, 32 * NA},
+        {(void**)&d_->posb, 32 * NA},   {(void**)&d_->prel, 16 * NA},   {(void**)&d_->cellof, 4 * NA},
+        {(void**)&d_->lcell, 4 * NA},   {(void**)&d_->slotin, 4 * NA},  {(void**)&d_->perm, 4 * NA},
+        {(void**)&d_->nn, 4 * NA},      {(void**)&d_->nbr, 4 * (size_t)npad_ * cap_},
+        {(void**)&d_->cell_count, 4 * NC}, {(void**)&d_->cell_start, 4 * NC},
+        {(void**)&d_->cell_sys, 4 * NC}, {(void**)&d_->blk_sys, 4 * NCH},
+        {(void**)&d_->blk_first, 4 * NCH}, {(void**)&d_->sp, sizeof(SysParams) * NS},
+        {(void**)&d_->st, sizeof(SysState) * NS}, {(void**)&d_->tab, sizeof(LJDev) * (size_t)opt.max_types_total},
+        {(void**)&d_->pe_part, 8 * NCH}, {(void**)&d_->ke_part, 8 * NCH}, {(void**)&d_->vir_part, 72 * NCH},
+        {(void**)&d_->pe_hist, 8 * NS * (size_t)opt.hist},
+    };
+    size_t total = 0;
+    for (auto& it : items) total += align_up(it.bytes, 256);
+    st = check(cudaMalloc(&mem_, total), "device allocation", err);
+    if (st) return st;
+    mem_bytes_ = total;
+    char* base = (char*)mem_;
+    for (auto& it : items) {
+        *it.p = base;
+        base += align_up(it.bytes, 256);
+    }
+    d_->keep = nullptr;
+    d_->npad = npad_;
+    d_->cap = (int32_t)cap_;
+    d_->hist = opt.hist;
+    d_->max_slots = opt.max_slots;
+    d_->zero_forces = half_ ? 1 : 0;
+    d_->full_list = half_ ? 0 : 1;
+    st = check(cudaMemsetAsync(mem_, 0, total, stream_), "memset", err);
+    if (st) return st;
+    st = check(cudaMemsetAsync(d_->cell_sys, 0xff, 4 * NC, stream_), "memset", err);
+    if (st) return st;
+    st = check(cudaMemsetAsync(d_->blk_sys, 0xff, 4 * NCH, stream_), "memset", err);
+    if (st) return st;
+    hp_.assign(NS, SysParams{});
+    slot_rlist_.assign(NS, 0.0);
+    free_atoms_.clear();
+    free_cells_.clear();
+    free_atoms_[0] = NA;
+    free_cells_[0] = NC;
+    free_tab_.assign(opt.max_types_total, 1);
+    slot_tab_size_.assign(NS, 0);
+    dirty_map_ = true;
+    return sync(err);
+}
+
+static bool take_range(std::map<int64_t, int64_t>& fr, int64_t len, int64_t& at) {
+    for (auto it = fr.begin(); it != fr.end(); ++it) {
+        if (it->second >= len) {
+            at = it->first;
+            int64_t rest = it->second - len;
+            fr.erase(it);
+            if (rest > 0) fr[at + len] = rest;
+            return true;
+        }
+    }
+    return false;
+}
+
+static void give_range(std::map<int64_t, int64_t>& fr, int64_t at, int64_t len) {
+    auto it = fr.emplace(at, len).first;
+    auto nx = std::next(it);
+    if (nx != fr.end() && it->first + it->second == nx->first) {
+        it->second += nx->second;
+        fr.erase(nx);
+    }
+    if (it != fr.begin()) {
+        auto pv = std::prev(it);
+        if (pv->first + pv->second == it->first) {
+            pv->second += it->second;
+            fr.erase(it);
+        }
+    }
+}
+
+// Cell grid at rcut + skin: n_d = floor(L_d / rlist) (Atoms::divide_into_cells,
+// src/atoms/neighbour_list.rs:45-57, evaluated at the list radius).
+static void cell_grid(const SlotDesc& d, double rlist, int nc[3]) {
+    for (int a = 0; a < 3; ++a) {
+        double L = d.h[4 * a];
+        double q = std::floor(L / rlist);
+        nc[a] = q < 1.0 ? 1 : (q > 2000.0 ? 2000 : (int)q);
+    }
+}
+
+static double slot_rlist(const SlotDesc& d) {
+    double rc = 0.0;
+    for (auto& e : d.table)
+        if (e.present && e.rcut > rc) rc = e.rcut;
+    return rc + d.skin;
+}
+
+bool Engine::fits(const SlotDesc& d) const {
+    int nc[3];
+    cell_grid(d, slot_rlist(d), nc);
+    int64_t ncell = (int64_t)nc[0] * nc[1] * nc[2] + 1;
+    bool a = false, c = false;
+    for (auto& kv : free_atoms_) a |= kv.second >= d.n;
+    for (auto& kv : free_cells_) c |= kv.second >= ncell;
+    int free_tab = 0, run = 0;
+    for (int v : free_tab_) {
+        run = v ? run + 1 : 0;
+        free_tab = std::max(free_tab, run);
+    }
+    int slots = 0;
+    for (auto& p : hp_) slots += !p.active;
+    return a && c && slots > 0 && free_tab >= d.n_types * d.n_types;
+}
+
+int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* pos, const double* vel,
+                     const double* force, std::string& err) {
+    if (d.n <= 0) {
+        err = "no atoms defined";
+        return -PIS_ERR_NO_ATOMS;
+    }
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            if (a != b && d.h[3 * a + b] != 0.0) {
+                err = "only orthorhombic boxes are supported (tilt factors must be zero)";
+                return -PIS_ERR_UNSUPPORTED;
+            }
+    for (int a = 0; a < 3; ++a)
+        if (!d.pbc[a]) {
+            err = "only fully periodic boxes are supported";
+            return -PIS_ERR_UNSUPPORTED;
+        }
+    const int nt = d.n_types;
+    if (nt < 1 || (int)d.table.size() != nt * nt || (int)d.masses.size() < nt) {
+        err = "pair table / masses do not match the number of types";
+        return -PIS_ERR_INVALID_ARGUMENT;
+    }
+    double rlist = slot_rlist(d);
+    if (rlist <= d.skin) {
+        err = "no pair potential defined";
+        return -PIS_ERR_MISSING_POTENTIAL;
+    }
+    for (int a = 0; a < 3; ++a) {
+        double L = d.h[4 * a];
+        if (!(L > 2.0 * rlist)) {
+            err = "box edge " + std::to_string(L) + " is not longer than 2 (rcut + skin) = " +
+                  std::to_string(2.0 * rlist);
+            return -PIS_ERR_BOX_TOO_SMALL;
+        }
+    }
+    for (int64_t k = 0; k < d.n; ++k)
+        if (type_ids[k] < 1 || type_ids[k] > nt) {
+            err = "atom type " + std::to_string(type_ids[k]) + " out of range";
+            return -PIS_ERR_INVALID_ATOM_TYPE;
+        }
+    int slot = -1;
+    for (int s = 0; s < opt_.max_slots; ++s)
+        if (!hp_[s].active) {
+            slot = s;
+            break;
+        }
+    if (slot < 0) {
+        err = "no free slot";
+        return -PIS_ERR_NO_MEMORY;
+    }
+    int nc[3];
+    cell_grid(d, rlist, nc);
+    int64_t ncell = (int64_t)nc[0] * nc[1] * nc[2];
+    int64_t a0 = 0, c0 = 0;
+    if (!take_range(free_atoms_, d.n, a0)) {
+        err = "not enough free atom capacity in the pool";
+        return -PIS_ERR_NO_MEMORY;
+    }
+    if (!take_range(free_cells_, ncell + 1, c0)) {
+        give_range(free_atoms_, a0, d.n);
+        err = "not enough free cell capacity in the pool";
+        return -PIS_ERR_NO_MEMORY;
+    }
+    int tab0 = -1;
+    {
+        int need = nt * nt, run = 0;
+        for (int k = 0; k < (int)free_tab_.size(); ++k) {
+            run = free_tab_[k] ? run + 1 : 0;
+            if (run == need) {
+                tab0 = k - need + 1;
+                break;
+            }
+        }
+        if (tab0 < 0) {
+            give_range(free_atoms_, a0, d.n);
+            give_range(free_cells_, c0, ncell + 1);
+            err = "pair table capacity exhausted";
+            return -PIS_ERR_NO_MEMORY;
+        }
+        for (int k = 0; k < need; ++k) free_tab_[tab0 + k] = 0;
+    }
+    slot_tab_size_[slot] = nt * nt;
+
+    // pair table
+    std::vector<LJDev> tab((size_t)nt * nt);
+    for (int k = 0; k < nt * nt; ++k) {
+        const LJHost& e = d.table[k];
+        LJDev& t = tab[k];
+        std::memset(&t, 0, sizeof(t));
+        t.present = e.present;
+        if (!e.present) continue;
+        // exactly the reference's per-pair constants: 4.0*eps, 24.0*eps, sigma.powi(2),
+        // u_cut from (sigma/rcut).powi(2) (src/potentials/lennard_jones.rs:33-55)
+        t.eps4 = 4.0 * e.epsilon;
+        t.eps24 = 24.0 * e.epsilon;
+        t.sigma2 = e.sigma * e.sigma;
+        t.rcut = e.rcut;
+        double rc2 = e.rcut * e.rcut;
+        t.rc2_lo = rc2 * (1.0 - 1e-12);
+        t.rc2_hi = rc2 * (1.0 + 1e-12);
+        double ucut = 0.0;
+        if (e.shift) {
+            double q = e.sigma / e.rcut;
+            double ci2 = q * q;
+            double ca = ci2 * (ci2 * ci2);
+            double cr = ca * ca;
+            ucut = 4.0 * e.epsilon * (cr - ca);
+        }
+        t.ucut = ucut;
+        t.feps4 = (float)t.eps4;
+        t.feps24 = (float)t.eps24;
+        t.fsigma2 = (float)t.sigma2;
+        t.frc2 = (float)rc2;
+        t.fucut = (float)ucut;
+    }
+    pis_status st = check(cudaMemcpyAsync(d_->tab + tab0, tab.data(), sizeof(LJDev) * tab.size(),
+                                          cudaMemcpyHostToDevice, stream_),
+                          "table upload", err);
+    if (st) return -st;
+
+    SysParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.a0 = a0;
+    p.c0 = c0;
+    p.n = (int32_t)d.n;
+    p.active = 1;
+    p.nt = nt;
+    p.tab0 = tab0;
+    for (int a = 0; a < 3; ++a) {
+        p.nc[a] = nc[a];
+        p.pbc[a] = 1;
+        p.h[a] = d.h[4 * a];
+    }
+    // h^-1 by adjugate / determinant, the reference's 3x3 inverse (src/simulation_box.rs:13)
+    {
+        const double* m = d.h;
+        double m11 = m[4] * m[8] - m[7] * m[5];
+        double det = m[0] * m11 - m[1] * (m[3] * m[8] - m[6] * m[5]) + m[2] * (m[3] * m[7] - m[6] * m[4]);
+        p.hinv[0] = m11 / det;
+        p.hinv[1] = (m[0] * m[8] - m[6] * m[2]) / det;
+        p.hinv[2] = (m[0] * m[4] - m[3] * m[1]) / det;
+    }
+    for (int a = 0; a < 3; ++a) {
+        p.cs[a] = p.h[a] / nc[a];
+        p.fcs[a] = (float)p.cs[a];
+    }
+    p.half_skin2 = 0.25 * d.skin * d.skin;
+    p.dt = d.dt;
+    p.dt2 = d.dt * d.dt;
+    double rl = rlist * (1.0 + 1e-5);
+    p.frlist2 = (float)(rl * rl);
+    // chunks
+    p.nch = (int32_t)((d.n + opt_.blk - 1) / opt_.blk);
+    p.ch0 = 0;  // assigned by the block map
+    hp_[slot] = p;
+    slot_rlist_[slot] = rlist;
+
+    // atom state: AoS (x,y,z per atom) -> double4 with the type (pos.w) and mass (vel.w)
+    std::vector<double4> hpos(d.n), hvel(d.n), hfrc(d.n);
+    std::vector<int32_t> hid(d.n);
+    for (int64_t k = 0; k < d.n; ++k) {
+        int t0 = type_ids[k] - 1;
+        double w;
+        int32_t hi = t0, lo = 0;
+        uint64_t bits = ((uint64_t)(uint32_t)hi << 32) | (uint32_t)lo;
+        std::memcpy(&w, &bits, 8);
+        hpos[k] = make_double4(pos[3 * k], pos[3 * k + 1], pos[3 * k + 2], w);
+        double m = d.masses[t0];
+        hvel[k] = vel ? make_double4(vel[3 * k], vel[3 * k + 1], vel[3 * k + 2], m) : make_double4(0, 0, 0, m);
+        hfrc[k] = force ? make_double4(force[3 * k], force[3 * k + 1], force[3 * k + 2], 0.0) : make_double4(0, 0, 0, 0);
+        hid[k] = (int32_t)k;
+    }
+    SysState ss;
+    std::memset(&ss, 0, sizeof(ss));
+    ss.cur = 0;
+    ss.rebuild = 1;
+    std::vector<int32_t> csys(ncell + 1, slot);
+#define CP(dst, src, bytes)                                                                             \
+    do {                                                                                                \
+        st = check(cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyHostToDevice, stream_), "upload", err); \
+        if (st) return -st;                                                                             \
+    } while (0)
+    CP(d_->pos[0] + a0, hpos.data(), 32 * d.n);
+    CP(d_->vel[0] + a0, hvel.data(), 32 * d.n);
+    CP(d_->frc + a0, hfrc.data(), 32 * d.n);
+    CP(d_->posb + a0, hpos.data(), 32 * d.n);
+    CP(d_->id[0] + a0, hid.data(), 4 * d.n);
+    st = check(cudaMemsetAsync(d_->acc[0] + a0, 0, 32 * d.n, stream_), "upload", err);
+    if (st) return -st;
+    st = check(cudaMemsetAsync(d_->cellof + a0, 0, 4 * d.n, stream_), "upload", err);
+    if (st) return -st;
+    st = check(cudaMemsetAsync(d_->nn + a0, 0, 4 * d.n, stream_), "upload", err);
+    if (st) return -st;
+    st = check(cudaMemsetAsync(d_->cell_count + c0, 0, 4 * (ncell + 1), stream_), "upload", err);
+    if (st) return -st;
+    CP(d_->cell_sys + c0, csys.data(), 4 * (ncell + 1));
+    CP(d_->st + slot, &ss, sizeof(ss));
+#undef CP
+    dirty_map_ = true;
+    st = rebuild_block_map(err);
+    if (st) return -st;
+    st = sync(err);
+    if (st) return -st;
+    return slot;
+}
+
+void Engine::remove_slot(int slot) {
+    if (slot < 0 || slot >= opt_.max_slots || !hp_[slot].active) return;
+    SysParams& p = hp_[slot];
+    int64_t ncell = (int64_t)p.nc[0] * p.nc[1] * p.nc[2];
+    give_range(free_atoms_, p.a0, p.n);
+    give_range(free_cells_, p.c0, ncell + 1);
+    for (int k = 0; k < slot_tab_size_[slot]; ++k) free_tab_[p.tab0 + k] = 1;
+    std::vector<int32_t> csys(ncell + 1, -1);
+    cudaMemcpyAsync(d_->cell_sys + p.c0, csys.data(), 4 * (ncell + 1), cudaMemcpyHostToDevice, stream_);
+    p.active = 0;
+    dirty_map_ = true;
+    std::string err;
+    rebuild_block_map(err);
+    cudaStreamSynchronize(stream_);
+}
+
+int Engine::n_active() const {
+    int k = 0;
+    for (auto& p : hp_) k += p.active;
+    return k;
+}
+
+// Chunk table: every active slot gets ceil(n / blk) consecutive chunks; the grid is always
+// max_chunks blocks so captured graphs stay valid when slots come and go.
+pis_status Engine::rebuild_block_map(std::string& err) {
+    if (!dirty_map_) return PIS_OK;
+    std::vector<int32_t> bs(max_chunks_, -1), bf(max_chunks_, 0);
+    int64_t c = 0;
+    for (int s = 0; s < opt_.max_slots; ++s) {
+        SysParams& p = hp_[s];
+        if (!p.active) continue;
+        p.ch0 = (int32_t)c;
+        for (int k = 0; k < p.nch; ++k, ++c) {
+            bs[c] = s;
+            bf[c] = (int32_t)(p.a0 + (int64_t)k * opt_.blk);
+        }
+    }
+    pis_status st = check(cudaMemcpyAsync(d_->blk_sys, bs.data(), 4 * max_chunks_, cudaMemcpyHostToDevice, stream_),
+                          "block map", err);
+    if (st) return st;
+    st = check(cudaMemcpyAsync(d_->blk_first, bf.data(), 4 * max_chunks_, cudaMemcpyHostToDevice, stream_),
+               "block map", err);
+    if (st) return st;
+    st = check(cudaMemcpyAsync(d_->sp, hp_.data(), sizeof(SysParams) * hp_.size(), cudaMemcpyHostToDevice, stream_),
+               "params", err);
+    if (st) return st;
+    // host staging vectors must outlive the async copies
+    st = check(cudaStreamSynchronize(stream_), "block map", err);
+    dirty_map_ = false;
+    return st;
+}
+
+pis_status Engine::sync(std::string& err) { return check(cudaStreamSynchronize(stream_), "stream sync", err); }
+
+pis_status Engine::set_dt(int slot, double dt, std::string& err) {
+    SysParams& p = hp_[slot];
+    if (p.dt == dt) return PIS_OK;
+    p.dt = dt;
+    p.dt2 = dt * dt;
+    pis_status st = check(cudaMemcpyAsync(d_->sp + slot, &p, sizeof(SysParams), cudaMemcpyHostToDevice, stream_),
+                          "params", err);
+    if (st) return st;
+    return sync(err);
+}
+
+pis_status Engine::set_steps(int slot, int64_t steps, std::string& err) {
+    pis_status st = check(cudaMemcpyAsync(&d_->st[slot].steps_left, &steps, 8, cudaMemcpyHostToDevice, stream_),
+                          "steps", err);
+    if (st) return st;
+    return sync(err);
+}
+
+void Engine::enqueue_rebuild(bool respect) {
+    const DP& P = *d_;
+    int r = respect ? 1 : 0;
+    LAUNCH(k_bin, (unsigned)max_chunks_, opt_.blk, P, r);
+    LAUNCH(k_scan, (unsigned)opt_.max_slots, SCAN_THREADS, P, r);
+    LAUNCH(k_scatter, (unsigned)max_chunks_, opt_.blk, P, r);
+    unsigned gcells = (unsigned)((opt_.max_cells * 32 + 255) / 256);
+    LAUNCH(k_gather, gcells, 256, P, (int64_t)opt_.max_cells, r);
+    if (half_)
+        LAUNCH(k_build<true>, (unsigned)max_chunks_, opt_.blk, P, r);
+    else
+        LAUNCH(k_build<false>, (unsigned)max_chunks_, opt_.blk, P, r);
+}
+
+void Engine::enqueue_step(bool respect, cudaEvent_t* ev) {
+    const DP& P = *d_;
+    int r = respect ? 1 : 0;
+    const bool mixed = opt_.precision == PIS_PRECISION_MIXED;
+    if (ev) cudaEventRecord(ev[0], stream_);
+    if (mixed)
+        LAUNCH(k_integrate1<true>, (unsigned)max_chunks_, opt_.blk, P);
+    else
+        LAUNCH(k_integrate1<false>, (unsigned)max_chunks_, opt_.blk, P);
+    if (ev) cudaEventRecord(ev[1], stream_);
+    enqueue_rebuild(respect);
+    if (ev) cudaEventRecord(ev[2], stream_);
+    if (mixed)
+        LAUNCH(k_force_mixed, (unsigned)max_chunks_, opt_.blk, P, r);
+    else if (half_)
+        LAUNCH(k_force_fp64<false>, (unsigned)max_chunks_, opt_.blk, P, r);
+    else
+        LAUNCH(k_force_fp64<true>, (unsigned)max_chunks_, opt_.blk, P, r);
+    if (ev) cudaEventRecord(ev[3], stream_);
+    LAUNCH(k_integrate2<true>, (unsigned)max_chunks_, opt_.blk, P, r);
+    if (ev) cudaEventRecord(ev[4], stream_);
+    LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 0);
+    if (ev) cudaEventRecord(ev[5], stream_);
+}
+
+void Engine::enqueue_potential() {
+    const DP& P = *d_;
+    LAUNCH(k_mark_rebuild, (unsigned)((opt_.max_slots + 127) / 128), 128, P);
+    LAUNCH(k_zero_forces, (unsigned)max_chunks_, opt_.blk, P);
+    enqueue_rebuild(false);
+    if (opt_.precision == PIS_PRECISION_MIXED)
+        LAUNCH(k_force_mixed, (unsigned)max_chunks_, opt_.blk, P, 0);
+    else if (half_)
+        LAUNCH(k_force_fp64<false>, (unsigned)max_chunks_, opt_.blk, P, 0);
+    else
+        LAUNCH(k_force_fp64<true>, (unsigned)max_chunks_, opt_.blk, P, 0);
+    LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 1);
+}
+
+pis_status Engine::compute_potential(std::string& err) {
+    pis_status st = rebuild_block_map(err);
+    if (st) return st;
+    enqueue_potential();
+    st = check(cudaGetLastError(), "launch", err);
+    if (st) return st;
+    return reduce_state(true, err);
+}
+
+pis_status Engine::reduce_state(bool virial, std::string& err) {
+    pis_status st = rebuild_block_map(err);
+    if (st) return st;
+    const DP& P = *d_;
+    std::vector<int32_t> wv(opt_.max_slots, virial ? 1 : 0);
+    for (int s = 0; s < opt_.max_slots; ++s)
+        if (hp_[s].active) {
+            st = check(cudaMemcpyAsync(&d_->st[s].want_virial, &wv[s], 4, cudaMemcpyHostToDevice, stream_), "flag", err);
+            if (st) return st;
+        }
+    LAUNCH(k_integrate2<false>, (unsigned)max_chunks_, opt_.blk, P, 0);
+    LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 2);
+    int32_t zero = 0;
+    for (int s = 0; s < opt_.max_slots; ++s)
+        if (hp_[s].active) {
+            st = check(cudaMemcpyAsync(&d_->st[s].want_virial, &zero, 4, cudaMemcpyHostToDevice, stream_), "flag", err);
+            if (st) return st;
+        }
+    st = check(cudaGetLastError(), "launch", err);
+    if (st) return st;
+    return sync(err);
+}
+
+void Engine::reset_stage_times() {
+    for (double& v : stage_ms_) v = 0.0;
+    stage_steps_ = 0;
+}
+
+pis_status Engine::run(int64_t k, std::string& err) {
+    pis_status st = rebuild_block_map(err);
+    if (st) return st;
+    const int64_t G = graph_steps_;
+    while (k > 0) {
+        int64_t g = k >= G ? G : k;
+        int64_t key = 2 * g + (instrument_ ? 1 : 0);
+        auto it = graphs_.find(key);
+        if (it == graphs_.end()) {
+            GraphRec rec;
+            if (instrument_) {
+                rec.ev.resize((size_t)(6 * g));
+                for (auto& e : rec.ev) {
+                    st = check(cudaEventCreate(&e), "event", err);
+                    if (st) return st;
+                }
+            }
+            cudaGraph_t graph;
+            st = check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture", err);
+            if (st) return st;
+            int64_t before = g_launches.load();
+            for (int64_t q = 0; q < g; ++q) enqueue_step(true, instrument_ ? rec.ev.data() + 6 * q : nullptr);
+            int64_t captured = g_launches.load() - before;
+            g_launches.fetch_sub(captured);
+            kernels_per_step_ = captured / g;
+            st = check(cudaStreamEndCapture(stream_, &graph), "capture", err);
+            if (st) return st;
+            st = check(cudaGraphInstantiate(&rec.exec, graph, 0), "instantiate", err);
+            cudaGraphDestroy(graph);
+            if (st) return st;
+            it = graphs_.emplace(key, rec).first;
+        }
+        st = check(cudaGraphLaunch(it->second.exec, stream_), "graph launch", err);
+        if (st) return st;
+        g_launches.fetch_add(kernels_per_step_ * g);
+        if (instrument_) {
+            st = sync(err);
+            if (st) return st;
+            for (int64_t q = 0; q < g; ++q)
+                for (int t = 0; t < 5; ++t) {
+                    float ms = 0.f;
+                    st = check(cudaEventElapsedTime(&ms, it->second.ev[6 * q + t], it->second.ev[6 * q + t + 1]),
+                               "event timing", err);
+                    if (st) return st;
+                    stage_ms_[t] += ms;
+                }
+            stage_steps_ += g;
+        }
+        k -= g;
+    }
+    return check(cudaGetLastError(), "run", err);
+}
+
+pis_status Engine::download(int slot, double* pos, double* vel, double* force, std::string& err) {
+    const SysParams& p = hp_[slot];
+    SysState ss;
+    pis_status st = read_state(slot, ss, err);
+    if (st) return st;
+    const int cur = ss.cur;
+    std::vector<double4> hp(p.n), hv(p.n), hf(p.n);
+    std::vector<int32_t> hid(p.n);
+    st = check(cudaMemcpyAsync(hid.data(), d_->id[cur] + p.a0, 4 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "download", err);
+    if (st) return st;
+    if (pos) {
+        st = check(cudaMemcpyAsync(hp.data(), d_->pos[cur] + p.a0, 32 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "download", err);
+        if (st) return st;
+    }
+    if (vel) {
+        st = check(cudaMemcpyAsync(hv.data(), d_->vel[cur] + p.a0, 32 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "download", err);
+        if (st) return st;
+    }
+    if (force) {
+        st = check(cudaMemcpyAsync(hf.data(), d_->frc + p.a0, 32 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "download", err);
+        if (st) return st;
+    }
+    st = sync(err);
+    if (st) return st;
+    for (int k = 0; k < p.n; ++k) {
+        int o = hid[k];
+        if (pos) {
+            pos[3 * o] = hp[k].x;
+            pos[3 * o + 1] = hp[k].y;
+            pos[3 * o + 2] = hp[k].z;
+        }
+        if (vel) {
+            vel[3 * o] = hv[k].x;
+            vel[3 * o + 1] = hv[k].y;
+            vel[3 * o + 2] = hv[k].z;
+        }
+        if (force) {
+            force[3 * o] = hf[k].x;
+            force[3 * o + 1] = hf[k].y;
+            force[3 * o + 2] = hf[k].z;
+        }
+    }
+    return PIS_OK;
+}
+
+pis_status Engine::read_state(int slot, SysState& ss, std::string& err) {
+    pis_status st = check(cudaMemcpyAsync(&ss, d_->st + slot, sizeof(SysState), cudaMemcpyDeviceToHost, stream_), "state", err);
+    if (st) return st;
+    return sync(err);
+}
+
+pis_status Engine::read_states(std::vector<SysState>& out, std::string& err) {
+    out.resize(opt_.max_slots);
+    pis_status st = check(cudaMemcpyAsync(out.data(), d_->st, sizeof(SysState) * opt_.max_slots,
+                                          cudaMemcpyDeviceToHost, stream_), "state", err);
+    if (st) return st;
+    return sync(err);
+}
+
+pis_status Engine::read_pe_history(int slot, int64_t n, double* out, std::string& err) {
+    SysState ss;
+    pis_status st = read_state(slot, ss, err);
+    if (st) return st;
+    if (n > opt_.hist || n > ss.steps_done) {
+        err = "energy history holds fewer steps than requested";
+        return PIS_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<double> ring(opt_.hist);
+    st = check(cudaMemcpyAsync(ring.data(), d_->pe_hist + (int64_t)slot * opt_.hist, 8 * opt_.hist,
+                               cudaMemcpyDeviceToHost, stream_), "history", err);
+    if (st) return st;
+    st = sync(err);
+    if (st) return st;
+    for (int64_t q = 0; q < n; ++q) out[q] = ring[(ss.steps_done - n + q) % opt_.hist];
+    return PIS_OK;
+}
+
+pis_status Engine::list_entries(int slot, int64_t& total, std::string& err) {
+    const SysParams& p = hp_[slot];
+    std::vector<int32_t> nn(p.n);
+    pis_status st = check(cudaMemcpyAsync(nn.data(), d_->nn + p.a0, 4 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "nn", err);
+    if (st) return st;
+    st = sync(err);
+    if (st) return st;
+    total = 0;
+    for (int32_t v : nn) total += v;
+    return PIS_OK;
+}
+
+pis_status Engine::neighbour_sets(int slot, std::vector<int64_t>& offsets, std::vector<int32_t>& idx,
+                                  std::string& err) {
+    const SysParams& p = hp_[slot];
+    SysState ss;
+    pis_status st = read_state(slot, ss, err);
+    if (st) return st;
+    if (!d_->keep) {
+        st = check(cudaMalloc(&d_->keep, (size_t)npad_ * cap_), "keep mask", err);
+        if (st) return st;
+    }
+    LAUNCH(k_keep, (unsigned)max_chunks_, opt_.blk, *d_, slot);
+    st = check(cudaGetLastError(), "keep", err);
+    if (st) return st;
+    std::vector<int32_t> nn(p.n), id(p.n);
+    st = check(cudaMemcpyAsync(nn.data(), d_->nn + p.a0, 4 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "nn", err);
+    if (st) return st;
+    st = check(cudaMemcpyAsync(id.data(), d_->id[ss.cur] + p.a0, 4 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "id", err);
+    if (st) return st;
+    int32_t maxnn = 0;
+    st = sync(err);
+    if (st) return st;
+    for (int32_t v : nn) maxnn = std::max(maxnn, v);
+    std::vector<uint32_t> ent((size_t)maxnn * p.n);
+    std::vector<uint8_t> kp((size_t)maxnn * p.n);
+    for (int k = 0; k < maxnn; ++k) {
+        st = check(cudaMemcpyAsync(ent.data() + (size_t)k * p.n, d_->nbr + (int64_t)k * npad_ + p.a0, 4 * (size_t)p.n,
+                                   cudaMemcpyDeviceToHost, stream_), "nbr", err);
+        if (st) return st;
+        st = check(cudaMemcpyAsync(kp.data() + (size_t)k * p.n, d_->keep + (int64_t)k * npad_ + p.a0, (size_t)p.n,
+                                   cudaMemcpyDeviceToHost, stream_), "keep", err);
+        if (st) return st;
+    }
+    st = sync(err);
+    if (st) return st;
+    std::vector<std::vector<int32_t>> sets(p.n);
+    for (int i = 0; i < p.n; ++i)
+        for (int k = 0; k < nn[i]; ++k) {
+            size_t q = (size_t)k * p.n + i;
+            if (!kp[q]) continue;
+            int j = (int)(ent[q] & JMASK) - (int)p.a0;
+            sets[id[i]].push_back(id[j]);
+            if (half_) sets[id[j]].push_back(id[i]);
+        }
+    offsets.assign(p.n + 1, 0);
+    idx.clear();
+    for (int i = 0; i < p.n; ++i) {
+        std::sort(sets[i].begin(), sets[i].end());
+        idx.insert(idx.end(), sets[i].begin(), sets[i].end());
+        offsets[i + 1] = (int64_t)idx.size();
+    }
+    return PIS_OK;
+}
+
+pis_status Engine::scale_velocities(int slot, const double* m, std::string& err) {
+    LAUNCH(k_scale_vel, (unsigned)max_chunks_, opt_.blk, *d_, slot, m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8]);
+    pis_status st = check(cudaGetLastError(), "scale velocities", err);
+    if (st) return st;
+    return sync(err);
+}
+
+pis_status Engine::scale_box(int slot, const double* m, std::string& err) {
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            if (a != b && m[3 * a + b] != 0.0) {
+                err = "box scaling must keep the box orthorhombic (diagonal matrix)";
+                return PIS_ERR_UNSUPPORTED;
+            }
+    SysParams& p = hp_[slot];
+    double nh[3] = {m[0] * p.h[0], m[4] * p.h[1], m[8] * p.h[2]};
+    double rl = slot_rlist_[slot];
+    for (int a = 0; a < 3; ++a)
+        if (!(nh[a] > 2.0 * rl)) {
+            err = "scaled box is shorter than 2 (rcut + skin)";
+            return PIS_ERR_BOX_TOO_SMALL;
+        }
+    LAUNCH(k_scale_pos, (unsigned)max_chunks_, opt_.blk, *d_, slot, p.hinv[0], p.hinv[1], p.hinv[2], nh[0], nh[1], nh[2]);
+    // new h and h^-1; the cell grid keeps its counts, the cell edge follows the box
+    for (int a = 0; a < 3; ++a) {
+        p.h[a] = nh[a];
+        int ncnew = (int)std::floor(nh[a] / rl);
+        (void)ncnew;
+        p.cs[a] = nh[a] / p.nc[a];
+        p.fcs[a] = (float)p.cs[a];
+    }
+    p.hinv[0] = (p.h[1] * p.h[2]) / (p.h[0] * (p.h[1] * p.h[2]));
+    p.hinv[1] = (p.h[0] * p.h[2]) / (p.h[0] * (p.h[1] * p.h[2]));
+    p.hinv[2] = (p.h[0] * p.h[1]) / (p.h[0] * (p.h[1] * p.h[2]));
+    for (int a = 0; a < 3; ++a)
+        if (p.cs[a] < rl) {
+            err = "box shrank below the cell size; re-create the state to re-grid";
+            return PIS_ERR_UNSUPPORTED;
+        }
+    pis_status st = check(cudaMemcpyAsync(d_->sp + slot, &p, sizeof(SysParams), cudaMemcpyHostToDevice, stream_), "params", err);
+    if (st) return st;
+    int32_t one = 1;
+    st = check(cudaMemcpyAsync(&d_->st[slot].rebuild, &one, 4, cudaMemcpyHostToDevice, stream_), "params", err);
+    if (st) return st;
+    return sync(err);
+}
+
+}  // namespace pis

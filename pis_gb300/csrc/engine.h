@@ -1,0 +1,188 @@
+// engine.h - host interface of the packed multi-system MD engine (GB300, sm_103a).
+//
+// One Engine owns a pool of device memory that holds any number of independent periodic
+// Lennard-Jones systems ("slots") packed back to back: atoms of slot s occupy a contiguous
+// atom range, its cells a contiguous cell range. Every kernel runs over the whole pool in one
+// launch; blocks map to (slot, chunk of atoms) through a device-side table, so the same
+// captured CUDA graph serves one 2M-atom system, 512 replicas, or a changing set of served
+// jobs. Per-slot device state (rebuild flag, steps left, energies) lives in device memory so a
+// multi-step graph needs no host round trip.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <map>
+
+#include "pis_gpu.h"
+
+namespace pis {
+
+// One entry of a dense per-slot type-pair table (both (ti,tj) and (tj,ti) filled).
+struct LJHost {
+    double epsilon = 0, sigma = 0, rcut = 0;
+    int present = 0;
+    int shift = 1;
+};
+
+struct SlotDesc {
+    int64_t n = 0;
+    int n_types = 1;
+    std::vector<LJHost> table;      // n_types * n_types
+    std::vector<double> masses;     // per type
+    double h[9] = {0};              // row-major box matrix (must be diagonal)
+    int pbc[3] = {1, 1, 1};
+    double skin = 0.3;
+    double dt = 0.005;
+};
+
+// Device-side per-slot parameters (read-only inside kernels).
+struct SysParams {
+    int64_t a0;        // first atom of the slot
+    int64_t c0;        // first entry of the slot's cell arrays (ncells + 1 entries)
+    int32_t n;         // atoms
+    int32_t active;
+    int32_t nt;        // types
+    int32_t tab0;      // first entry in the global pair table
+    int32_t nc[3];     // cells per axis
+    int32_t pbc[3];
+    int32_t ch0, nch;  // chunk range of the slot
+    double h[3];       // diagonal of h
+    double hinv[3];    // diagonal of h^-1 (adjugate / determinant, as the reference)
+    double cs[3];      // cell edge
+    double half_skin2; // (skin / 2)^2
+    double dt, dt2;    // dt, dt*dt
+    float fcs[3];
+    float frlist2;     // FP32 list radius squared, padded so the FP32 test is a superset
+};
+
+// Device-side pair parameters: FP64 quantities computed exactly as the reference does per pair,
+// plus FP32 copies for the mixed path.
+struct LJDev {
+    double eps4, eps24, sigma2, rcut, rc2_lo, rc2_hi, ucut;
+    float feps4, feps24, fsigma2, frc2, fucut;
+    int32_t present;
+};
+
+// Mutable per-slot device state.
+struct SysState {
+    int32_t cur;          // which of the two atom buffer sets is current
+    int32_t rebuild;      // neighbour list must be rebuilt in this step
+    int32_t flags;        // FLAG_* bits
+    int32_t want_virial;  // compute sum_i r_i F_i^T in the next reductions
+    int64_t steps_left;   // steps still to take; a slot at 0 is frozen during run()
+    int64_t steps_done;
+    int64_t rebuilds;
+    double pe, ke;
+    double virial[9];
+};
+
+enum : int32_t { FLAG_NAN = 1, FLAG_LIST_OVERFLOW = 2, FLAG_CELL_OVERFLOW = 4 };
+
+struct PoolOptions {
+    int precision = PIS_PRECISION_FP64;
+    int list_kind = PIS_LIST_DEFAULT;
+    int blk = 256;             // atoms per chunk = threads per block of every atom kernel
+    int list_cap = 0;          // per-atom neighbour capacity (0 = from density)
+    int64_t max_atoms = 0;
+    int max_slots = 1;
+    int64_t max_cells = 0;     // total cell entries (including one sentinel per slot)
+    int max_types_total = 64;  // pair-table entries
+    int hist = 1024;           // per-slot energy history ring
+};
+
+class Engine {
+  public:
+    Engine();
+    ~Engine();
+    Engine(const Engine&) = delete;
+    Engine& operator=(const Engine&) = delete;
+
+    pis_status init(const PoolOptions& opt, std::string& err);
+    // Place a system in the pool. Returns the slot id (>= 0) or a negative pis_status.
+    int add_slot(const SlotDesc& d, const int32_t* type_ids, const double* pos, const double* vel,
+                 const double* force, std::string& err);
+    void remove_slot(int slot);
+    // Ask whether a system of this shape fits in the free space right now.
+    bool fits(const SlotDesc& d) const;
+    int64_t list_cap() const { return cap_; }
+    int precision() const { return opt_.precision; }
+    bool half_list() const { return half_; }
+
+    pis_status set_dt(int slot, double dt, std::string& err);
+    pis_status set_steps(int slot, int64_t steps, std::string& err);
+    // Zero forces, rebuild lists, evaluate forces + PE (+ KE and virial) for every active slot.
+    pis_status compute_potential(std::string& err);
+    // Run k velocity-Verlet steps on every active slot with steps_left > 0 (graph chunks).
+    pis_status run(int64_t k, std::string& err);
+    // KE and virial of every active slot at the current state.
+    pis_status reduce_state(bool virial, std::string& err);
+    pis_status sync(std::string& err);
+
+    pis_status download(int slot, double* pos, double* vel, double* force, std::string& err);
+    pis_status read_state(int slot, SysState& st, std::string& err);
+    pis_status read_states(std::vector<SysState>& st, std::string& err);
+    // Last n energies of the slot's history ring (oldest first).
+    pis_status read_pe_history(int slot, int64_t n, double* out, std::string& err);
+    pis_status neighbour_sets(int slot, std::vector<int64_t>& offsets, std::vector<int32_t>& idx,
+                              std::string& err);
+    pis_status list_entries(int slot, int64_t& total, std::string& err);
+    pis_status scale_velocities(int slot, const double* m, std::string& err);
+    pis_status scale_box(int slot, const double* m, std::string& err);
+    const SysParams& params(int slot) const { return hp_[slot]; }
+    int n_active() const;
+    cudaStream_t stream() const { return stream_; }
+    // Kernel launches issued (graph launches count every captured kernel).
+    static int64_t launches();
+    // Per-kernel-name launch counts (for bench accounting).
+    int64_t graph_kernels_per_step() const { return kernels_per_step_; }
+    // Stage timing with CUDA events captured into the step graphs (integrate1, list rebuild,
+    // force, integrate2, reductions); costs one host sync per graph launch while enabled.
+    void set_instrument(bool on) { instrument_ = on; }
+    void reset_stage_times();
+    const double* stage_ms() const { return stage_ms_; }
+    int64_t stage_steps() const { return stage_steps_; }
+    void set_graph_steps(int64_t g) { graph_steps_ = g > 0 ? g : 1; }
+
+    struct DevPtrs;  // device pointer bundle passed by value to every kernel
+
+  private:
+    pis_status upload_tables(std::string& err);
+    pis_status rebuild_block_map(std::string& err);
+    void enqueue_step(bool respect_steps, cudaEvent_t* ev);
+    void enqueue_rebuild(bool respect_steps);
+    void enqueue_potential();
+    pis_status check(cudaError_t e, const char* what, std::string& err);
+
+    PoolOptions opt_;
+    bool half_ = true;
+    int64_t cap_ = 0;
+    int64_t npad_ = 0;
+    int64_t max_chunks_ = 0;
+    cudaStream_t stream_ = nullptr;
+    std::vector<SysParams> hp_;
+    std::vector<LJHost> slot_tables_flat_;
+    std::vector<int> slot_tab_size_;
+    std::vector<double> slot_rlist_;
+    // free-space bookkeeping (first fit over atom and cell index ranges)
+    std::map<int64_t, int64_t> free_atoms_, free_cells_;
+    std::vector<int> free_tab_;
+    // device allocations
+    void* mem_ = nullptr;
+    size_t mem_bytes_ = 0;
+    DevPtrs* d_ = nullptr;
+    struct GraphRec {
+        cudaGraphExec_t exec = nullptr;
+        std::vector<cudaEvent_t> ev;  // 6 per step when instrumented
+    };
+    std::map<int64_t, GraphRec> graphs_;
+    bool instrument_ = false;
+    int64_t graph_steps_ = 50;
+    double stage_ms_[5] = {0, 0, 0, 0, 0};
+    int64_t stage_steps_ = 0;
+    int64_t kernels_per_step_ = 0;
+    bool dirty_map_ = true;
+};
+
+}  // namespace pis

@@ -1,0 +1,324 @@
+// pis_gpu.cu - single-system C ABI (include/pis_gpu.h) over the packed engine.
+//
+// A pis_gpu_ctx is the GPU counterpart of one PotentialManager bound to one Atoms state: the
+// pair table is fixed at creation, set_state places the atoms in a one-slot engine pool, and
+// compute_potential / verlet_step_nve run on the device with the state kept resident.
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "pis_gpu.h"
+
+struct pis_gpu_ctx {
+    std::vector<pis::LJHost> table;
+    int n_types = 0;
+    double skin = 0.3;
+    int precision = PIS_PRECISION_FP64;
+    int list_kind = PIS_LIST_DEFAULT;
+    std::unique_ptr<pis::Engine> eng;
+    int slot = -1;
+    int64_t n = 0;
+    double dt = 0.0;
+    std::string err;
+};
+
+namespace {
+
+pis_status fail(pis_gpu_ctx* ctx, pis_status st, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return st;
+}
+
+bool have_state(pis_gpu_ctx* ctx) { return ctx && ctx->eng && ctx->slot >= 0; }
+
+// Per-atom list capacity from the mean density: 1.6x the expected full-list count + 32.
+int list_capacity(int64_t n, const double* h_rowmajor, double rlist) {
+    double vol = std::fabs(h_rowmajor[0] * h_rowmajor[4] * h_rowmajor[8]);
+    double rho = vol > 0 ? (double)n / vol : 0.0;
+    double full = rho * 4.0 / 3.0 * M_PI * rlist * rlist * rlist;
+    double cap = 1.6 * full + 32.0;
+    if (cap > 4096) cap = 4096;
+    return ((int)std::ceil(cap) + 7) / 8 * 8;
+}
+
+pis_status flags_to_status(pis_gpu_ctx* ctx, const pis::SysState& ss) {
+    if (ss.flags & pis::FLAG_NAN) return fail(ctx, PIS_ERR_NAN_DETECTED, "NaN detected in positions or energies");
+    if (ss.flags & pis::FLAG_LIST_OVERFLOW)
+        return fail(ctx, PIS_ERR_LIST_OVERFLOW, "neighbour list capacity exceeded; results are invalid");
+    return PIS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pis_status pis_gpu_create(const pis_lj_pair* table, int32_t n_pairs, int32_t n_types, double skin,
+                          int32_t precision, pis_gpu_ctx** out) {
+    if (!out) return PIS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (n_types < 1 || n_types > 8) return PIS_ERR_INVALID_ARGUMENT;
+    if (n_pairs < 1 || !table) return PIS_ERR_MISSING_POTENTIAL;
+    if (!(skin >= 0.0)) return PIS_ERR_INVALID_ARGUMENT;
+    if (precision != PIS_PRECISION_FP64 && precision != PIS_PRECISION_MIXED) return PIS_ERR_INVALID_ARGUMENT;
+    auto* ctx = new pis_gpu_ctx();
+    ctx->n_types = n_types;
+    ctx->skin = skin;
+    ctx->precision = precision;
+    ctx->table.assign((size_t)n_types * n_types, pis::LJHost{});
+    for (int k = 0; k < n_pairs; ++k) {
+        const pis_lj_pair& p = table[k];
+        if (p.ti < 1 || p.tj < 1 || p.ti > n_types || p.tj > n_types || !(p.rcut > 0.0) || !(p.sigma > 0.0)) {
+            delete ctx;
+            return PIS_ERR_INVALID_ARGUMENT;
+        }
+        pis::LJHost e;
+        e.epsilon = p.epsilon;
+        e.sigma = p.sigma;
+        e.rcut = p.rcut;
+        e.present = 1;
+        e.shift = p.shift;
+        // the reference looks pairs up by (min, max) type (src/potentials/potential.rs:181-192)
+        ctx->table[(size_t)(p.ti - 1) * n_types + (p.tj - 1)] = e;
+        ctx->table[(size_t)(p.tj - 1) * n_types + (p.ti - 1)] = e;
+    }
+    *out = ctx;
+    return PIS_OK;
+}
+
+pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t force_block) {
+    if (!ctx) return PIS_ERR_INVALID_ARGUMENT;
+    if (list_kind < PIS_LIST_DEFAULT || list_kind > PIS_LIST_FULL)
+        return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown list kind");
+    if (force_block != 0 && force_block != 256)
+        return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "force block size must be 256");
+    if (ctx->precision == PIS_PRECISION_MIXED && list_kind == PIS_LIST_HALF)
+        return fail(ctx, PIS_ERR_UNSUPPORTED, "the mixed-precision path uses a full list");
+    ctx->list_kind = list_kind;
+    return PIS_OK;
+}
+
+pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_ids, const double* masses_per_type,
+                             const double* pos, const double* vel, const double* force, const double* h_colmajor,
+                             const uint8_t* pbc) {
+    if (!ctx) return PIS_ERR_INVALID_ARGUMENT;
+    if (n <= 0) return fail(ctx, PIS_ERR_NO_ATOMS, "no atoms defined");
+    if (!type_ids || !masses_per_type || !pos || !h_colmajor)
+        return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "null state array");
+    pis::SlotDesc d;
+    d.n = n;
+    d.n_types = ctx->n_types;
+    d.table = ctx->table;
+    d.masses.assign(masses_per_type, masses_per_type + ctx->n_types);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) d.h[3 * r + c] = h_colmajor[3 * c + r];
+    for (int a = 0; a < 3; ++a) d.pbc[a] = pbc ? (pbc[a] ? 1 : 0) : 1;
+    d.skin = ctx->skin;
+    d.dt = ctx->dt > 0 ? ctx->dt : 0.005;
+    double rc = 0.0;
+    for (auto& e : d.table)
+        if (e.present && e.rcut > rc) rc = e.rcut;
+    double rlist = rc + ctx->skin;
+
+    ctx->eng.reset();
+    ctx->slot = -1;
+    ctx->n = 0;
+    auto eng = std::make_unique<pis::Engine>();
+    pis::PoolOptions opt;
+    opt.precision = ctx->precision;
+    opt.list_kind = ctx->list_kind;
+    opt.max_atoms = n;
+    opt.max_slots = 1;
+    int64_t ncell = 1;
+    for (int a = 0; a < 3; ++a) {
+        double q = std::floor(d.h[4 * a] / rlist);
+        ncell *= (int64_t)(q < 1 ? 1 : (q > 2000 ? 2000 : q));
+    }
+    opt.max_cells = ncell + 1;
+    opt.max_types_total = ctx->n_types * ctx->n_types;
+    opt.list_cap = list_capacity(n, d.h, rlist);
+    std::string err;
+    pis_status st = eng->init(opt, err);
+    if (st) return fail(ctx, st, err);
+    int slot = eng->add_slot(d, type_ids, pos, vel, force, err);
+    if (slot < 0) return fail(ctx, (pis_status)(-slot), err);
+    ctx->eng = std::move(eng);
+    ctx->slot = slot;
+    ctx->n = n;
+    return PIS_OK;
+}
+
+pis_status pis_gpu_compute_potential(pis_gpu_ctx* ctx, double* pe_out, double* forces) {
+    if (!have_state(ctx)) return fail(ctx, PIS_ERR_STATE, "no atoms uploaded");
+    std::string err;
+    pis_status st = ctx->eng->compute_potential(err);
+    if (st) return fail(ctx, st, err);
+    pis::SysState ss;
+    st = ctx->eng->read_state(ctx->slot, ss, err);
+    if (st) return fail(ctx, st, err);
+    if (pe_out) *pe_out = ss.pe;
+    if (forces) {
+        st = ctx->eng->download(ctx->slot, nullptr, nullptr, forces, err);
+        if (st) return fail(ctx, st, err);
+    }
+    return flags_to_status(ctx, ss);
+}
+
+pis_status pis_gpu_verlet_step_nve(pis_gpu_ctx* ctx, double dt, int64_t n_steps, double* pe_out) {
+    if (!have_state(ctx)) return fail(ctx, PIS_ERR_STATE, "no atoms uploaded");
+    if (n_steps < 0 || !(dt == dt)) return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "bad step count or dt");
+    std::string err;
+    pis_status st = ctx->eng->set_dt(ctx->slot, dt, err);
+    if (st) return fail(ctx, st, err);
+    ctx->dt = dt;
+    const int64_t chunk = 1000;
+    int64_t done = 0;
+    while (done < n_steps) {
+        int64_t k = std::min(chunk, n_steps - done);
+        st = ctx->eng->set_steps(ctx->slot, k, err);
+        if (st) return fail(ctx, st, err);
+        st = ctx->eng->run(k, err);
+        if (st) return fail(ctx, st, err);
+        pis::SysState ss;
+        st = ctx->eng->read_state(ctx->slot, ss, err);
+        if (st) return fail(ctx, st, err);
+        if (pe_out) {
+            st = ctx->eng->read_pe_history(ctx->slot, k, pe_out + done, err);
+            if (st) return fail(ctx, st, err);
+        }
+        st = flags_to_status(ctx, ss);
+        if (st) return st;
+        done += k;
+    }
+    return PIS_OK;
+}
+
+pis_status pis_gpu_run_timed(pis_gpu_ctx* ctx, double dt, int64_t n_steps, double* device_ms, double* stage_ms) {
+    if (!have_state(ctx)) return fail(ctx, PIS_ERR_STATE, "no atoms uploaded");
+    if (n_steps < 1 || !(dt == dt)) return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "bad step count or dt");
+    std::string err;
+    pis::Engine& e = *ctx->eng;
+    pis_status st = e.set_dt(ctx->slot, dt, err);
+    if (st) return fail(ctx, st, err);
+    ctx->dt = dt;
+    st = e.set_steps(ctx->slot, n_steps, err);
+    if (st) return fail(ctx, st, err);
+    e.set_instrument(stage_ms != nullptr);
+    e.reset_stage_times();
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, e.stream());
+    st = e.run(n_steps, err);
+    cudaEventRecord(b, e.stream());
+    cudaError_t ce = cudaEventSynchronize(b);
+    float ms = 0.f;
+    if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    e.set_instrument(false);
+    if (st) return fail(ctx, st, err);
+    if (ce != cudaSuccess) return fail(ctx, PIS_ERR_CUDA, cudaGetErrorString(ce));
+    if (device_ms) *device_ms = ms;
+    if (stage_ms)
+        for (int t = 0; t < 5; ++t) stage_ms[t] = e.stage_ms()[t];
+    pis::SysState ss;
+    st = e.read_state(ctx->slot, ss, err);
+    if (st) return fail(ctx, st, err);
+    return flags_to_status(ctx, ss);
+}
+
+pis_status pis_gpu_get_state(pis_gpu_ctx* ctx, double* pos, double* vel, double* force) {
+    if (!have_state(ctx)) return fail(ctx, PIS_ERR_STATE, "no atoms uploaded");
+    std::string err;
+    pis_status st = ctx->eng->download(ctx->slot, pos, vel, force, err);
+    return st ? fail(ctx, st, err) : PIS_OK;
+}
+
+pis_status pis_gpu_reductions(pis_gpu_ctx* ctx, double* ke, double* virial) {
+    if (!have_state(ctx)) return fail(ctx, PIS_ERR_STATE, "no atoms uploaded");
+    std::string err;
+    pis_status st = ctx->eng->reduce_state(virial != nullptr, err);
+    if (st) return fail(ctx, st, err);
+    pis::SysState ss;
+    st = ctx->eng->read_state(ctx->slot, ss, err);
+    if (st) return fail(ctx, st, err);
+    if (ke) *ke = ss.ke;
+    if (virial)
+        for (int q = 0; q < 9; ++q) virial[q] = ss.virial[q];
+    return PIS_OK;
+}
+
+pis_status pis_gpu_neighbour_list(pis_gpu_ctx* ctx, int64_t* offsets, int32_t* idx, int64_t cap, int64_t* total) {
+    if (!have_state(ctx)) return fail(ctx, PIS_ERR_STATE, "no atoms uploaded");
+    if (!offsets) return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "offsets is null");
+    std::string err;
+    pis::SysState ss;
+    pis_status st = ctx->eng->read_state(ctx->slot, ss, err);
+    if (st) return fail(ctx, st, err);
+    if (ss.rebuild) {
+        // no list for the current positions yet: evaluate once (builds it)
+        st = ctx->eng->compute_potential(err);
+        if (st) return fail(ctx, st, err);
+    }
+    std::vector<int64_t> off;
+    std::vector<int32_t> id;
+    st = ctx->eng->neighbour_sets(ctx->slot, off, id, err);
+    if (st) return fail(ctx, st, err);
+    std::memcpy(offsets, off.data(), sizeof(int64_t) * off.size());
+    if (idx) std::memcpy(idx, id.data(), sizeof(int32_t) * (size_t)std::min<int64_t>(cap, (int64_t)id.size()));
+    if (total) *total = (int64_t)id.size();
+    return PIS_OK;
+}
+
+pis_status pis_gpu_scale_velocities(pis_gpu_ctx* ctx, const double* m) {
+    if (!have_state(ctx)) return fail(ctx, PIS_ERR_STATE, "no atoms uploaded");
+    if (!m) return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "null matrix");
+    std::string err;
+    pis_status st = ctx->eng->scale_velocities(ctx->slot, m, err);
+    return st ? fail(ctx, st, err) : PIS_OK;
+}
+
+pis_status pis_gpu_scale_box(pis_gpu_ctx* ctx, const double* m) {
+    if (!have_state(ctx)) return fail(ctx, PIS_ERR_STATE, "no atoms uploaded");
+    if (!m) return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "null matrix");
+    std::string err;
+    pis_status st = ctx->eng->scale_box(ctx->slot, m, err);
+    return st ? fail(ctx, st, err) : PIS_OK;
+}
+
+pis_status pis_gpu_get_stats(pis_gpu_ctx* ctx, pis_gpu_stats* out) {
+    if (!have_state(ctx)) return fail(ctx, PIS_ERR_STATE, "no atoms uploaded");
+    if (!out) return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "null output");
+    std::string err;
+    pis::SysState ss;
+    pis_status st = ctx->eng->read_state(ctx->slot, ss, err);
+    if (st) return fail(ctx, st, err);
+    int64_t entries = 0;
+    st = ctx->eng->list_entries(ctx->slot, entries, err);
+    if (st) return fail(ctx, st, err);
+    std::memset(out, 0, sizeof(*out));
+    out->n_atoms = ctx->n;
+    out->steps = ss.steps_done;
+    out->rebuilds = ss.rebuilds;
+    out->list_entries = entries;
+    out->list_capacity = (int32_t)ctx->eng->list_cap();
+    const pis::SysParams& p = ctx->eng->params(ctx->slot);
+    for (int a = 0; a < 3; ++a) out->cells[a] = p.nc[a];
+    out->pe = ss.pe;
+    out->ke = ss.ke;
+    for (int q = 0; q < 9; ++q) out->virial[q] = ss.virial[q];
+    return PIS_OK;
+}
+
+const char* pis_gpu_last_error(const pis_gpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+void pis_gpu_destroy(pis_gpu_ctx* ctx) { delete ctx; }
+
+int64_t pis_gpu_kernel_launches(void) { return pis::Engine::launches(); }
+
+const char* pis_gpu_version(void) { return "pis_gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,66 @@
+"""The C-ABI library builds, loads and exports every symbol its headers declare (no GPU needed:
+nothing here calls into the device)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    syms = []
+    for name in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not name.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", name)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        syms += re.findall(r"\b(pis_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(syms))
+
+
+@pytest.fixture(scope="module")
+def built_lib():
+    from pis_gb300 import build
+    return ctypes.CDLL(build.build())
+
+
+def test_every_declared_symbol_is_exported(built_lib):
+    syms = declared_symbols()
+    assert "pis_gpu_create" in syms and "pis_gpu_verlet_step_nve" in syms
+    missing = [s for s in syms if not hasattr(built_lib, s)]
+    assert not missing, missing
+
+
+def test_ffi_signatures_cover_header():
+    from pis_gb300 import _ffi
+    bound = {name for name, _, _ in _ffi.SIGNATURES}
+    gpu_syms = [s for s in declared_symbols() if s.startswith("pis_gpu_")]
+    assert set(gpu_syms) <= bound
+
+
+def test_version_string(built_lib):
+    built_lib.pis_gpu_version.restype = ctypes.c_char_p
+    assert b"sm_103a" in built_lib.pis_gpu_version()
+
+
+def test_create_validates_without_gpu():
+    from pis_gb300 import _ffi
+    lib = _ffi.lib()
+    h = ctypes.c_void_p()
+    pair = (_ffi.LJPair * 1)(_ffi.LJPair(1, 3, 1.0, 1.0, 2.5, 1))
+    assert lib.pis_gpu_create(pair, 1, 2, 0.3, 0, ctypes.byref(h)) == 1  # type 3 > n_types
+    pair = (_ffi.LJPair * 1)(_ffi.LJPair(1, 1, 1.0, 1.0, 2.5, 1))
+    assert lib.pis_gpu_create(pair, 1, 1, 0.3, 7, ctypes.byref(h)) == 1  # unknown precision
+    assert lib.pis_gpu_create(pair, 1, 1, 0.3, 0, ctypes.byref(h)) == 0
+    lib.pis_gpu_destroy(h)
+
+
+def test_product_never_imports_oracle():
+    for dirpath, _, files in os.walk(os.path.join(ROOT, "pis_gb300")):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cpp", ".h", ".cuh")):
+                text = open(os.path.join(dirpath, f)).read()
+                assert "import oracle" not in text and "from oracle" not in text, f
+                assert "liboracle" not in text, f
