@@ -1,0 +1,337 @@
+"""Benchmark of the PIS LJ MD step on GB300.
+
+Workload (one "step" = one velocity-Verlet NVE step of the hot path: integrate, skin test and
+conditional neighbour-list rebuild, LJ forces/energy, integrate, reductions): the reduced-unit
+LJ liquid with N = 2,048,000 atoms (80^3 FCC cells, rho* = 0.8442, T* = 0.72, rc = 2.5,
+skin = 0.3, dt* = 0.005), melted from the lattice with seeded Maxwell-Boltzmann velocities.
+Synthetic data: the reference ships no benchmark inputs; this is its own lattice generator's
+layout with this project's seeded velocities.
+
+`value` is the mixed-precision path's whole-job atom-steps/s (device-timed, state resident in
+HBM); `fp64` reports the plain FP64 GPU path on the same state; `e2e` repeats the mixed
+measurement through the C ABI with host buffers (upload, force, K steps with per-step energy
+read-back, download). `--impl reference` times the CPU restatement of the reference's
+multithreaded manager (LJVParallelManager) on the same workload with all host cores.
+
+Multi-GPU: replicas only (each rank advances its own independent system; no collective on the
+data path); rank 0 prints the JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+TABLE = {(1, 1): (1.0, 1.0, 2.5)}
+RHO, TSTAR, DT, SKIN = 0.8442, 0.72, 0.005, 0.3
+HBM_FALLBACK_GBS = 6800.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=1000)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--cells", type=int, default=80, help="FCC cells per edge (80 -> 2,048,000 atoms)")
+    p.add_argument("--equil", type=int, default=300, help="unreported mixed-precision melt steps")
+    p.add_argument("--fp64-steps", type=int, default=200)
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    return p.parse_args()
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("PIS_BENCH_GLOO") is None else "gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_state(cells, seed):
+    from pis_gb300.lattice import lj_liquid
+    pos, vel, L = lj_liquid(cells, RHO, TSTAR, seed)
+    return pos, vel, L
+
+
+def cpu_sample(pos, vel, L, steps, threads):
+    """Oracle restatement of the reference's multithreaded manager, timed on host cores."""
+    import oracle
+    n = len(pos)
+    s = oracle.System(pos, np.ones(n, np.int32), [1.0], np.eye(3) * L, TABLE, velocities=vel)
+    s.compute_potential(manager=oracle.PARALLEL, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.verlet_step_nve(DT, manager=oracle.PARALLEL, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return n * steps / dt, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    threads = oracle.num_threads_available()
+    pos, vel, L = make_state(args.cells, 1)
+    n = len(pos)
+    # bounded sample: each timed step of the 2M-atom system costs ~0.5 s on 16 cores
+    k = max(1, min(args.steps, 5))
+    w = max(0, min(args.warmup, 1))
+    import oracle as O
+    s = O.System(pos, np.ones(n, np.int32), [1.0], np.eye(3) * L, TABLE, velocities=vel)
+    s.compute_potential(manager=O.PARALLEL, nthreads=threads)
+    for _ in range(w):
+        s.verlet_step_nve(DT, manager=O.PARALLEL, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(k):
+        s.verlet_step_nve(DT, manager=O.PARALLEL, nthreads=threads)
+    el = time.perf_counter() - t0
+    v = n * k / el
+    line = {
+        "impl": "reference", "metric": "atom-steps/s", "value": v, "unit": "atom-steps/s", "n_gpus": world,
+        "steps": k, "warmup": w, "ms_per_step": el / k * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args, n),
+        "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{k} NVE steps of the {n}-atom liquid after {w} warm-up step(s), "
+                                   "LJVParallelManager restated with OpenMP (oracle/pis_oracle.cpp)"},
+        "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, n):
+    return {"workload": f"LJ liquid N={n} (FCC {args.cells}^3 melted), rho*={RHO}, T*={TSTAR}, rc=2.5, "
+                        f"skin={SKIN}, dt*={DT}, NVE",
+            "atoms": n, "rho": RHO, "t_star": TSTAR, "rcut": 2.5, "skin": SKIN, "dt": DT,
+            "equilibration_steps": args.equil, "l2": "inputs larger than L2 (state + list ~2 GB resident)",
+            "parallelism": f"replicas{args.gpus}" if args.gpus > 1 else "single"}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    from pis_gb300 import build as B
+    B.build()
+    from pis_gb300.potentials import GpuContext, kernel_launches
+
+    pos, vel, L = make_state(args.cells, 1 + rank)
+    n = len(pos)
+    types = np.ones(n, np.int32)
+    h = np.eye(3) * L
+    hbm_peak, peak_src = peaks()
+
+    # ---- mixed precision (the headline form) -------------------------------------------------
+    mix = GpuContext(TABLE, 1, skin=SKIN, precision="mixed")
+    mix.set_state(pos, types, [1.0], h, velocities=vel)
+    mix.compute_potential(want_forces=False)
+    mix.run_timed(DT, max(args.equil, 1))          # melt (unreported)
+    melt_pos, melt_vel, _ = mix.get_state()
+    mix.set_state(melt_pos, types, [1.0], h, velocities=melt_vel)
+    mix.compute_potential(want_forces=False)
+    mix.run_timed(DT, max(args.warmup, 3))         # warm-up
+    barrier(world)
+    launches0 = kernel_launches()
+    with ClockSampler(local) as clk:
+        ms, _ = mix.run_timed(DT, args.steps)
+    launches = kernel_launches() - launches0
+    ms = max_over_ranks(ms, world)
+    st = mix.stats()
+    value = world * n * args.steps / (ms * 1e-3)
+    # stage breakdown (events captured in the graphs), separate pass of the same length
+    ms_s, stages = mix.run_timed(DT, args.steps, stages=True)
+    stages_per = stages / args.steps
+    list_per_atom = st["list_entries"] / n
+    # force-kernel algorithmic bytes: list entries + own cell-relative position + nn + force write
+    force_bytes = n * (4 + 16 + 32) + st["list_entries"] * 4
+    force_ms = stages_per[2]
+    achieved = force_bytes / (force_ms * 1e-3) / 1e9
+    pairs_per_step = 27.6 * n  # in-cutoff unordered pairs per step at rho* = 0.8442
+    traffic = read_traffic("force_mixed", n)
+
+    # ---- plain FP64 on the same state --------------------------------------------------------
+    f64 = GpuContext(TABLE, 1, skin=SKIN, precision="fp64")
+    f64.set_state(melt_pos, types, [1.0], h, velocities=melt_vel)
+    pe64, F64 = f64.compute_potential()
+    f64.run_timed(DT, 3)
+    k64 = max(3, min(args.fp64_steps, args.steps))
+    ms64, _ = f64.run_timed(DT, k64)
+    ms64 = max_over_ranks(ms64, world)
+    v64 = world * n * k64 / (ms64 * 1e-3)
+    mixf = GpuContext(TABLE, 1, skin=SKIN, precision="mixed")
+    mixf.set_state(melt_pos, types, [1.0], h, velocities=melt_vel)
+    pem, Fm = mixf.compute_potential()
+    force_rms = float(np.sqrt(np.sum((Fm - F64) ** 2) / np.sum(F64 ** 2)))
+    pe_rel = abs(pem - pe64) / abs(pe64)
+    mixf.close()
+    f64.close()
+
+    # ---- end to end through the C ABI with host buffers -------------------------------------
+    k_e2e = args.steps
+    e2e_pos = np.ascontiguousarray(melt_pos)
+    e2e_vel = np.ascontiguousarray(melt_vel)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    mix.set_state(e2e_pos, types, [1.0], h, velocities=e2e_vel)
+    mix.compute_potential(want_forces=False)
+    pe_steps = mix.verlet_step_nve(DT, k_e2e)
+    out_pos, out_vel, out_f = mix.get_state()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_value = world * n * k_e2e / e2e_s
+    h2d = n * 3 * 8 * 2 + n * 4
+    d2h = n * 3 * 8 * 3 + k_e2e * 8
+    mix.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        oracle.build()
+        threads = oracle.num_threads_available()
+        v_cpu, el = cpu_sample(melt_pos, melt_vel, L, 2, threads)
+        cpu = {"value": v_cpu, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+               "sample": f"2 NVE steps of the same {n}-atom liquid ({el:.1f} s), LJVParallelManager restated "
+                         "with OpenMP (oracle/pis_oracle.cpp)"}
+
+    if rank == 0:
+        line = {
+            "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32-pair/f64-accumulate",
+            "data": "synthetic", "config": workload_config(args, n),
+            "precision": "mixed",
+            "pairs_per_s": world * pairs_per_step * args.steps / (ms * 1e-3),
+            "fp64": {"value": v64, "unit": "atom-steps/s", "steps": k64, "ms_per_step": ms64 / k64,
+                     "dtype": "f64", "list": "half"},
+            "mixed_over_fp64": value / v64,
+            "error_vs_fp64": {"force_rms_rel": force_rms, "pe_rel": pe_rel},
+            "stages_ms_per_step": {"integrate1": stages_per[0], "rebuild": stages_per[1], "force": stages_per[2],
+                                   "integrate2": stages_per[3], "reduce": stages_per[4]},
+            "rebuilds_per_step": None,
+            "list_entries_per_atom": list_per_atom,
+            "roofline": {"bound": "hbm", "kernel": "k_force_mixed", "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_src,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": force_bytes},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d / k_e2e,
+                    "d2h_bytes_per_step": d2h / k_e2e, "seconds": e2e_s,
+                    "path": "pis_gpu_set_state + compute_potential + verlet_step_nve(K, per-step PE) + get_state"},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def read_traffic(kernel, n):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, scaled to n atoms."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    try:
+        with open(path) as fh:
+            for line in fh:
+                f = line.split()
+                if len(f) >= 3 and f[0] == kernel:
+                    return float(f[1]) * n / float(f[2])
+    except OSError:
+        pass
+    return None
+
+
+if __name__ == "__main__":
+    main()

@@ -1179,25 +1179,25 @@ void Engine::enqueue_step(bool respect, cudaEvent_t* ev) {
     const DP& P = *d_;
     int r = respect ? 1 : 0;
     const bool mixed = opt_.precision == PIS_PRECISION_MIXED;
-    if (ev) cudaEventRecord(ev[0], stream_);
+    if (ev) cudaEventRecordWithFlags(ev[0], stream_, cudaEventRecordExternal);
     if (mixed)
         LAUNCH(k_integrate1<true>, (unsigned)max_chunks_, opt_.blk, P);
     else
         LAUNCH(k_integrate1<false>, (unsigned)max_chunks_, opt_.blk, P);
-    if (ev) cudaEventRecord(ev[1], stream_);
+    if (ev) cudaEventRecordWithFlags(ev[1], stream_, cudaEventRecordExternal);
     enqueue_rebuild(respect);
-    if (ev) cudaEventRecord(ev[2], stream_);
+    if (ev) cudaEventRecordWithFlags(ev[2], stream_, cudaEventRecordExternal);
     if (mixed)
         LAUNCH(k_force_mixed, (unsigned)max_chunks_, opt_.blk, P, r);
     else if (half_)
         LAUNCH(k_force_fp64<false>, (unsigned)max_chunks_, opt_.blk, P, r);
     else
         LAUNCH(k_force_fp64<true>, (unsigned)max_chunks_, opt_.blk, P, r);
-    if (ev) cudaEventRecord(ev[3], stream_);
+    if (ev) cudaEventRecordWithFlags(ev[3], stream_, cudaEventRecordExternal);
     LAUNCH(k_integrate2<true>, (unsigned)max_chunks_, opt_.blk, P, r);
-    if (ev) cudaEventRecord(ev[4], stream_);
+    if (ev) cudaEventRecordWithFlags(ev[4], stream_, cudaEventRecordExternal);
     LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 0);
-    if (ev) cudaEventRecord(ev[5], stream_);
+    if (ev) cudaEventRecordWithFlags(ev[5], stream_, cudaEventRecordExternal);
 }
 
 void Engine::enqueue_potential() {

@@ -163,7 +163,8 @@ def test_two_type_mixture(oracle_lib, cuda_lib):
 
 def test_missing_cross_pair_is_skipped(oracle_lib, cuda_lib):
     # types 1 and 2 with no (1,2) entry: the reference prints and skips those pairs
-    s = liquid(nc=5, rho=0.8)
+    # (6 FCC cells -> 3 reference cells at rcut 3.0, so the reference stencil is exact)
+    s = liquid(nc=6, rho=0.8)
     n = len(s["pos"])
     s["types"] = (np.arange(n) % 2 + 1).astype(np.int32)
     s["masses"] = np.array([1.0, 2.0])
