@@ -88,9 +88,14 @@ typedef struct {
 pis_status pis_gpu_create(const pis_lj_pair* table, int32_t n_pairs, int32_t n_types, double skin,
                           int32_t precision, pis_gpu_ctx** out);
 
-/* Select a measured variant: list kind (pis_list_kind) and threads per block for the force
- * kernel (0 = default). Takes effect at the next set_state. */
-pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t force_block);
+/* Variant flags for pis_gpu_set_options. */
+#define PIS_OPT_FP64_FAST 1  /* FP64 forces with fused multiply-adds and a Newton reciprocal; the
+                              * cutoff is still decided with the reference's exact arithmetic */
+#define PIS_OPT_MIXED_KAHAN 2 /* mixed path: compensated FP32 sums instead of FP64 batch sums */
+
+/* Select a measured variant: list kind (pis_list_kind) and PIS_OPT_* flags. Takes effect at the
+ * next set_state. */
+pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flags);
 
 /* Upload the Atoms state (src/atoms/new.rs:9-17). force may be NULL (zero forces, as the
  * data-file reader leaves them, src/readers/input_file/commands.rs:367). The only

@@ -43,6 +43,7 @@ struct Engine::DevPtrs {
     double4* frc;
     double4* posb;
     float4* prel;
+    float4* prelb;
     int32_t* cellof;
     int32_t* lcell;
     int32_t* slotin;
@@ -169,6 +170,10 @@ __device__ __forceinline__ float4 cell_relative(const SysParams& sp, double4 p, 
 // step kernels
 // ---------------------------------------------------------------------------------------------
 // First half of PotentialManager::verlet_step_nve (src/potentials/potential.rs:16-24).
+// a_t = F/m is not recomputed: acc holds it from the last force evaluation (same bits, one
+// FP64 division fewer per component - the FP64 pipe is the scarce unit on GB300).
+// EXACT (FP64 path): the reference's rounding sequence and wrap of every atom every step.
+// Mixed path: FP64 with fused multiply-adds, and only atoms that left the box are wrapped.
 template <bool MIXED>
 __global__ void k_integrate1(const DP P) {
     int s, i;
@@ -177,33 +182,48 @@ __global__ void k_integrate1(const DP P) {
     const SysParams& sp = P.sp[s];
     SysState& st = P.st[s];
     const int cur = st.cur;
-    double4 p = P.pos[cur][i];
-    double4 v = P.vel[cur][i];
-    double4 f = P.frc[i];
-    const double m = v.w;
-    // Atoms::current_acceleration: a = 0 + F/m (src/atoms/properties.rs:32-39)
-    double ax = __dadd_rn(0.0, __ddiv_rn(f.x, m));
-    double ay = __dadd_rn(0.0, __ddiv_rn(f.y, m));
-    double az = __dadd_rn(0.0, __ddiv_rn(f.z, m));
-    // positions += v*dt + (a*0.5)*dt^2
-    double x = __dadd_rn(p.x, __dadd_rn(__dmul_rn(v.x, sp.dt), __dmul_rn(__dmul_rn(ax, 0.5), sp.dt2)));
-    double y = __dadd_rn(p.y, __dadd_rn(__dmul_rn(v.y, sp.dt), __dmul_rn(__dmul_rn(ay, 0.5), sp.dt2)));
-    double z = __dadd_rn(p.z, __dadd_rn(__dmul_rn(v.z, sp.dt), __dmul_rn(__dmul_rn(az, 0.5), sp.dt2)));
-    x = wrap_axis(x, sp.h[0], sp.hinv[0]);
-    y = wrap_axis(y, sp.h[1], sp.hinv[1]);
-    z = wrap_axis(z, sp.h[2], sp.hinv[2]);
+    const double4 p = P.pos[cur][i];
+    const double4 v = P.vel[cur][i];
+    const double4 a = P.acc[cur][i];
+    double x, y, z;
+    if (!MIXED) {
+        // positions += v*dt + (a*0.5)*dt^2, then s = h^-1 x; s -= floor(s); x = h s
+        x = __dadd_rn(p.x, __dadd_rn(__dmul_rn(v.x, sp.dt), __dmul_rn(__dmul_rn(a.x, 0.5), sp.dt2)));
+        y = __dadd_rn(p.y, __dadd_rn(__dmul_rn(v.y, sp.dt), __dmul_rn(__dmul_rn(a.y, 0.5), sp.dt2)));
+        z = __dadd_rn(p.z, __dadd_rn(__dmul_rn(v.z, sp.dt), __dmul_rn(__dmul_rn(a.z, 0.5), sp.dt2)));
+        x = wrap_axis(x, sp.h[0], sp.hinv[0]);
+        y = wrap_axis(y, sp.h[1], sp.hinv[1]);
+        z = wrap_axis(z, sp.h[2], sp.hinv[2]);
+    } else {
+        const double hdt2 = 0.5 * sp.dt2;
+        x = p.x + fma(v.x, sp.dt, a.x * hdt2);
+        y = p.y + fma(v.y, sp.dt, a.y * hdt2);
+        z = p.z + fma(v.z, sp.dt, a.z * hdt2);
+        x = (x < 0.0) ? x + sp.h[0] : ((x >= sp.h[0]) ? x - sp.h[0] : x);
+        y = (y < 0.0) ? y + sp.h[1] : ((y >= sp.h[1]) ? y - sp.h[1] : y);
+        z = (z < 0.0) ? z + sp.h[2] : ((z >= sp.h[2]) ? z - sp.h[2] : z);
+    }
     P.pos[cur][i] = make_double4(x, y, z, p.w);
-    P.acc[cur][i] = make_double4(ax, ay, az, 0.0);
     if (P.zero_forces) P.frc[i] = make_double4(0.0, 0.0, 0.0, 0.0);
-    // skin test: rebuild when any atom moved more than skin/2 since the last build
-    double4 b = P.posb[i];
-    double dx = min_image_axis(x - b.x, sp.h[0], sp.hinv[0]);
-    double dy = min_image_axis(y - b.y, sp.h[1], sp.hinv[1]);
-    double dz = min_image_axis(z - b.z, sp.h[2], sp.hinv[2]);
-    double d2 = dx * dx + dy * dy + dz * dz;
-    if (!(d2 <= sp.half_skin2)) st.rebuild = 1;  // NaN also requests a rebuild
-    if (x != x || y != y || z != z) atomicOr(&st.flags, FLAG_NAN);
-    if (MIXED) P.prel[i] = cell_relative(sp, make_double4(x, y, z, 0.0), P.cellof[i], type_of(p.w));
+    // skin test: rebuild when any atom moved more than skin/2 since the last build. The
+    // minimum image is only taken when the plain difference fails the test (moved far, or
+    // crossed the periodic boundary).
+    const double4 b = P.posb[i];
+    double dx = x - b.x, dy = y - b.y, dz = z - b.z;
+    double d2 = fma(dx, dx, fma(dy, dy, dz * dz));
+    if (!(d2 <= sp.half_skin2)) {
+        dx = min_image_axis(dx, sp.h[0], sp.hinv[0]);
+        dy = min_image_axis(dy, sp.h[1], sp.hinv[1]);
+        dz = min_image_axis(dz, sp.h[2], sp.hinv[2]);
+        d2 = fma(dx, dx, fma(dy, dy, dz * dz));
+        if (!(d2 <= sp.half_skin2)) st.rebuild = 1;  // NaN also requests a rebuild
+        if (x != x || y != y || z != z) atomicOr(&st.flags, FLAG_NAN);
+    }
+    if (MIXED) {
+        // cell-relative FP32 coordinates = build-time ones + displacement since the build
+        const float4 q = P.prelb[i];
+        P.prel[i] = make_float4(q.x + (float)dx, q.y + (float)dy, q.z + (float)dz, q.w);
+    }
 }
 
 // Counting sort, pass 1: cell of every atom (reference binning of src/atoms/neighbour_list.rs:
@@ -336,15 +356,25 @@ __global__ void k_gather(const DP P, int64_t max_cells, int respect_steps) {
         P.id[dst_set][dst] = myid;
         P.posb[dst] = p;
         P.cellof[dst] = lc;
-        P.prel[dst] = cell_relative(sp, p, lc, type_of(p.w));
+        const float4 q = cell_relative(sp, p, lc, type_of(p.w));
+        P.prel[dst] = q;
+        P.prelb[dst] = q;
     }
 }
 
-// Neighbour-list build at rcut + skin, one thread per atom in cell order. The distance test runs
-// in FP32 on cell-relative coordinates with a radius padded by 1e-5, so the list is a superset
-// of the exact FP64 list; the force kernels apply the exact cutoff. Entry = j | image code << 26,
-// the code giving the cell offset (0, +1, -1 per axis, 2 bits each) that makes the displacement
-// minimum-image at build time.
+// Neighbour-list build at rcut + skin, one thread per atom in cell order (the atoms of a cell
+// are consecutive threads and walk the same neighbour cells, so their loads of prel[j] are
+// broadcasts). The distance test runs in FP32 on cell-relative coordinates with a radius
+// padded by 1e-5, so the list is a superset of the exact FP64 list; the force kernels apply the
+// exact cutoff. Entry = j | image code << 26, the code giving the cell offset (0, +1, -1 per
+// axis, 2 bits each) that makes prel_j - prel_i + offset * cell the minimum-image displacement
+// at build time. Axes with only two cells reach the same neighbour cell through +1 and -1; the
+// generic path keeps, per pair, whichever image is nearer.
+__device__ __forceinline__ int wrapc(int c, int n) {
+    c += (c < 0) ? n : 0;
+    return c - ((c >= n) ? n : 0);
+}
+
 template <bool HALF>
 __global__ void k_build(const DP P, int respect_steps) {
     int s, i;
@@ -361,50 +391,58 @@ __global__ void k_build(const DP P, int respect_steps) {
     const float rl2 = sp.frlist2;
     const int64_t npad = P.npad;
     const int cap = P.cap;
+    const int32_t* __restrict__ cstart = P.cell_start + sp.c0;
+    const float4* __restrict__ prel = P.prel;
+    uint32_t* out = P.nbr + i;
     int cnt = 0;
+    const bool generic = nx < 3 || ny < 3 || nz < 3;
     const int zlo = nz >= 3 ? -1 : 0, ylo = ny >= 3 ? -1 : 0, xlo = nx >= 3 ? -1 : 0;
     for (int oz = zlo; oz <= 1; ++oz) {
-        int z2 = cz + oz;
-        z2 += (z2 < 0) ? nz : 0;
-        z2 -= (z2 >= nz) ? nz : 0;
+        const int z2 = wrapc(cz + oz, nz);
         for (int oy = ylo; oy <= 1; ++oy) {
-            int y2 = cy + oy;
-            y2 += (y2 < 0) ? ny : 0;
-            y2 -= (y2 >= ny) ? ny : 0;
+            const int y2 = wrapc(cy + oy, ny);
             for (int ox = xlo; ox <= 1; ++ox) {
-                int x2 = cx + ox;
-                x2 += (x2 < 0) ? nx : 0;
-                x2 -= (x2 >= nx) ? nx : 0;
+                const int x2 = wrapc(cx + ox, nx);
                 const int nb = (z2 * ny + y2) * nx + x2;
-                const int b0 = P.cell_start[sp.c0 + nb], b1 = P.cell_start[sp.c0 + nb + 1];
-                for (int j = b0; j < b1; ++j) {
-                    if (HALF ? (j <= i) : (j == i)) continue;
-                    const float4 pj = P.prel[j];
-                    float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                    uint32_t code = 0;
-                    // axis x
-                    if (ox != 0) {
-                        float a = dx + csx, b = dx - csx;
-                        bool usep = (nx == 2) ? (fabsf(a) <= fabsf(b)) : (ox > 0);
-                        dx = usep ? a : b;
-                        code |= usep ? 1u : 2u;
+                const int b0 = cstart[nb], b1 = cstart[nb + 1];
+                if (!generic) {
+                    const float sx = ox * csx - pi.x, sy = oy * csy - pi.y, sz = oz * csz - pi.z;
+                    const uint32_t code = (((uint32_t)(ox < 0 ? 2 : ox)) | ((uint32_t)(oy < 0 ? 2 : oy) << 2) |
+                                           ((uint32_t)(oz < 0 ? 2 : oz) << 4))
+                                          << JBITS;
+                    for (int j = b0; j < b1; ++j) {
+                        const float4 pj = prel[j];
+                        const float dx = pj.x + sx, dy = pj.y + sy, dz = pj.z + sz;
+                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        const bool take = (r2 <= rl2) && (HALF ? (j > i) : (j != i));
+                        if (take) {
+                            if (cnt < cap) *out = (uint32_t)j | code;
+                            out += npad;
+                            ++cnt;
+                        }
                     }
-                    if (oy != 0) {
-                        float a = dy + csy, b = dy - csy;
-                        bool usep = (ny == 2) ? (fabsf(a) <= fabsf(b)) : (oy > 0);
-                        dy = usep ? a : b;
-                        code |= (usep ? 1u : 2u) << 2;
-                    }
-                    if (oz != 0) {
-                        float a = dz + csz, b = dz - csz;
-                        bool usep = (nz == 2) ? (fabsf(a) <= fabsf(b)) : (oz > 0);
-                        dz = usep ? a : b;
-                        code |= (usep ? 1u : 2u) << 4;
-                    }
-                    float r2 = dx * dx + dy * dy + dz * dz;
-                    if (r2 <= rl2) {
-                        if (cnt < cap) P.nbr[(int64_t)cnt * npad + i] = (uint32_t)j | (code << JBITS);
-                        ++cnt;
+                } else {
+                    for (int j = b0; j < b1; ++j) {
+                        if (HALF ? (j <= i) : (j == i)) continue;
+                        const float4 pj = prel[j];
+                        float d[3] = {pj.x - pi.x, pj.y - pi.y, pj.z - pi.z};
+                        const int o[3] = {ox, oy, oz}, n[3] = {nx, ny, nz};
+                        const float c3[3] = {csx, csy, csz};
+                        uint32_t code = 0;
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) {
+                            if (o[a] == 0) continue;
+                            const float up = d[a] + c3[a], dn = d[a] - c3[a];
+                            const bool usep = (n[a] == 2) ? (fabsf(up) <= fabsf(dn)) : (o[a] > 0);
+                            d[a] = usep ? up : dn;
+                            code |= (usep ? 1u : 2u) << (2 * a);
+                        }
+                        const float r2 = fmaf(d[0], d[0], fmaf(d[1], d[1], d[2] * d[2]));
+                        if (r2 <= rl2) {
+                            if (cnt < cap) *out = (uint32_t)j | (code << JBITS);
+                            out += npad;
+                            ++cnt;
+                        }
                     }
                 }
             }
@@ -417,10 +455,28 @@ __global__ void k_build(const DP P, int respect_steps) {
     P.nn[i] = cnt;
 }
 
-// FP64 forces, Newton-3 half list: the pair evaluation of LJVOffsetManager
-// (src/potentials/lennard_jones.rs:214-235) - F_i -= f, F_j += f (j's share by FP64 atomics),
-// PE += u. Forces must be zero on entry.
-template <bool FULL>
+// FP64 forces: the pair evaluation of LJVOffsetManager (src/potentials/lennard_jones.rs:214-235),
+// F_i -= f, F_j += f, PE += u.
+//   FULL = false: Newton-3 half list, j's share scattered with FP64 atomics (forces zeroed by
+//     integrate-1). Each lane starts its walk at a different list position so the atoms of one
+//     cell, which share most neighbours, do not hit the same j's force at the same time.
+//   FULL = true: full list, F_i only, no atomics; PE halved at the reduction.
+//   FAST = false: the reference's rounding sequence operation for operation (min-image through
+//     h^-1 and h, x*x+y*y+z*z, true division).
+//   FAST = true: fused multiply-adds, min-image as r - L*rint(r/L), and 1/r^2 by Newton-Raphson
+//     (y <- y + y(1 - r^2 y), twice) from the hardware approximation rcp.approx.f64. Pairs within
+//     a 1e-12 band of rcut are re-tested with the exact reference arithmetic, so the set of
+//     interacting pairs is identical to the reference's.
+__device__ __forceinline__ double rcp_newton(double x) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
+template <bool FULL, bool FAST>
 __global__ void k_force_fp64(const DP P, int respect_steps) {
     __shared__ double sh[32];
     int s, i;
@@ -442,26 +498,63 @@ __global__ void k_force_fp64(const DP P, int respect_steps) {
         double fx = 0.0, fy = 0.0, fz = 0.0;
         const int nn = P.nn[i];
         const int64_t npad = P.npad;
-        for (int k = 0; k < nn; ++k) {
+        int k = FULL ? 0 : (nn > 0 ? (int)(threadIdx.x & 31) % nn : 0);
+        for (int t = 0; t < nn; ++t) {
             const int j = (int)(P.nbr[(int64_t)k * npad + i] & JMASK);
+            if (++k == nn) k = 0;
             const double4 pj = pos[j];
-            double rx = min_image_axis(__dsub_rn(pj.x, pi.x), hx, ix);
-            double ry = min_image_axis(__dsub_rn(pj.y, pi.y), hy, iy);
-            double rz = min_image_axis(__dsub_rn(pj.z, pi.z), hz, iz);
-            double r2 = norm2_ref(rx, ry, rz);
             LJ64 L = P0;
             if (!one_type) {
                 const LJDev& T = tab[type_of(pj.w)];
                 if (!T.present) continue;
                 L = lj64_load(T);
             }
-            double u, c;
-            if (!lj_fp64(L, r2, u, c)) continue;
-            double gx = __dmul_rn(c, rx), gy = __dmul_rn(c, ry), gz = __dmul_rn(c, rz);
-            fx = __dsub_rn(fx, gx);
-            fy = __dsub_rn(fy, gy);
-            fz = __dsub_rn(fz, gz);
-            e = __dadd_rn(e, u);
+            double rx, ry, rz, u, c;
+            if (!FAST) {
+                rx = min_image_axis(__dsub_rn(pj.x, pi.x), hx, ix);
+                ry = min_image_axis(__dsub_rn(pj.y, pi.y), hy, iy);
+                rz = min_image_axis(__dsub_rn(pj.z, pi.z), hz, iz);
+                if (!lj_fp64(L, norm2_ref(rx, ry, rz), u, c)) continue;
+            } else {
+                rx = pj.x - pi.x;
+                ry = pj.y - pi.y;
+                rz = pj.z - pi.z;
+                rx = fma(-hx, rint(rx * ix), rx);
+                ry = fma(-hy, rint(ry * iy), ry);
+                rz = fma(-hz, rint(rz * iz), rz);
+                const double r2 = fma(rx, rx, fma(ry, ry, rz * rz));
+                if (r2 > L.rc2_hi) continue;
+                if (r2 >= L.rc2_lo) {
+                    double qx = min_image_axis(__dsub_rn(pj.x, pi.x), hx, ix);
+                    double qy = min_image_axis(__dsub_rn(pj.y, pi.y), hy, iy);
+                    double qz = min_image_axis(__dsub_rn(pj.z, pi.z), hz, iz);
+                    if (sqrt(norm2_ref(qx, qy, qz)) > L.rcut) continue;
+                }
+                const double inv = rcp_newton(r2);
+                const double s2 = L.sigma2 * inv;
+                const double vdw = s2 * s2 * s2;
+                const double rep = vdw * vdw;
+                u = fma(L.eps4, rep - vdw, -L.ucut);
+                c = L.eps24 * fma(2.0, rep, -vdw) * inv;
+            }
+            double gx, gy, gz;
+            if (!FAST) {
+                gx = __dmul_rn(c, rx);
+                gy = __dmul_rn(c, ry);
+                gz = __dmul_rn(c, rz);
+                fx = __dsub_rn(fx, gx);
+                fy = __dsub_rn(fy, gy);
+                fz = __dsub_rn(fz, gz);
+                e = __dadd_rn(e, u);
+            } else {
+                gx = c * rx;
+                gy = c * ry;
+                gz = c * rz;
+                fx -= gx;
+                fy -= gy;
+                fz -= gz;
+                e += u;
+            }
             if (!FULL) {
                 atomicAdd(&P.frc[j].x, gx);
                 atomicAdd(&P.frc[j].y, gy);
@@ -481,52 +574,77 @@ __global__ void k_force_fp64(const DP P, int respect_steps) {
 }
 
 // Mixed precision forces, full list: FP32 pair arithmetic on cell-relative coordinates
-// (displacement = prel_j - prel_i + image shift), FP32 partial sums over runs of 32 neighbours
-// folded into FP64 accumulators. PE is sum_i sum_j u_ij, halved at the reduction.
-__global__ void k_force_mixed(const DP P, int respect_steps) {
+// (displacement = prel_j - prel_i + image shift). Entries are consumed in batches of 8: the 8
+// list words are loaded first, then the 8 position gathers, so each thread keeps 8 independent
+// loads in flight. Image shifts come from a 64-entry table in shared memory indexed by the
+// entry's code. Pair terms are summed in FP32 over each batch and the batch sums are added in
+// FP64 (ACC = 0), or kept as compensated FP32 sums (ACC = 1, a measured variant) and converted
+// once at the end. PE = sum_i sum_j u_ij, halved at the reduction.
+constexpr int MIX_BATCH = 8;
+
+template <int ACC>
+__global__ void __launch_bounds__(256) k_force_mixed(const DP P, int respect_steps) {
     __shared__ double sh[32];
+    __shared__ float4 shift[64];
     int s, i;
     bool live = atom_of(P, s, i);
     if (s < 0) return;
     if (!slot_runs(P, s, respect_steps)) return;
+    const SysParams& sp = P.sp[s];
+    if (threadIdx.x < 64) {
+        const int c = threadIdx.x;
+        const int bx = c & 3, by = (c >> 2) & 3, bz = (c >> 4) & 3;
+        const float fx = bx == 1 ? 1.f : (bx == 2 ? -1.f : 0.f);
+        const float fy = by == 1 ? 1.f : (by == 2 ? -1.f : 0.f);
+        const float fz = bz == 1 ? 1.f : (bz == 2 ? -1.f : 0.f);
+        shift[c] = make_float4(fx * sp.fcs[0], fy * sp.fcs[1], fz * sp.fcs[2], 0.f);
+    }
+    __syncthreads();
     double e = 0.0;
     if (live) {
-        const SysParams& sp = P.sp[s];
         const float4* __restrict__ prel = P.prel;
         const float4 pi = prel[i];
         const int ti = __float_as_int(pi.w);
         const LJDev* tab = P.tab + sp.tab0 + ti * sp.nt;
         const bool one_type = sp.nt == 1;
-        const LJDev P0 = tab[0];
-        const float csx = sp.fcs[0], csy = sp.fcs[1], csz = sp.fcs[2];
+        const float frc2_0 = tab[0].frc2, fs2_0 = tab[0].fsigma2, fe24_0 = tab[0].feps24, fe4_0 = tab[0].feps4,
+                    fuc_0 = tab[0].fucut;
         double fx = 0.0, fy = 0.0, fz = 0.0;
+        float cx = 0.f, cy = 0.f, cz = 0.f, ce = 0.f;  // compensation terms (ACC = 1)
+        float sx = 0.f, sy = 0.f, sz = 0.f, se = 0.f;  // compensated sums (ACC = 1)
         const int nn = P.nn[i];
         const int64_t npad = P.npad;
-        const uint32_t* __restrict__ nb = P.nbr + i;
-        for (int k0 = 0; k0 < nn; k0 += 32) {
-            const int k1 = min(nn, k0 + 32);
+        const uint32_t* __restrict__ nbp = P.nbr + i;
+        const uint32_t self = (uint32_t)i;
+        for (int k0 = 0; k0 < nn; k0 += MIX_BATCH) {
+            uint32_t ent[MIX_BATCH];
+            const uint32_t* q = nbp + (int64_t)k0 * npad;
+#pragma unroll
+            for (int b = 0; b < MIX_BATCH; ++b) {
+                ent[b] = (k0 + b < nn) ? __ldg(q) : self;
+                q += npad;
+            }
+            float4 pj[MIX_BATCH];
+#pragma unroll
+            for (int b = 0; b < MIX_BATCH; ++b) pj[b] = __ldg(prel + (ent[b] & JMASK));
             float px = 0.f, py = 0.f, pz = 0.f, pe = 0.f;
-#pragma unroll 4
-            for (int k = k0; k < k1; ++k) {
-                const uint32_t ent = __ldg(nb + (int64_t)k * npad);
-                const int j = (int)(ent & JMASK);
-                const uint32_t code = ent >> JBITS;
-                const float4 pj = __ldg(prel + j);
-                float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                dx += (code & 1u) ? csx : ((code & 2u) ? -csx : 0.f);
-                dy += (code & 4u) ? csy : ((code & 8u) ? -csy : 0.f);
-                dz += (code & 16u) ? csz : ((code & 32u) ? -csz : 0.f);
+#pragma unroll
+            for (int b = 0; b < MIX_BATCH; ++b) {
+                const float4 sv = shift[ent[b] >> JBITS];
+                const float dx = (pj[b].x - pi.x) + sv.x;
+                const float dy = (pj[b].y - pi.y) + sv.y;
+                const float dz = (pj[b].z - pi.z) + sv.z;
                 const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                float frc2 = P0.frc2, fs2 = P0.fsigma2, fe24 = P0.feps24, fe4 = P0.feps4, fuc = P0.fucut;
+                float frc2 = frc2_0, fs2 = fs2_0, fe24 = fe24_0, fe4 = fe4_0, fuc = fuc_0;
                 if (!one_type) {
-                    const LJDev& L = tab[__float_as_int(pj.w)];
+                    const LJDev& L = tab[__float_as_int(pj[b].w)];
                     frc2 = L.present ? L.frc2 : -1.f;
                     fs2 = L.fsigma2;
                     fe24 = L.feps24;
                     fe4 = L.feps4;
                     fuc = L.fucut;
                 }
-                if (r2 <= frc2) {
+                if (r2 <= frc2 && r2 > 0.f) {
                     const float inv = __fdividef(1.0f, r2);
                     const float s2 = fs2 * inv;
                     const float s6 = s2 * s2 * s2;
@@ -537,10 +655,32 @@ __global__ void k_force_mixed(const DP P, int respect_steps) {
                     pe += fmaf(fe4 * s6, s6 - 1.0f, -fuc);
                 }
             }
-            fx += (double)px;
-            fy += (double)py;
-            fz += (double)pz;
-            e += (double)pe;
+            if (ACC == 0) {
+                fx += (double)px;
+                fy += (double)py;
+                fz += (double)pz;
+                e += (double)pe;
+            } else {
+                // Kahan summation of the batch sums
+                float y = px - cx, t = sx + y;
+                cx = (t - sx) - y;
+                sx = t;
+                y = py - cy, t = sy + y;
+                cy = (t - sy) - y;
+                sy = t;
+                y = pz - cz, t = sz + y;
+                cz = (t - sz) - y;
+                sz = t;
+                y = pe - ce, t = se + y;
+                ce = (t - se) - y;
+                se = t;
+            }
+        }
+        if (ACC == 1) {
+            fx = (double)sx - (double)cx;
+            fy = (double)sy - (double)cy;
+            fz = (double)sz - (double)cz;
+            e = (double)se - (double)ce;
         }
         P.frc[i] = make_double4(fx, fy, fz, 0.0);
     }
@@ -549,9 +689,12 @@ __global__ void k_force_mixed(const DP P, int respect_steps) {
 }
 
 // Second half of verlet_step_nve (src/potentials/potential.rs:28-30):
-// v += ((a_t + a_tdt) * 0.5) * dt, then chunk partials of KE = sum 0.5 m |v|^2
-// (src/atoms/properties.rs:17-24) and, on request, W = sum r_i F_i^T (:49-51).
-template <bool UPDATE>
+// a_tdt = F/m; v += ((a_t + a_tdt) * 0.5) * dt; acc <- a_tdt (the next step's a_t); then chunk
+// partials of KE = sum 0.5 m |v|^2 (src/atoms/properties.rs:17-24) and, on request,
+// W = sum r_i F_i^T (:49-51). UPDATE = false only refreshes acc = F/m and reduces (after a
+// force evaluation). EXACT keeps the reference's division and rounding order; the mixed path
+// multiplies by the stored 1/m (acc.w) and fuses.
+template <bool UPDATE, bool EXACT>
 __global__ void k_integrate2(const DP P, int respect_steps) {
     __shared__ double sh[32];
     int s, i;
@@ -562,22 +705,36 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
     const SysState& st = P.st[s];
     const int cur = st.cur;
     double ke = 0.0;
-    double w[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     double4 p = make_double4(0, 0, 0, 0), f = p;
     if (live) {
         double4 v = P.vel[cur][i];
+        const double4 a = P.acc[cur][i];
         f = P.frc[i];
         const double m = v.w;
+        double bx, by, bz;
+        if (EXACT) {
+            bx = __dadd_rn(0.0, __ddiv_rn(f.x, m));
+            by = __dadd_rn(0.0, __ddiv_rn(f.y, m));
+            bz = __dadd_rn(0.0, __ddiv_rn(f.z, m));
+        } else {
+            bx = f.x * a.w;
+            by = f.y * a.w;
+            bz = f.z * a.w;
+        }
         if (UPDATE) {
-            double4 a = P.acc[cur][i];
-            double bx = __dadd_rn(0.0, __ddiv_rn(f.x, m));
-            double by = __dadd_rn(0.0, __ddiv_rn(f.y, m));
-            double bz = __dadd_rn(0.0, __ddiv_rn(f.z, m));
-            v.x = __dadd_rn(v.x, __dmul_rn(__dmul_rn(__dadd_rn(a.x, bx), 0.5), sp.dt));
-            v.y = __dadd_rn(v.y, __dmul_rn(__dmul_rn(__dadd_rn(a.y, by), 0.5), sp.dt));
-            v.z = __dadd_rn(v.z, __dmul_rn(__dmul_rn(__dadd_rn(a.z, bz), 0.5), sp.dt));
+            if (EXACT) {
+                v.x = __dadd_rn(v.x, __dmul_rn(__dmul_rn(__dadd_rn(a.x, bx), 0.5), sp.dt));
+                v.y = __dadd_rn(v.y, __dmul_rn(__dmul_rn(__dadd_rn(a.y, by), 0.5), sp.dt));
+                v.z = __dadd_rn(v.z, __dmul_rn(__dmul_rn(__dadd_rn(a.z, bz), 0.5), sp.dt));
+            } else {
+                const double hdt = 0.5 * sp.dt;
+                v.x = fma(a.x + bx, hdt, v.x);
+                v.y = fma(a.y + by, hdt, v.y);
+                v.z = fma(a.z + bz, hdt, v.z);
+            }
             P.vel[cur][i] = v;
         }
+        P.acc[cur][i] = make_double4(bx, by, bz, a.w);
         ke = __dmul_rn(__dmul_rn(0.5, m), norm2_ref(v.x, v.y, v.z));
         if (st.want_virial) p = P.pos[cur][i];
     }
@@ -593,7 +750,6 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
                 if (threadIdx.x == 0) P.vir_part[(int64_t)blockIdx.x * 9 + a * 3 + b] = t;
             }
     }
-    (void)w;
 }
 
 // Per-slot end of a step (or of a force evaluation): deterministic sums of the chunk partials,
@@ -775,7 +931,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         {(void**)&d_->pos[0], 32 * NA}, {(void**)&d_->pos[1], 32 * NA}, {(void**)&d_->vel[0], 32 * NA},
         {(void**)&d_->vel[1], 32 * NA}, {(void**)&d_->acc[0], 32 * NA}, {(void**)&d_->acc[1], 32 * NA},
         {(void**)&d_->id[0], 4 * NA},   {(void**)&d_->id[1], 4 * NA},   {(void**)&d_->frc, 32 * NA},
-        {(void**)&d_->posb, 32 * NA},   {(void**)&d_->prel, 16 * NA},   {(void**)&d_->cellof, 4 * NA},
+        {(void**)&d_->posb, 32 * NA},   {(void**)&d_->prel, 16 * NA}, {(void**)&d_->prelb, 16 * NA},   {(void**)&d_->cellof, 4 * NA},
         {(void**)&d_->lcell, 4 * NA},   {(void**)&d_->slotin, 4 * NA},  {(void**)&d_->perm, 4 * NA},
         {(void**)&d_->nn, 4 * NA},      {(void**)&d_->nbr, 4 * (size_t)npad_ * cap_},
         {(void**)&d_->cell_count, 4 * NC}, {(void**)&d_->cell_start, 4 * NC},
@@ -1041,7 +1197,7 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     slot_rlist_[slot] = rlist;
 
     // atom state: AoS (x,y,z per atom) -> double4 with the type (pos.w) and mass (vel.w)
-    std::vector<double4> hpos(d.n), hvel(d.n), hfrc(d.n);
+    std::vector<double4> hpos(d.n), hvel(d.n), hfrc(d.n), hacc(d.n);
     std::vector<int32_t> hid(d.n);
     for (int64_t k = 0; k < d.n; ++k) {
         int t0 = type_ids[k] - 1;
@@ -1053,6 +1209,8 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
         double m = d.masses[t0];
         hvel[k] = vel ? make_double4(vel[3 * k], vel[3 * k + 1], vel[3 * k + 2], m) : make_double4(0, 0, 0, m);
         hfrc[k] = force ? make_double4(force[3 * k], force[3 * k + 1], force[3 * k + 2], 0.0) : make_double4(0, 0, 0, 0);
+        // acc = 0 + F/m (Atoms::current_acceleration) and 1/m for the mixed path
+        hacc[k] = make_double4(0.0 + hfrc[k].x / m, 0.0 + hfrc[k].y / m, 0.0 + hfrc[k].z / m, 1.0 / m);
         hid[k] = (int32_t)k;
     }
     SysState ss;
@@ -1070,8 +1228,7 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     CP(d_->frc + a0, hfrc.data(), 32 * d.n);
     CP(d_->posb + a0, hpos.data(), 32 * d.n);
     CP(d_->id[0] + a0, hid.data(), 4 * d.n);
-    st = check(cudaMemsetAsync(d_->acc[0] + a0, 0, 32 * d.n, stream_), "upload", err);
-    if (st) return -st;
+    CP(d_->acc[0] + a0, hacc.data(), 32 * d.n);
     st = check(cudaMemsetAsync(d_->cellof + a0, 0, 4 * d.n, stream_), "upload", err);
     if (st) return -st;
     st = check(cudaMemsetAsync(d_->nn + a0, 0, 4 * d.n, stream_), "upload", err);
@@ -1175,6 +1332,27 @@ void Engine::enqueue_rebuild(bool respect) {
         LAUNCH(k_build<false>, (unsigned)max_chunks_, opt_.blk, P, r);
 }
 
+void Engine::launch_force_mixed(int r) {
+    const DP& P = *d_;
+    if (opt_.mixed_kahan)
+        LAUNCH(k_force_mixed<1>, (unsigned)max_chunks_, opt_.blk, P, r);
+    else
+        LAUNCH(k_force_mixed<0>, (unsigned)max_chunks_, opt_.blk, P, r);
+}
+
+void Engine::launch_force_fp64(int r) {
+    const DP& P = *d_;
+    const bool fast = opt_.fp64_fast;
+    if (half_ && !fast)
+        LAUNCH((k_force_fp64<false, false>), (unsigned)max_chunks_, opt_.blk, P, r);
+    else if (half_)
+        LAUNCH((k_force_fp64<false, true>), (unsigned)max_chunks_, opt_.blk, P, r);
+    else if (!fast)
+        LAUNCH((k_force_fp64<true, false>), (unsigned)max_chunks_, opt_.blk, P, r);
+    else
+        LAUNCH((k_force_fp64<true, true>), (unsigned)max_chunks_, opt_.blk, P, r);
+}
+
 void Engine::enqueue_step(bool respect, cudaEvent_t* ev) {
     const DP& P = *d_;
     int r = respect ? 1 : 0;
@@ -1188,13 +1366,14 @@ void Engine::enqueue_step(bool respect, cudaEvent_t* ev) {
     enqueue_rebuild(respect);
     if (ev) cudaEventRecordWithFlags(ev[2], stream_, cudaEventRecordExternal);
     if (mixed)
-        LAUNCH(k_force_mixed, (unsigned)max_chunks_, opt_.blk, P, r);
-    else if (half_)
-        LAUNCH(k_force_fp64<false>, (unsigned)max_chunks_, opt_.blk, P, r);
+        launch_force_mixed(r);
     else
-        LAUNCH(k_force_fp64<true>, (unsigned)max_chunks_, opt_.blk, P, r);
+        launch_force_fp64(r);
     if (ev) cudaEventRecordWithFlags(ev[3], stream_, cudaEventRecordExternal);
-    LAUNCH(k_integrate2<true>, (unsigned)max_chunks_, opt_.blk, P, r);
+    if (mixed)
+        LAUNCH((k_integrate2<true, false>), (unsigned)max_chunks_, opt_.blk, P, r);
+    else
+        LAUNCH((k_integrate2<true, true>), (unsigned)max_chunks_, opt_.blk, P, r);
     if (ev) cudaEventRecordWithFlags(ev[4], stream_, cudaEventRecordExternal);
     LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 0);
     if (ev) cudaEventRecordWithFlags(ev[5], stream_, cudaEventRecordExternal);
@@ -1206,11 +1385,9 @@ void Engine::enqueue_potential() {
     LAUNCH(k_zero_forces, (unsigned)max_chunks_, opt_.blk, P);
     enqueue_rebuild(false);
     if (opt_.precision == PIS_PRECISION_MIXED)
-        LAUNCH(k_force_mixed, (unsigned)max_chunks_, opt_.blk, P, 0);
-    else if (half_)
-        LAUNCH(k_force_fp64<false>, (unsigned)max_chunks_, opt_.blk, P, 0);
+        launch_force_mixed(0);
     else
-        LAUNCH(k_force_fp64<true>, (unsigned)max_chunks_, opt_.blk, P, 0);
+        launch_force_fp64(0);
     LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 1);
 }
 
@@ -1233,7 +1410,10 @@ pis_status Engine::reduce_state(bool virial, std::string& err) {
             st = check(cudaMemcpyAsync(&d_->st[s].want_virial, &wv[s], 4, cudaMemcpyHostToDevice, stream_), "flag", err);
             if (st) return st;
         }
-    LAUNCH(k_integrate2<false>, (unsigned)max_chunks_, opt_.blk, P, 0);
+    if (opt_.precision == PIS_PRECISION_MIXED)
+        LAUNCH((k_integrate2<false, false>), (unsigned)max_chunks_, opt_.blk, P, 0);
+    else
+        LAUNCH((k_integrate2<false, true>), (unsigned)max_chunks_, opt_.blk, P, 0);
     LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 2);
     int32_t zero = 0;
     for (int s = 0; s < opt_.max_slots; ++s)

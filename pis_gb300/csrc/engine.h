@@ -90,6 +90,8 @@ struct PoolOptions {
     int64_t max_cells = 0;     // total cell entries (including one sentinel per slot)
     int max_types_total = 64;  // pair-table entries
     int hist = 1024;           // per-slot energy history ring
+    bool fp64_fast = false;    // FP64 force kernel with FMAs and Newton reciprocal (variant)
+    bool mixed_kahan = false;  // mixed force kernel with compensated FP32 sums (variant)
 };
 
 class Engine {
@@ -153,6 +155,8 @@ class Engine {
     void enqueue_step(bool respect_steps, cudaEvent_t* ev);
     void enqueue_rebuild(bool respect_steps);
     void enqueue_potential();
+    void launch_force_fp64(int respect_steps);
+    void launch_force_mixed(int respect_steps);
     pis_status check(cudaError_t e, const char* what, std::string& err);
 
     PoolOptions opt_;

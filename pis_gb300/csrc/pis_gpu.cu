@@ -18,6 +18,8 @@ struct pis_gpu_ctx {
     double skin = 0.3;
     int precision = PIS_PRECISION_FP64;
     int list_kind = PIS_LIST_DEFAULT;
+    bool fp64_fast = false;
+    bool mixed_kahan = false;
     std::unique_ptr<pis::Engine> eng;
     int slot = -1;
     int64_t n = 0;
@@ -88,12 +90,14 @@ pis_status pis_gpu_create(const pis_lj_pair* table, int32_t n_pairs, int32_t n_t
     return PIS_OK;
 }
 
-pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t force_block) {
+pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flags) {
     if (!ctx) return PIS_ERR_INVALID_ARGUMENT;
     if (list_kind < PIS_LIST_DEFAULT || list_kind > PIS_LIST_FULL)
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown list kind");
-    if (force_block != 0 && force_block != 256)
-        return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "force block size must be 256");
+    if (flags & ~(PIS_OPT_FP64_FAST | PIS_OPT_MIXED_KAHAN))
+        return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown option flag");
+    ctx->fp64_fast = (flags & PIS_OPT_FP64_FAST) != 0;
+    ctx->mixed_kahan = (flags & PIS_OPT_MIXED_KAHAN) != 0;
     if (ctx->precision == PIS_PRECISION_MIXED && list_kind == PIS_LIST_HALF)
         return fail(ctx, PIS_ERR_UNSUPPORTED, "the mixed-precision path uses a full list");
     ctx->list_kind = list_kind;
@@ -129,6 +133,8 @@ pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_id
     pis::PoolOptions opt;
     opt.precision = ctx->precision;
     opt.list_kind = ctx->list_kind;
+    opt.fp64_fast = ctx->fp64_fast;
+    opt.mixed_kahan = ctx->mixed_kahan;
     opt.max_atoms = n;
     opt.max_slots = 1;
     int64_t ncell = 1;

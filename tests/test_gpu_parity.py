@@ -56,11 +56,12 @@ def test_force_pe_virial_argon_fp64(argon_c1, list_kind):
     assert np.abs(w - w_ref).max() <= FP64_TOL * scale
 
 
+@pytest.mark.parametrize("fast", [False, True])
 @pytest.mark.parametrize("list_kind", ["half", "full"])
-def test_force_pe_liquid_fp64(liquid_melt, list_kind):
+def test_force_pe_liquid_fp64(liquid_melt, list_kind, fast):
     o = to_oracle(liquid_melt)
     pe_ref = o.compute_potential()
-    g = to_gpu(liquid_melt, "fp64", list_kind=list_kind)
+    g = to_gpu(liquid_melt, "fp64", list_kind=list_kind, fp64_fast=fast)
     pe, f = g.compute_potential()
     assert abs(pe - pe_ref) <= FP64_TOL * abs(pe_ref)
     assert rel_norm(f, o.force) <= FP64_TOL
@@ -106,10 +107,11 @@ def test_trajectory_100_steps_argon(argon_c1):
     assert rel_norm(vel, o.vel) <= 1e-10
 
 
-def test_trajectory_100_steps_liquid(liquid_melt):
+@pytest.mark.parametrize("fast", [False, True])
+def test_trajectory_100_steps_liquid(liquid_melt, fast):
     o = to_oracle(liquid_melt)
     pe_ref, _ = o.run_nve(0.005, 100)
-    g = to_gpu(liquid_melt, "fp64")
+    g = to_gpu(liquid_melt, "fp64", fp64_fast=fast)
     g.compute_potential()
     pe = g.verlet_step_nve(0.005, 100)
     pos, vel, _ = g.get_state()
@@ -121,10 +123,11 @@ def test_trajectory_100_steps_liquid(liquid_melt):
     assert st["rebuilds"] >= 2  # the skin test fired during the run
 
 
-def test_mixed_force_error(liquid_melt):
+@pytest.mark.parametrize("kahan", [False, True])
+def test_mixed_force_error(liquid_melt, kahan):
     o = to_oracle(liquid_melt)
     pe_ref = o.compute_potential()
-    g = to_gpu(liquid_melt, "mixed")
+    g = to_gpu(liquid_melt, "mixed", mixed_kahan=kahan)
     pe, f = g.compute_potential()
     rms = np.sqrt(np.sum((f - o.force) ** 2) / np.sum(o.force ** 2))
     assert rms <= 1e-5, rms
