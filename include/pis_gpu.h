@@ -145,6 +145,23 @@ void pis_gpu_destroy(pis_gpu_ctx* ctx);
  * summed over the steps, at the cost of one host sync per 50-step graph. */
 pis_status pis_gpu_run_timed(pis_gpu_ctx* ctx, double dt, int64_t n_steps, double* device_ms, double* stage_ms);
 
+/* Force evaluation that allocates no device memory (no counterpart in the reference). For callers
+ * that cannot allocate device memory while running - a host whose framework owns the whole device
+ * memory pool, or a real-time loop where cudaMalloc's latency and implicit synchronisation are not
+ * allowed. Same result as pis_gpu_compute_potential (FP64, reference arithmetic) on buffers the
+ * caller owns: d_type_ids (n, 1-based), d_pos (3 x n) are device inputs; d_forces (3 x n) and d_pe
+ * (1 value) are device outputs; table and h_colmajor are host arrays; stream is a cudaStream_t
+ * (NULL = default stream) and the call returns once the work is enqueued on it.
+ * Limits of the fixed scratch: n <= 262144 atoms, at most 65536 cells at the largest cutoff, at
+ * least 3 cells per axis, at most 4 atom types; larger inputs return PIS_ERR_INVALID_ARGUMENT
+ * (PIS_ERR_BOX_TOO_SMALL below 3 cells). The scratch is one device array shared by every call on
+ * a device: calls that overlap on the GPU race and must be serialised by the caller. The first
+ * call on a device looks up the scratch address; make it before any stream capture. */
+pis_status pis_gpu_compute_potential_noalloc(const pis_lj_pair* table, int32_t n_pairs, int32_t n_types, int64_t n,
+                                             const int32_t* d_type_ids, const double* d_pos,
+                                             const double* h_colmajor, double* d_forces, double* d_pe,
+                                             void* stream);
+
 /* Number of kernel launches this library issued on the calling thread's contexts since load
  * (every kernel of this library, graph launches counted per contained kernel). */
 int64_t pis_gpu_kernel_launches(void);

@@ -64,6 +64,8 @@ SIGNATURES = [
     ("pis_gpu_last_error", C.c_char_p, [_VP]),
     ("pis_gpu_destroy", None, [_VP]),
     ("pis_gpu_run_timed", C.c_int, [_VP, C.c_double, C.c_int64, _DP, _DP]),
+    ("pis_gpu_compute_potential_noalloc", C.c_int, [C.POINTER(LJPair), C.c_int32, C.c_int32, C.c_int64, _VP, _VP, _DP,
+                                                    _VP, _VP, _VP]),
     ("pis_gpu_kernel_launches", C.c_int64, []),
     ("pis_gpu_version", C.c_char_p, []),
 ]

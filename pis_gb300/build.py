@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libpis_gpu.so")
 
-CU_SOURCES = ["engine.cu", "pis_gpu.cu"]
+CU_SOURCES = ["engine.cu", "pis_gpu.cu", "noalloc.cu"]
 CXX_SOURCES: list[str] = []
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
