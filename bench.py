@@ -46,6 +46,10 @@ def parse():
     p.add_argument("--equil", type=int, default=300, help="unreported mixed-precision melt steps")
     p.add_argument("--fp64-steps", type=int, default=200)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    p.add_argument("--no-batch", action="store_true", help="skip the 512-replica batched measurement")
+    p.add_argument("--batch-steps", type=int, default=200)
+    p.add_argument("--no-serve", action="store_true", help="skip the served-stream measurement")
+    p.add_argument("--serve-jobs", type=int, default=32)
     return p.parse_args()
 
 
@@ -252,6 +256,13 @@ def main():
     ms64, _ = f64.run_timed(DT, k64)
     ms64 = max_over_ranks(ms64, world)
     v64 = world * n * k64 / (ms64 * 1e-3)
+    f64f = GpuContext(TABLE, 1, skin=SKIN, precision="fp64", fp64_fast=True)
+    f64f.set_state(melt_pos, types, [1.0], h, velocities=melt_vel)
+    f64f.compute_potential(want_forces=False)
+    f64f.run_timed(DT, 3)
+    ms64f, _ = f64f.run_timed(DT, k64)
+    v64f = world * n * k64 / (max_over_ranks(ms64f, world) * 1e-3)
+    f64f.close()
     mixf = GpuContext(TABLE, 1, skin=SKIN, precision="mixed")
     mixf.set_state(melt_pos, types, [1.0], h, velocities=melt_vel)
     pem, Fm = mixf.compute_potential()
@@ -277,6 +288,9 @@ def main():
     d2h = n * 3 * 8 * 3 + k_e2e * 8
     mix.close()
 
+    batched = None if args.no_batch else run_batched(args, rank, world)
+    served = None if (args.no_serve or rank != 0) else run_served(args)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         import oracle
@@ -297,7 +311,11 @@ def main():
             "pairs_per_s": world * pairs_per_step * args.steps / (ms * 1e-3),
             "fp64": {"value": v64, "unit": "atom-steps/s", "steps": k64, "ms_per_step": ms64 / k64,
                      "dtype": "f64", "list": "half"},
+            "fp64_fast": {"value": v64f, "unit": "atom-steps/s", "steps": k64, "dtype": "f64",
+                          "note": "FMA / Newton-reciprocal variant, same cutoff decisions"},
             "mixed_over_fp64": value / v64,
+            "batched": batched,
+            "served": served,
             "error_vs_fp64": {"force_rms_rel": force_rms, "pe_rel": pe_rel},
             "stages_ms_per_step": {"integrate1": stages_per[0], "rebuild": stages_per[1], "force": stages_per[2],
                                    "integrate2": stages_per[3], "reduce": stages_per[4]},
@@ -317,6 +335,81 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def batch_jobs(seed=2024, count=512):
+    """512 replicas: N log-uniform in [500, 32000] rounded to 4 k^3 FCC, rho* in U[0.70, 0.95],
+    T* in U[0.5, 1.5], per-replica seeds."""
+    import math
+    from pis_gb300.batch import lj_job
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for r in range(count):
+        N = math.exp(rng.uniform(math.log(500), math.log(32000)))
+        k = int(min(20, max(5, round((N / 4) ** (1 / 3)))))
+        jobs.append(lj_job(k, rng.uniform(0.70, 0.95), rng.uniform(0.5, 1.5), 10 ** 9, 1000 + r))
+    return jobs
+
+
+def run_batched(args, rank, world):
+    """All 512 replicas advanced together (one launch per kernel per step, 50-step graphs)."""
+    from pis_gb300.batch import Batch, lj_pool_cells
+    jobs = batch_jobs(seed=2024 + rank)
+    atoms = sum(4 * j.k ** 3 for j in jobs)
+    cells = sum(lj_pool_cells(j.k, j.rho) for j in jobs)
+    out = {"replicas": len(jobs), "atoms": atoms, "steps": args.batch_steps}
+    for prec, kw in (("mixed", {}), ("fp64", {}), ("fp64_fast", {"fp64_fast": True})):
+        precision = "mixed" if prec == "mixed" else "fp64"
+        k = args.batch_steps if prec == "mixed" else max(3, args.batch_steps // 5)
+        b = Batch(atoms + 1024, len(jobs), cells + 1024, precision=precision, **kw)
+        for j in jobs:
+            b.admit_lj(j)
+        b.run_timed(100)  # warm-up and melt
+        barrier(world)
+        ms = max_over_ranks(b.run_timed(k), world)
+        out[prec] = world * atoms * k / (ms * 1e-3)
+        b.close()
+    out["mixed_over_fp64"] = out["mixed"] / out["fp64"]
+    return out
+
+
+def serve_requests(count, seed=77, rate=200.0, step_scale=0.2):
+    """Poisson arrivals (rate jobs/s) of LJ jobs: N log-uniform in [1000, 256000] rounded to 4 k^3,
+    rho* in U[0.70, 0.95], T* in U[0.5, 1.5], steps U[100, 5000] scaled by step_scale."""
+    import math
+    from pis_gb300.batch import lj_job
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    reqs = []
+    for q in range(count):
+        t += rng.exponential(1.0 / rate)
+        N = math.exp(rng.uniform(math.log(1000), math.log(256000)))
+        k = int(min(40, max(6, round((N / 4) ** (1 / 3)))))
+        steps = int(round(rng.uniform(100, 5000) * step_scale))
+        reqs.append((t, lj_job(k, rng.uniform(0.70, 0.95), rng.uniform(0.5, 1.5), steps, 5000 + q)))
+    return reqs
+
+
+def run_served(args):
+    """Served stream with continuous batching (mixed precision, one pool) against the plain FP64
+    path serving the same requests one at a time."""
+    from pis_gb300.batch import Batch, lj_pool_cells
+    reqs = serve_requests(args.serve_jobs)
+    work = sum(4 * j.k ** 3 * j.steps for _, j in reqs)
+    offered = sum(4 * j.k ** 3 * j.steps for _, j in reqs) / max(reqs[-1][0], 1e-9)
+    out = {"jobs": len(reqs), "arrival_rate_per_s": 200.0, "step_scale": 0.2, "atom_steps": work,
+           "offered_atom_steps_per_s": offered}
+    max_atoms = 4 * 40 ** 3 * 8
+    max_cells = max(lj_pool_cells(j.k, j.rho) for _, j in reqs) * 16
+    for name, precision, slots in (("mixed_batched", "mixed", 64), ("fp64_one_at_a_time", "fp64", 1)):
+        b = Batch(max_atoms, slots, max_cells, precision=precision)
+        res, wall = b.serve(reqs, graph_steps=50)
+        b.close()
+        lat = np.array([r["finished_s"] - r["arrival_s"] for r in res])
+        ok = all(r["status"] == 0 for r in res)
+        out[name] = {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+                     "atom_steps_per_s": work / wall, "wall_s": wall, "all_ok": ok}
+    return out
 
 
 def read_traffic(kernel, n):

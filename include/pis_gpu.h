@@ -92,6 +92,8 @@ pis_status pis_gpu_create(const pis_lj_pair* table, int32_t n_pairs, int32_t n_t
 #define PIS_OPT_FP64_FAST 1  /* FP64 forces with fused multiply-adds and a Newton reciprocal; the
                               * cutoff is still decided with the reference's exact arithmetic */
 #define PIS_OPT_MIXED_KAHAN 2 /* mixed path: compensated FP32 sums instead of FP64 batch sums */
+#define PIS_OPT_LANES(n) ((n) << 8) /* lanes per atom in the list build and force kernels:
+                                     * 1 (thread per atom, default), 4, 8, 16 or 32 (warp per atom) */
 
 /* Select a measured variant: list kind (pis_list_kind) and PIS_OPT_* flags. Takes effect at the
  * next set_state. */
@@ -161,6 +163,89 @@ pis_status pis_gpu_compute_potential_noalloc(const pis_lj_pair* table, int32_t n
                                              const int32_t* d_type_ids, const double* d_pos,
                                              const double* h_colmajor, double* d_forces, double* d_pe,
                                              void* stream);
+
+/* ---- Batched replicas and served jobs -------------------------------------------------------
+ * A batch is one device pool holding many independent periodic systems ("slots"). Every step of
+ * pis_batch_advance advances all slots that still have steps left, in one launch per kernel over
+ * the whole pool, captured as CUDA graphs of up to 50 steps; a slot whose step count runs out
+ * mid-graph stops exactly there. Slots are admitted and released between advances (continuous
+ * batching). Each slot's arithmetic is independent of the others': a job gives the same result
+ * alone and in any mix. No counterpart in the reference, which runs one system per process
+ * (src/simulation.rs:8-39); each slot follows the same NVE step as pis_gpu_verlet_step_nve. */
+typedef struct pis_batch pis_batch;
+
+/* A job given by its state (the arrays of pis_gpu_set_state) and its run length. */
+typedef struct {
+    int64_t n;
+    int32_t n_types;
+    const int32_t* type_ids;
+    const double* masses_per_type;
+    const double* pos;
+    const double* vel;         /* may be NULL */
+    const double* h_colmajor;
+    const pis_lj_pair* table;
+    int32_t n_pairs;
+    double skin;
+    double dt;
+    int64_t steps;
+} pis_job;
+
+/* A job given by the synthetic LJ-liquid recipe (reduced units, eps = sigma = mass = 1): 4 k^3
+ * atoms on an FCC lattice at number density rho in the atom order of the reference's lattice
+ * generator (src/bin/sapphire/main.rs:61-76), Maxwell-Boltzmann velocities at T* from `seed`
+ * (drift removed and rescaled as src/atoms/velocities.rs:35-59), shifted LJ cut at rcut. */
+typedef struct {
+    int32_t k;
+    double rho, t_star, rcut, skin, dt;
+    int64_t steps;
+    uint64_t seed;
+} pis_lj_job;
+
+pis_status pis_batch_create(int64_t max_atoms, int32_t max_slots, int64_t max_cells, int32_t precision,
+                            int32_t flags, pis_batch** out);
+/* Admit a job: place it in free pool space, evaluate its initial forces, set its step count.
+ * PIS_ERR_NO_MEMORY when it does not fit right now (retry after a release). */
+pis_status pis_batch_admit(pis_batch* b, const pis_job* job, int32_t* slot);
+pis_status pis_batch_admit_lj(pis_batch* b, const pis_lj_job* job, int32_t* slot);
+/* 1 if the job fits in the free pool space now, else 0 (admission by device-memory footprint). */
+int32_t pis_batch_fits_lj(const pis_batch* b, const pis_lj_job* job);
+/* Advance every slot with steps left by up to k steps. */
+pis_status pis_batch_advance(pis_batch* b, int64_t k);
+/* Same, timed with CUDA events on the batch's stream (device milliseconds). */
+pis_status pis_batch_run_timed(pis_batch* b, int64_t k, double* device_ms);
+/* Slots whose steps are done and not yet released (up to cap of them). */
+pis_status pis_batch_poll(pis_batch* b, int32_t* done, int32_t cap, int32_t* n_done);
+/* State of a slot (3 x n arrays, any may be NULL) and its last energies and step count. */
+pis_status pis_batch_result(pis_batch* b, int32_t slot, double* pos, double* vel, double* force, double* pe,
+                            double* ke, int64_t* steps_done);
+/* Per-step potential energies of a slot's last n steps (n <= 1024). */
+pis_status pis_batch_pe_history(pis_batch* b, int32_t slot, int64_t n, double* pe);
+pis_status pis_batch_release(pis_batch* b, int32_t slot);
+int64_t pis_batch_atoms(const pis_batch* b);
+const char* pis_batch_last_error(const pis_batch* b);
+void pis_batch_destroy(pis_batch* b);
+
+/* One request of a served stream: an LJ job arriving `arrival_s` seconds after the start. */
+typedef struct {
+    double arrival_s;
+    pis_lj_job job;
+} pis_request;
+
+typedef struct {
+    double admitted_s;  /* wall seconds after the start */
+    double finished_s;
+    int64_t atoms;
+    int64_t steps;
+    double pe, ke;      /* energies after the last step */
+    int32_t status;     /* pis_status of the job */
+} pis_request_result;
+
+/* Serve a request stream in wall-clock time: requests are queued at their arrival times,
+ * admitted as soon as pool space allows (continuous batching: they join slots already running),
+ * advanced in graphs of graph_steps steps, and released when done. Returns per-request times and
+ * the total wall seconds. */
+pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64_t graph_steps,
+                         pis_request_result* out, double* wall_s);
 
 /* Number of kernel launches this library issued on the calling thread's contexts since load
  * (every kernel of this library, graph launches counted per contained kernel). */

@@ -42,6 +42,28 @@ class Stats(C.Structure):
                 ("pe", C.c_double), ("ke", C.c_double), ("virial", C.c_double * 9)]
 
 
+class Job(C.Structure):
+    _fields_ = [("n", C.c_int64), ("n_types", C.c_int32), ("type_ids", C.POINTER(C.c_int32)),
+                ("masses_per_type", C.POINTER(C.c_double)), ("pos", C.POINTER(C.c_double)),
+                ("vel", C.POINTER(C.c_double)), ("h_colmajor", C.POINTER(C.c_double)),
+                ("table", C.POINTER(LJPair)), ("n_pairs", C.c_int32), ("skin", C.c_double), ("dt", C.c_double),
+                ("steps", C.c_int64)]
+
+
+class LJJob(C.Structure):
+    _fields_ = [("k", C.c_int32), ("rho", C.c_double), ("t_star", C.c_double), ("rcut", C.c_double),
+                ("skin", C.c_double), ("dt", C.c_double), ("steps", C.c_int64), ("seed", C.c_uint64)]
+
+
+class Request(C.Structure):
+    _fields_ = [("arrival_s", C.c_double), ("job", LJJob)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("admitted_s", C.c_double), ("finished_s", C.c_double), ("atoms", C.c_int64), ("steps", C.c_int64),
+                ("pe", C.c_double), ("ke", C.c_double), ("status", C.c_int32)]
+
+
 _lib = None
 
 # (name, restype, argtypes) of every C-ABI entry point declared in include/pis_gpu.h
@@ -66,8 +88,45 @@ SIGNATURES = [
     ("pis_gpu_run_timed", C.c_int, [_VP, C.c_double, C.c_int64, _DP, _DP]),
     ("pis_gpu_compute_potential_noalloc", C.c_int, [C.POINTER(LJPair), C.c_int32, C.c_int32, C.c_int64, _VP, _VP, _DP,
                                                     _VP, _VP, _VP]),
+    ("pis_batch_create", C.c_int, [C.c_int64, C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.POINTER(_VP)]),
+    ("pis_batch_admit", C.c_int, [_VP, C.POINTER(Job), C.POINTER(C.c_int32)]),
+    ("pis_batch_admit_lj", C.c_int, [_VP, C.POINTER(LJJob), C.POINTER(C.c_int32)]),
+    ("pis_batch_fits_lj", C.c_int32, [_VP, C.POINTER(LJJob)]),
+    ("pis_batch_advance", C.c_int, [_VP, C.c_int64]),
+    ("pis_batch_run_timed", C.c_int, [_VP, C.c_int64, _DP]),
+    ("pis_batch_poll", C.c_int, [_VP, C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32)]),
+    ("pis_batch_result", C.c_int, [_VP, C.c_int32, _DP, _DP, _DP, _DP, _DP, C.POINTER(C.c_int64)]),
+    ("pis_batch_pe_history", C.c_int, [_VP, C.c_int32, C.c_int64, _DP]),
+    ("pis_batch_release", C.c_int, [_VP, C.c_int32]),
+    ("pis_batch_atoms", C.c_int64, [_VP]),
+    ("pis_batch_last_error", C.c_char_p, [_VP]),
+    ("pis_batch_destroy", None, [_VP]),
+    ("pis_serve_run", C.c_int, [_VP, C.POINTER(Request), C.c_int32, C.c_int64, C.POINTER(RequestResult), _DP]),
     ("pis_gpu_kernel_launches", C.c_int64, []),
     ("pis_gpu_version", C.c_char_p, []),
+]
+
+
+HOST_SIGNATURES = [
+    ("pis_data_read", C.c_int, [C.c_char_p, C.POINTER(_VP), C.c_char_p, C.c_int32]),
+    ("pis_data_n_atoms", C.c_int64, [_VP]),
+    ("pis_data_n_types", C.c_int32, [_VP]),
+    ("pis_data_n_pairs", C.c_int32, [_VP]),
+    ("pis_data_get", C.c_int, [_VP, C.POINTER(C.c_int32), _DP, _DP, _DP, _DP, C.POINTER(C.c_int32)]),
+    ("pis_data_pairs", C.c_int, [_VP, C.POINTER(LJPair)]),
+    ("pis_data_free", None, [_VP]),
+    ("pis_data_write", C.c_int, [C.c_char_p, C.c_int64, C.c_int32, C.POINTER(C.c_int32), _DP, _DP, _DP, _DP,
+                                 C.POINTER(LJPair), C.c_int32]),
+    ("pis_maxwell_boltzmann", C.c_int, [C.c_int64, _DP, C.c_double, C.c_uint64, _DP]),
+    ("pis_format_f64", C.c_int32, [C.c_double, C.c_char_p, C.c_int32]),
+    ("pis_system_open", C.c_int, [C.c_char_p, C.c_int32, C.c_double, C.POINTER(_VP)]),
+    ("pis_system_run", C.c_int, [_VP, C.c_char_p]),
+    ("pis_system_steps", C.c_int64, [_VP]),
+    ("pis_system_timestep", C.c_double, [_VP]),
+    ("pis_system_ensemble", C.c_int32, [_VP]),
+    ("pis_system_state", C.c_int, [_VP, _DP, _DP, _DP]),
+    ("pis_system_last_error", C.c_char_p, [_VP]),
+    ("pis_system_close", None, [_VP]),
 ]
 
 
@@ -79,7 +138,7 @@ def lib() -> C.CDLL:
             raise ImportError(f"{LIB} is missing: build it with `python -m pis_gb300.build` "
                               "(pis_gb300 has no CPU fallback)")
         L = C.CDLL(LIB)
-        for name, res, args in SIGNATURES:
+        for name, res, args in SIGNATURES + HOST_SIGNATURES:
             fn = getattr(L, name)
             fn.restype = res
             fn.argtypes = args

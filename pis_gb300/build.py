@@ -19,8 +19,10 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libpis_gpu.so")
 
-CU_SOURCES = ["engine.cu", "pis_gpu.cu", "noalloc.cu"]
-CXX_SOURCES: list[str] = []
+CU_SOURCES = ["engine.cu", "pis_gpu.cu", "pis_batch.cu", "noalloc.cu"]
+CXX_SOURCES = ["host_io.cpp", "host_system.cpp"]
+CLI_SOURCE = "pis_gpu_run.cpp"
+CLI = os.path.join(OUT_DIR, "pis_gpu_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
@@ -59,8 +61,7 @@ def build(verbose: bool = False, force: bool = False, extra_flags: list[str] | N
         obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         objs.append(obj)
         if force or _stale(obj, [path] + hdrs):
-            lang = [] if src.endswith(".cu") else ["-x", "cu"]
-            jobs.append([nvcc, *ARCH, *flags, *lang, "-c", path, "-o", obj])
+            jobs.append([nvcc, *ARCH, *flags, "-c", path, "-o", obj])
 
     def run(cmd):
         if verbose:
@@ -75,6 +76,9 @@ def build(verbose: bool = False, force: bool = False, extra_flags: list[str] | N
         list(ex.map(run, jobs))
     if force or jobs or _stale(LIB, objs):
         run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+    cli_src = os.path.join(CSRC, CLI_SOURCE)
+    if force or _stale(CLI, [cli_src, LIB] + hdrs):
+        run([nvcc, *ARCH, *flags, "-o", CLI, cli_src, "-L", OUT_DIR, "-lpis_gpu", "-Xlinker", "-rpath,$ORIGIN"])
     return LIB
 
 

@@ -20,10 +20,14 @@
 // intrinsics so no multiply-add is fused where the reference has two roundings.
 #include "engine.h"
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstring>
+
+namespace cg = cooperative_groups;
 
 namespace pis {
 
@@ -33,15 +37,16 @@ int64_t Engine::launches() { return g_launches.load(); }
 constexpr int JBITS = 26;                  // atom-index bits of a neighbour entry
 constexpr uint32_t JMASK = (1u << JBITS) - 1u;
 constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 8;
 constexpr int END_THREADS = 256;
 
 struct Engine::DevPtrs {
-    double4* pos[2];
-    double4* vel[2];
-    double4* acc[2];
+    double4_32a* pos[2];
+    double4_32a* vel[2];
+    double4_32a* acc[2];
     int32_t* id[2];
-    double4* frc;
-    double4* posb;
+    double4_32a* frc;
+    double4_32a* posb;
     float4* prel;
     float4* prelb;
     int32_t* cellof;
@@ -69,6 +74,7 @@ struct Engine::DevPtrs {
     int32_t max_slots;
     int32_t zero_forces;  // half list: integrate1 clears F for the atomic scatter
     int32_t full_list;
+    int32_t pe_stride;    // force-kernel blocks per chunk (lanes per atom)
 };
 using DP = Engine::DevPtrs;
 
@@ -85,6 +91,15 @@ __device__ __forceinline__ double min_image_axis(double r, double h, double hinv
     double s = __dmul_rn(hinv, r);
     s = __dsub_rn(s, rint(s));
     return __dmul_rn(h, s);
+}
+// Mixed path wrap: only a coordinate that left [0, L) moves. Tested on the bit pattern (a
+// negative double has the sign bit set; non-negative doubles order like their bits), so the test
+// costs no FP64 instruction.
+__device__ __forceinline__ double wrap_if_out(double x, double L) {
+    const long long b = __double_as_longlong(x);
+    if (b < 0) return x + L;
+    if (b >= __double_as_longlong(L)) return x - L;
+    return x;
 }
 // One axis of SimulationBox::apply_boundary_conditions_pos: s = hinv*r; s -= floor(s); r = h*s.
 __device__ __forceinline__ double wrap_axis(double r, double h, double hinv) {
@@ -149,11 +164,33 @@ __device__ __forceinline__ bool atom_of(const DP& P, int& s, int& i) {
     return i < (int)(sp.a0 + sp.n);
 }
 
-__device__ __forceinline__ bool slot_runs(const DP& P, int s, bool respect_steps) {
-    return !respect_steps || P.st[s].steps_left > 0;
+// Lanes-per-atom kernels: LPA consecutive lanes (a cooperative-groups tile) share one atom and
+// the grid has LPA blocks per chunk. Returns false for padding groups; s < 0 for unused chunks.
+template <int LPA>
+__device__ __forceinline__ bool group_atom_of(const DP& P, int& s, int& i) {
+    const int chunk = blockIdx.x / LPA, sub = blockIdx.x % LPA;
+    s = P.blk_sys[chunk];
+    if (s < 0) return false;
+    i = P.blk_first[chunk] + sub * (256 / LPA) + (int)(threadIdx.x / LPA);
+    const SysParams& sp = P.sp[s];
+    return i < (int)(sp.a0 + sp.n);
 }
 
-__device__ __forceinline__ float4 cell_relative(const SysParams& sp, double4 p, int lc, int type) {
+// Neighbour-list layout: entry k of atom i lives at (k / LPA) * (npad * LPA) + i * LPA + k % LPA.
+// The LPA lanes of one atom read or write one contiguous run of LPA words, and consecutive atoms'
+// runs are adjacent, so a warp touches whole 128-byte lines. LPA = 1 is plain column-major.
+template <int LPA>
+__device__ __forceinline__ int64_t nbr_index(int i, int k, int64_t npad) {
+    return (int64_t)(k / LPA) * (npad * LPA) + (int64_t)i * LPA + (k % LPA);
+}
+
+// Step mode (nonzero): slots with steps left take part. Evaluation mode (0): only slots the host
+// marked for a force evaluation or reduction.
+__device__ __forceinline__ bool slot_runs(const DP& P, int s, int step_mode) {
+    return step_mode ? P.st[s].steps_left > 0 : P.st[s].eval != 0;
+}
+
+__device__ __forceinline__ float4 cell_relative(const SysParams& sp, double4_32a p, int lc, int type) {
     int cx = lc % sp.nc[0];
     int cy = (lc / sp.nc[0]) % sp.nc[1];
     int cz = lc / (sp.nc[0] * sp.nc[1]);
@@ -182,9 +219,9 @@ __global__ void k_integrate1(const DP P) {
     const SysParams& sp = P.sp[s];
     SysState& st = P.st[s];
     const int cur = st.cur;
-    const double4 p = P.pos[cur][i];
-    const double4 v = P.vel[cur][i];
-    const double4 a = P.acc[cur][i];
+    const double4_32a p = P.pos[cur][i];
+    const double4_32a v = P.vel[cur][i];
+    const double4_32a a = P.acc[cur][i];
     double x, y, z;
     if (!MIXED) {
         // positions += v*dt + (a*0.5)*dt^2, then s = h^-1 x; s -= floor(s); x = h s
@@ -199,19 +236,21 @@ __global__ void k_integrate1(const DP P) {
         x = p.x + fma(v.x, sp.dt, a.x * hdt2);
         y = p.y + fma(v.y, sp.dt, a.y * hdt2);
         z = p.z + fma(v.z, sp.dt, a.z * hdt2);
-        x = (x < 0.0) ? x + sp.h[0] : ((x >= sp.h[0]) ? x - sp.h[0] : x);
-        y = (y < 0.0) ? y + sp.h[1] : ((y >= sp.h[1]) ? y - sp.h[1] : y);
-        z = (z < 0.0) ? z + sp.h[2] : ((z >= sp.h[2]) ? z - sp.h[2] : z);
+        x = wrap_if_out(x, sp.h[0]);
+        y = wrap_if_out(y, sp.h[1]);
+        z = wrap_if_out(z, sp.h[2]);
     }
-    P.pos[cur][i] = make_double4(x, y, z, p.w);
-    if (P.zero_forces) P.frc[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+    P.pos[cur][i] = make_double4_32a(x, y, z, p.w);
+    if (P.zero_forces) P.frc[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
     // skin test: rebuild when any atom moved more than skin/2 since the last build. The
     // minimum image is only taken when the plain difference fails the test (moved far, or
     // crossed the periodic boundary).
-    const double4 b = P.posb[i];
+    const double4_32a b = P.posb[i];
     double dx = x - b.x, dy = y - b.y, dz = z - b.z;
     double d2 = fma(dx, dx, fma(dy, dy, dz * dz));
-    if (!(d2 <= sp.half_skin2)) {
+    // d2 >= 0, so comparing bit patterns as integers orders it like the doubles (a NaN with
+    // either sign fails the test too: its magnitude bits exceed every finite value's)
+    if ((__double_as_longlong(d2) & 0x7fffffffffffffffll) > __double_as_longlong(sp.half_skin2)) {
         dx = min_image_axis(dx, sp.h[0], sp.hinv[0]);
         dy = min_image_axis(dy, sp.h[1], sp.hinv[1]);
         dz = min_image_axis(dz, sp.h[2], sp.hinv[2]);
@@ -236,13 +275,13 @@ __global__ void k_bin(const DP P, int respect_steps) {
     const SysParams& sp = P.sp[s];
     const SysState& st = P.st[s];
     if (!st.rebuild) return;
-    double4 p = P.pos[st.cur][i];
+    double4_32a p = P.pos[st.cur][i];
     int c[3];
     double q[3] = {p.x, p.y, p.z};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        double t = floor(__dmul_rn(__dmul_rn(sp.hinv[d], q[d]), (double)sp.nc[d]));
-        long long k = (t == t) ? (long long)fmax(fmin(t, 4.0e18), -4.0e18) : 0;
+        // floor and conversion in one saturating instruction
+        long long k = __double2ll_rd(__dmul_rn(__dmul_rn(sp.hinv[d], q[d]), (double)sp.nc[d]));
         k %= sp.nc[d];
         if (k < 0) k += sp.nc[d];
         c[d] = (int)k;
@@ -253,29 +292,40 @@ __global__ void k_bin(const DP P, int respect_steps) {
 }
 
 // Counting sort, pass 2: exclusive scan of the cell counts of one slot (one block per slot),
-// writing absolute atom indices; also flips the slot's buffer set.
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan(const DP P, int respect_steps) {
+// writing absolute atom indices; also flips the slot's buffer set. Counts are staged through
+// shared memory so global loads and stores stay coalesced while each thread scans SCAN_ITEMS
+// consecutive cells.
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan(const DP P, int step_mode) {
     int s = blockIdx.x;
     const SysParams& sp = P.sp[s];
     if (!sp.active) return;
-    if (!slot_runs(P, s, respect_steps)) return;
+    if (!slot_runs(P, s, step_mode)) return;
     SysState& st = P.st[s];
     if (!st.rebuild) return;
+    __shared__ int buf[SCAN_THREADS * SCAN_ITEMS];
     __shared__ int warp_tot[SCAN_THREADS / 32];
     __shared__ int carry_sh;
     const int ncell = sp.nc[0] * sp.nc[1] * sp.nc[2];
+    int32_t* __restrict__ cnt_g = P.cell_count + sp.c0;
+    int32_t* __restrict__ start_g = P.cell_start + sp.c0;
     int carry = (int)sp.a0;
     const int t = threadIdx.x, l = t & 31, w = t >> 5;
-    for (int base = 0; base < ncell; base += SCAN_THREADS * 4) {
-        int v[4], sum = 0;
+    for (int base = 0; base < ncell; base += SCAN_THREADS * SCAN_ITEMS) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            int c = base + t * 4 + k;
-            v[k] = 0;
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            const int c = base + k * SCAN_THREADS + t;
+            int v = 0;
             if (c < ncell) {
-                v[k] = P.cell_count[sp.c0 + c];
-                P.cell_count[sp.c0 + c] = 0;
+                v = cnt_g[c];
+                cnt_g[c] = 0;
             }
+            buf[k * SCAN_THREADS + t] = v;
+        }
+        __syncthreads();
+        int v[SCAN_ITEMS], sum = 0;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            v[k] = buf[t * SCAN_ITEMS + k];
             sum += v[k];
         }
         int incl = sum;
@@ -300,16 +350,21 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const DP P, int respect_s
         __syncthreads();
         int run = carry + warp_tot[w] + incl - sum;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            int c = base + t * 4 + k;
-            if (c < ncell) P.cell_start[sp.c0 + c] = run;
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            buf[t * SCAN_ITEMS + k] = run;
             run += v[k];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            const int c = base + k * SCAN_THREADS + t;
+            if (c < ncell) start_g[c] = buf[k * SCAN_THREADS + t];
         }
         carry += carry_sh;
         __syncthreads();
     }
     if (t == 0) {
-        P.cell_start[sp.c0 + ncell] = carry;
+        start_g[ncell] = carry;
         st.cur ^= 1;
     }
 }
@@ -343,13 +398,44 @@ __global__ void k_gather(const DP P, int64_t max_cells, int respect_steps) {
     const int dst_set = st.cur, src_set = st.cur ^ 1;
     const int beg = P.cell_start[g], end = P.cell_start[g + 1];
     const int cnt = end - beg;
+    // rank of every member by original id: ids held in lane registers for cells of up to 64
+    // atoms (one or two per lane), compared through warp shuffles; larger cells re-read ids
+    int rk[2] = {0, 0}, srcs[2] = {-1, -1}, ids[2] = {0x7fffffff, 0x7fffffff};
+    if (cnt <= 64) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int k = lane + 32 * h;
+            if (k < cnt) {
+                srcs[h] = P.perm[beg + k];
+                ids[h] = P.id[src_set][srcs[h]];
+            }
+        }
+        const int n0 = cnt < 32 ? cnt : 32;
+        for (int q = 0; q < n0; ++q) {
+            const int v = __shfl_sync(0xffffffffu, ids[0], q);
+            rk[0] += v < ids[0];
+            rk[1] += v < ids[1];
+        }
+        for (int q = 32; q < cnt; ++q) {
+            const int v = __shfl_sync(0xffffffffu, ids[1], q - 32);
+            rk[0] += v < ids[0];
+            rk[1] += v < ids[1];
+        }
+    }
     for (int k = lane; k < cnt; k += 32) {
-        int src = P.perm[beg + k];
-        int myid = P.id[src_set][src];
-        int rank = 0;
-        for (int q = 0; q < cnt; ++q) rank += P.id[src_set][P.perm[beg + q]] < myid;
+        int src, myid, rank = 0;
+        if (cnt <= 64) {
+            const bool hi = k >= 32;
+            src = hi ? srcs[1] : srcs[0];
+            myid = hi ? ids[1] : ids[0];
+            rank = hi ? rk[1] : rk[0];
+        } else {
+            src = P.perm[beg + k];
+            myid = P.id[src_set][src];
+            for (int q = 0; q < cnt; ++q) rank += P.id[src_set][P.perm[beg + q]] < myid;
+        }
         int dst = beg + rank;
-        double4 p = P.pos[src_set][src];
+        double4_32a p = P.pos[src_set][src];
         P.pos[dst_set][dst] = p;
         P.vel[dst_set][dst] = P.vel[src_set][src];
         P.acc[dst_set][dst] = P.acc[src_set][src];
@@ -362,27 +448,33 @@ __global__ void k_gather(const DP P, int64_t max_cells, int respect_steps) {
     }
 }
 
-// Neighbour-list build at rcut + skin, one thread per atom in cell order (the atoms of a cell
-// are consecutive threads and walk the same neighbour cells, so their loads of prel[j] are
-// broadcasts). The distance test runs in FP32 on cell-relative coordinates with a radius
-// padded by 1e-5, so the list is a superset of the exact FP64 list; the force kernels apply the
-// exact cutoff. Entry = j | image code << 26, the code giving the cell offset (0, +1, -1 per
-// axis, 2 bits each) that makes prel_j - prel_i + offset * cell the minimum-image displacement
-// at build time. Axes with only two cells reach the same neighbour cell through +1 and -1; the
-// generic path keeps, per pair, whichever image is nearer.
+// Neighbour-list build at rcut + skin. LPA lanes share one home atom (atoms in cell order, so
+// neighbouring groups walk the same cells) and split each neighbour cell's atoms among
+// themselves; the accepted pairs are compacted with a ballot over the group and a prefix
+// popcount, so each group writes its new entries as one contiguous run of the list layout. The
+// distance test runs in FP32 on cell-relative coordinates with a radius padded by 1e-5, so the
+// list is a superset of the exact FP64 list; the force kernels apply the exact cutoff.
+// Entry = j | image code << 26, the code giving the cell offset (0, +1, -1 per axis, 2 bits each)
+// that makes prel_j - prel_i + offset * cell the minimum-image displacement at build time. Axes
+// with only two cells reach the same neighbour cell through +1 and -1; the generic path keeps, per
+// pair, whichever image is nearer.
 __device__ __forceinline__ int wrapc(int c, int n) {
     c += (c < 0) ? n : 0;
     return c - ((c >= n) ? n : 0);
 }
 
-template <bool HALF>
-__global__ void k_build(const DP P, int respect_steps) {
+template <bool HALF, int LPA>
+__global__ void __launch_bounds__(256) k_build(const DP P, int step_mode) {
+    auto tile = cg::tiled_partition<LPA>(cg::this_thread_block());
     int s, i;
-    if (!atom_of(P, s, i)) return;
-    if (!slot_runs(P, s, respect_steps)) return;
+    const bool live = group_atom_of<LPA>(P, s, i);
+    if (s < 0 || !live) return;  // uniform over the group (one atom per group)
+    if (!slot_runs(P, s, step_mode)) return;
     const SysParams& sp = P.sp[s];
     SysState& st = P.st[s];
     if (!st.rebuild) return;
+    const int gl = (int)tile.thread_rank();
+    const uint32_t below = (1u << gl) - 1u;
     const int nx = sp.nc[0], ny = sp.nc[1], nz = sp.nc[2];
     const int lc = P.cellof[i];
     const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
@@ -393,10 +485,29 @@ __global__ void k_build(const DP P, int respect_steps) {
     const int cap = P.cap;
     const int32_t* __restrict__ cstart = P.cell_start + sp.c0;
     const float4* __restrict__ prel = P.prel;
-    uint32_t* out = P.nbr + i;
     int cnt = 0;
     const bool generic = nx < 3 || ny < 3 || nz < 3;
     const int zlo = nz >= 3 ? -1 : 0, ylo = ny >= 3 ? -1 : 0, xlo = nx >= 3 ? -1 : 0;
+    // squared distance from the atom to the face of a neighbouring cell along one axis (the
+    // atom sits at pi relative to its own cell centre); the padding keeps the test conservative
+    const float gxm = fmaxf(pi.x + 0.5f * csx, 0.f), gxp = fmaxf(0.5f * csx - pi.x, 0.f);
+    const float gym = fmaxf(pi.y + 0.5f * csy, 0.f), gyp = fmaxf(0.5f * csy - pi.y, 0.f);
+    const float gzm = fmaxf(pi.z + 0.5f * csz, 0.f), gzp = fmaxf(0.5f * csz - pi.z, 0.f);
+    auto append = [&](bool take, int j, uint32_t code) {
+        if (LPA == 1) {
+            if (take) {
+                if (cnt < cap) P.nbr[nbr_index<1>(i, cnt, npad)] = (uint32_t)j | (code << JBITS);
+                ++cnt;
+            }
+        } else {
+            const uint32_t m = tile.ballot(take);
+            if (take) {
+                const int pos = cnt + __popc(m & below);
+                if (pos < cap) P.nbr[nbr_index<LPA>(i, pos, npad)] = (uint32_t)j | (code << JBITS);
+            }
+            cnt += __popc(m);
+        }
+    };
     for (int oz = zlo; oz <= 1; ++oz) {
         const int z2 = wrapc(cz + oz, nz);
         for (int oy = ylo; oy <= 1; ++oy) {
@@ -405,61 +516,62 @@ __global__ void k_build(const DP P, int respect_steps) {
                 const int x2 = wrapc(cx + ox, nx);
                 const int nb = (z2 * ny + y2) * nx + x2;
                 const int b0 = cstart[nb], b1 = cstart[nb + 1];
+                const uint32_t cell_code = ((uint32_t)(ox < 0 ? 2 : ox)) | ((uint32_t)(oy < 0 ? 2 : oy) << 2) |
+                                           ((uint32_t)(oz < 0 ? 2 : oz) << 4);
                 if (!generic) {
+                    // skip the whole cell when its nearest point is beyond the list radius
+                    const float ex = ox < 0 ? gxm : (ox > 0 ? gxp : 0.f);
+                    const float ey = oy < 0 ? gym : (oy > 0 ? gyp : 0.f);
+                    const float ez = oz < 0 ? gzm : (oz > 0 ? gzp : 0.f);
+                    if (LPA == 1 && fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > rl2) continue;
                     const float sx = ox * csx - pi.x, sy = oy * csy - pi.y, sz = oz * csz - pi.z;
-                    const uint32_t code = (((uint32_t)(ox < 0 ? 2 : ox)) | ((uint32_t)(oy < 0 ? 2 : oy) << 2) |
-                                           ((uint32_t)(oz < 0 ? 2 : oz) << 4))
-                                          << JBITS;
-                    for (int j = b0; j < b1; ++j) {
-                        const float4 pj = prel[j];
-                        const float dx = pj.x + sx, dy = pj.y + sy, dz = pj.z + sz;
-                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                        const bool take = (r2 <= rl2) && (HALF ? (j > i) : (j != i));
-                        if (take) {
-                            if (cnt < cap) *out = (uint32_t)j | code;
-                            out += npad;
-                            ++cnt;
+                    for (int j0 = b0; j0 < b1; j0 += LPA) {
+                        const int j = j0 + gl;
+                        bool take = false;
+                        if (j < b1 && (HALF ? (j > i) : (j != i))) {
+                            const float4 pj = prel[j];
+                            const float dx = pj.x + sx, dy = pj.y + sy, dz = pj.z + sz;
+                            take = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= rl2;
                         }
+                        append(take, j, cell_code);
                     }
                 } else {
-                    for (int j = b0; j < b1; ++j) {
-                        if (HALF ? (j <= i) : (j == i)) continue;
-                        const float4 pj = prel[j];
-                        float d[3] = {pj.x - pi.x, pj.y - pi.y, pj.z - pi.z};
-                        const int o[3] = {ox, oy, oz}, n[3] = {nx, ny, nz};
-                        const float c3[3] = {csx, csy, csz};
+                    for (int j0 = b0; j0 < b1; j0 += LPA) {
+                        const int j = j0 + gl;
+                        bool take = false;
                         uint32_t code = 0;
+                        if (j < b1 && (HALF ? (j > i) : (j != i))) {
+                            const float4 pj = prel[j];
+                            float d[3] = {pj.x - pi.x, pj.y - pi.y, pj.z - pi.z};
+                            const int o[3] = {ox, oy, oz}, n[3] = {nx, ny, nz};
+                            const float c3[3] = {csx, csy, csz};
 #pragma unroll
-                        for (int a = 0; a < 3; ++a) {
-                            if (o[a] == 0) continue;
-                            const float up = d[a] + c3[a], dn = d[a] - c3[a];
-                            const bool usep = (n[a] == 2) ? (fabsf(up) <= fabsf(dn)) : (o[a] > 0);
-                            d[a] = usep ? up : dn;
-                            code |= (usep ? 1u : 2u) << (2 * a);
+                            for (int a = 0; a < 3; ++a) {
+                                if (o[a] == 0) continue;
+                                const float up = d[a] + c3[a], dn = d[a] - c3[a];
+                                const bool usep = (n[a] == 2) ? (fabsf(up) <= fabsf(dn)) : (o[a] > 0);
+                                d[a] = usep ? up : dn;
+                                code |= (usep ? 1u : 2u) << (2 * a);
+                            }
+                            take = fmaf(d[0], d[0], fmaf(d[1], d[1], d[2] * d[2])) <= rl2;
                         }
-                        const float r2 = fmaf(d[0], d[0], fmaf(d[1], d[1], d[2] * d[2]));
-                        if (r2 <= rl2) {
-                            if (cnt < cap) *out = (uint32_t)j | (code << JBITS);
-                            out += npad;
-                            ++cnt;
-                        }
+                        append(take, j, code);
                     }
                 }
             }
         }
     }
-    if (cnt > cap) {
-        atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
-        cnt = cap;
+    if (gl == 0) {
+        if (cnt > cap) atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
+        P.nn[i] = cnt > cap ? cap : cnt;
     }
-    P.nn[i] = cnt;
 }
 
 // FP64 forces: the pair evaluation of LJVOffsetManager (src/potentials/lennard_jones.rs:214-235),
-// F_i -= f, F_j += f, PE += u.
+// F_i -= f, F_j += f, PE += u. LPA lanes share one atom, stride through its list, and reduce
+// their partial forces with tile shuffles.
 //   FULL = false: Newton-3 half list, j's share scattered with FP64 atomics (forces zeroed by
-//     integrate-1). Each lane starts its walk at a different list position so the atoms of one
-//     cell, which share most neighbours, do not hit the same j's force at the same time.
+//     integrate-1).
 //   FULL = true: full list, F_i only, no atomics; PE halved at the reduction.
 //   FAST = false: the reference's rounding sequence operation for operation (min-image through
 //     h^-1 and h, x*x+y*y+z*z, true division).
@@ -476,33 +588,32 @@ __device__ __forceinline__ double rcp_newton(double x) {
     return fma(y, e, y);
 }
 
-template <bool FULL, bool FAST>
-__global__ void k_force_fp64(const DP P, int respect_steps) {
+template <bool FULL, bool FAST, int LPA>
+__global__ void __launch_bounds__(256) k_force_fp64(const DP P, int respect_steps) {
     __shared__ double sh[32];
+    auto tile = cg::tiled_partition<LPA>(cg::this_thread_block());
     int s, i;
-    bool live = atom_of(P, s, i);
+    const bool live = group_atom_of<LPA>(P, s, i);
     if (s < 0) return;
     if (!slot_runs(P, s, respect_steps)) return;  // uniform per block (one slot per chunk)
-    double e = 0.0;
+    const int gl = (int)tile.thread_rank();
+    double e = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
     if (live) {
         const SysParams& sp = P.sp[s];
         const int cur = P.st[s].cur;
-        const double4* __restrict__ pos = P.pos[cur];
-        const double4 pi = pos[i];
+        const double4_32a* __restrict__ pos = P.pos[cur];
+        const double4_32a pi = pos[i];
         const int ti = type_of(pi.w);
         const LJDev* tab = P.tab + sp.tab0 + ti * sp.nt;
         const bool one_type = sp.nt == 1;
         const LJ64 P0 = lj64_load(tab[0]);
         const double hx = sp.h[0], hy = sp.h[1], hz = sp.h[2];
         const double ix = sp.hinv[0], iy = sp.hinv[1], iz = sp.hinv[2];
-        double fx = 0.0, fy = 0.0, fz = 0.0;
         const int nn = P.nn[i];
         const int64_t npad = P.npad;
-        int k = FULL ? 0 : (nn > 0 ? (int)(threadIdx.x & 31) % nn : 0);
-        for (int t = 0; t < nn; ++t) {
-            const int j = (int)(P.nbr[(int64_t)k * npad + i] & JMASK);
-            if (++k == nn) k = 0;
-            const double4 pj = pos[j];
+        for (int k = gl; k < nn; k += LPA) {
+            const int j = (int)(P.nbr[nbr_index<LPA>(i, k, npad)] & JMASK);
+            const double4_32a pj = pos[j];
             LJ64 L = P0;
             if (!one_type) {
                 const LJDev& T = tab[type_of(pj.w)];
@@ -561,8 +672,16 @@ __global__ void k_force_fp64(const DP P, int respect_steps) {
                 atomicAdd(&P.frc[j].z, gz);
             }
         }
+    }
+#pragma unroll
+    for (int o = LPA / 2; o > 0; o >>= 1) {
+        fx += tile.shfl_down(fx, o);
+        fy += tile.shfl_down(fy, o);
+        fz += tile.shfl_down(fz, o);
+    }
+    if (live && gl == 0) {
         if (FULL) {
-            P.frc[i] = make_double4(fx, fy, fz, 0.0);
+            P.frc[i] = make_double4_32a(fx, fy, fz, 0.0);
         } else {
             atomicAdd(&P.frc[i].x, fx);
             atomicAdd(&P.frc[i].y, fy);
@@ -574,94 +693,61 @@ __global__ void k_force_fp64(const DP P, int respect_steps) {
 }
 
 // Mixed precision forces, full list: FP32 pair arithmetic on cell-relative coordinates
-// (displacement = prel_j - prel_i + image shift). Entries are consumed in batches of 8: the 8
-// list words are loaded first, then the 8 position gathers, so each thread keeps 8 independent
-// loads in flight. Image shifts come from a 64-entry table in shared memory indexed by the
-// entry's code. Pair terms are summed in FP32 over each batch and the batch sums are added in
-// FP64 (ACC = 0), or kept as compensated FP32 sums (ACC = 1, a measured variant) and converted
-// once at the end. PE = sum_i sum_j u_ij, halved at the reduction.
-constexpr int MIX_BATCH = 8;
-
-template <int ACC>
-__global__ void __launch_bounds__(256) k_force_mixed(const DP P, int respect_steps) {
+// (displacement = prel_j - prel_i + image shift). LPA lanes share one atom and stride through its
+// list; each lane consumes its entries in batches (list words first, then the position gathers,
+// so several independent loads are in flight). Image shifts come from a 64-entry table in shared
+// memory indexed by the entry's code. Pair terms are summed in FP32 over a batch and the batch
+// sums are added in FP64 (ACC = 0), or kept as compensated FP32 sums (ACC = 1, a measured variant)
+// and converted once at the end; the group's lanes are then reduced in FP64 with tile shuffles.
+// PE = sum_i sum_j u_ij, halved at the reduction.
+template <int ACC, int LPA, bool ONE>
+__global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) {
     __shared__ double sh[32];
     __shared__ float4 shift[64];
+    auto tile = cg::tiled_partition<LPA>(cg::this_thread_block());
     int s, i;
-    bool live = atom_of(P, s, i);
+    const bool live = group_atom_of<LPA>(P, s, i);
     if (s < 0) return;
-    if (!slot_runs(P, s, respect_steps)) return;
+    if (!slot_runs(P, s, step_mode)) return;
     const SysParams& sp = P.sp[s];
     if (threadIdx.x < 64) {
+        // code -> image shift; a 3 in any field marks a padding entry and sends it out of range
         const int c = threadIdx.x;
         const int bx = c & 3, by = (c >> 2) & 3, bz = (c >> 4) & 3;
         const float fx = bx == 1 ? 1.f : (bx == 2 ? -1.f : 0.f);
         const float fy = by == 1 ? 1.f : (by == 2 ? -1.f : 0.f);
         const float fz = bz == 1 ? 1.f : (bz == 2 ? -1.f : 0.f);
-        shift[c] = make_float4(fx * sp.fcs[0], fy * sp.fcs[1], fz * sp.fcs[2], 0.f);
+        const bool pad = bx == 3 || by == 3 || bz == 3;
+        shift[c] = pad ? make_float4(1e18f, 1e18f, 1e18f, 0.f)
+                       : make_float4(fx * sp.fcs[0], fy * sp.fcs[1], fz * sp.fcs[2], 0.f);
     }
     __syncthreads();
-    double e = 0.0;
+    const int gl = (int)tile.thread_rank();
+    constexpr int MIX_BATCH = LPA >= 8 ? 4 : 8;
+    constexpr int FLUSH = 32;  // entries per lane between FP64 (or compensated) folds
+    double e = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
     if (live) {
         const float4* __restrict__ prel = P.prel;
         const float4 pi = prel[i];
         const int ti = __float_as_int(pi.w);
         const LJDev* tab = P.tab + sp.tab0 + ti * sp.nt;
-        const bool one_type = sp.nt == 1;
         const float frc2_0 = tab[0].frc2, fs2_0 = tab[0].fsigma2, fe24_0 = tab[0].feps24, fe4_0 = tab[0].feps4,
                     fuc_0 = tab[0].fucut;
-        double fx = 0.0, fy = 0.0, fz = 0.0;
-        float cx = 0.f, cy = 0.f, cz = 0.f, ce = 0.f;  // compensation terms (ACC = 1)
-        float sx = 0.f, sy = 0.f, sz = 0.f, se = 0.f;  // compensated sums (ACC = 1)
+        float cx = 0.f, cy = 0.f, cz = 0.f, ce = 0.f;  // Kahan compensation (ACC = 1)
+        float sx = 0.f, sy = 0.f, sz = 0.f, se = 0.f;  // Kahan sums (ACC = 1)
         const int nn = P.nn[i];
-        const int64_t npad = P.npad;
-        const uint32_t* __restrict__ nbp = P.nbr + i;
-        const uint32_t self = (uint32_t)i;
-        for (int k0 = 0; k0 < nn; k0 += MIX_BATCH) {
-            uint32_t ent[MIX_BATCH];
-            const uint32_t* q = nbp + (int64_t)k0 * npad;
-#pragma unroll
-            for (int b = 0; b < MIX_BATCH; ++b) {
-                ent[b] = (k0 + b < nn) ? __ldg(q) : self;
-                q += npad;
-            }
-            float4 pj[MIX_BATCH];
-#pragma unroll
-            for (int b = 0; b < MIX_BATCH; ++b) pj[b] = __ldg(prel + (ent[b] & JMASK));
-            float px = 0.f, py = 0.f, pz = 0.f, pe = 0.f;
-#pragma unroll
-            for (int b = 0; b < MIX_BATCH; ++b) {
-                const float4 sv = shift[ent[b] >> JBITS];
-                const float dx = (pj[b].x - pi.x) + sv.x;
-                const float dy = (pj[b].y - pi.y) + sv.y;
-                const float dz = (pj[b].z - pi.z) + sv.z;
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                float frc2 = frc2_0, fs2 = fs2_0, fe24 = fe24_0, fe4 = fe4_0, fuc = fuc_0;
-                if (!one_type) {
-                    const LJDev& L = tab[__float_as_int(pj[b].w)];
-                    frc2 = L.present ? L.frc2 : -1.f;
-                    fs2 = L.fsigma2;
-                    fe24 = L.feps24;
-                    fe4 = L.feps4;
-                    fuc = L.fucut;
-                }
-                if (r2 <= frc2 && r2 > 0.f) {
-                    const float inv = __fdividef(1.0f, r2);
-                    const float s2 = fs2 * inv;
-                    const float s6 = s2 * s2 * s2;
-                    const float c = fe24 * s6 * fmaf(2.0f, s6, -1.0f) * inv;
-                    px = fmaf(-c, dx, px);
-                    py = fmaf(-c, dy, py);
-                    pz = fmaf(-c, dz, pz);
-                    pe += fmaf(fe4 * s6, s6 - 1.0f, -fuc);
-                }
-            }
+        const int64_t row = P.npad * LPA;
+        const uint32_t* __restrict__ nbp = P.nbr + (int64_t)i * LPA + gl;
+        const uint32_t pad = (uint32_t)i | (63u << JBITS);
+        float px = 0.f, py = 0.f, pz = 0.f, pe = 0.f;
+        int since = 0;
+        auto fold = [&]() {
             if (ACC == 0) {
                 fx += (double)px;
                 fy += (double)py;
                 fz += (double)pz;
                 e += (double)pe;
             } else {
-                // Kahan summation of the batch sums
                 float y = px - cx, t = sx + y;
                 cx = (t - sx) - y;
                 sx = t;
@@ -675,15 +761,67 @@ __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int respect_ste
                 ce = (t - se) - y;
                 se = t;
             }
+            px = py = pz = pe = 0.f;
+        };
+        for (int k0 = 0; k0 < nn; k0 += LPA * MIX_BATCH) {
+            uint32_t ent[MIX_BATCH];
+            const uint32_t* q = nbp + (int64_t)(k0 / LPA) * row;
+#pragma unroll
+            for (int b = 0; b < MIX_BATCH; ++b) {
+                ent[b] = (k0 + b * LPA + gl < nn) ? __ldg(q) : pad;
+                q += row;
+            }
+            float4 pj[MIX_BATCH];
+#pragma unroll
+            for (int b = 0; b < MIX_BATCH; ++b) pj[b] = __ldg(prel + (ent[b] & JMASK));
+#pragma unroll
+            for (int b = 0; b < MIX_BATCH; ++b) {
+                const float4 sv = shift[ent[b] >> JBITS];
+                const float dx = (pj[b].x - pi.x) + sv.x;
+                const float dy = (pj[b].y - pi.y) + sv.y;
+                const float dz = (pj[b].z - pi.z) + sv.z;
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                float frc2 = frc2_0, fs2 = fs2_0, fe24 = fe24_0, fe4 = fe4_0, fuc = fuc_0;
+                if (!ONE) {
+                    const LJDev& L = tab[__float_as_int(pj[b].w)];
+                    frc2 = L.present ? L.frc2 : -1.f;
+                    fs2 = L.fsigma2;
+                    fe24 = L.feps24;
+                    fe4 = L.feps4;
+                    fuc = L.fucut;
+                }
+                if (r2 <= frc2) {
+                    const float inv = __fdividef(1.0f, r2);
+                    const float s2 = fs2 * inv;
+                    const float s6 = s2 * s2 * s2;
+                    const float c = fe24 * s6 * fmaf(2.0f, s6, -1.0f) * inv;
+                    px = fmaf(-c, dx, px);
+                    py = fmaf(-c, dy, py);
+                    pz = fmaf(-c, dz, pz);
+                    pe += fmaf(fe4 * s6, s6 - 1.0f, -fuc);
+                }
+            }
+            since += MIX_BATCH;
+            if (since >= FLUSH) {
+                fold();
+                since = 0;
+            }
         }
+        fold();
         if (ACC == 1) {
             fx = (double)sx - (double)cx;
             fy = (double)sy - (double)cy;
             fz = (double)sz - (double)cz;
             e = (double)se - (double)ce;
         }
-        P.frc[i] = make_double4(fx, fy, fz, 0.0);
     }
+#pragma unroll
+    for (int o = LPA / 2; o > 0; o >>= 1) {
+        fx += tile.shfl_down(fx, o);
+        fy += tile.shfl_down(fy, o);
+        fz += tile.shfl_down(fz, o);
+    }
+    if (live && gl == 0) P.frc[i] = make_double4_32a(fx, fy, fz, 0.0);
     double tot = block_sum<256>(e, sh);
     if (threadIdx.x == 0) P.pe_part[blockIdx.x] = tot;
 }
@@ -705,10 +843,10 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
     const SysState& st = P.st[s];
     const int cur = st.cur;
     double ke = 0.0;
-    double4 p = make_double4(0, 0, 0, 0), f = p;
+    double4_32a p = make_double4_32a(0, 0, 0, 0), f = p;
     if (live) {
-        double4 v = P.vel[cur][i];
-        const double4 a = P.acc[cur][i];
+        double4_32a v = P.vel[cur][i];
+        const double4_32a a = P.acc[cur][i];
         f = P.frc[i];
         const double m = v.w;
         double bx, by, bz;
@@ -734,7 +872,7 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
             }
             P.vel[cur][i] = v;
         }
-        P.acc[cur][i] = make_double4(bx, by, bz, a.w);
+        P.acc[cur][i] = make_double4_32a(bx, by, bz, a.w);
         ke = __dmul_rn(__dmul_rn(0.5, m), norm2_ref(v.x, v.y, v.z));
         if (st.want_virial) p = P.pos[cur][i];
     }
@@ -762,11 +900,13 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
     if (!sp.active) return;
     SysState& st = P.st[s];
     if (mode == 0 && st.steps_left <= 0) return;
+    if (mode != 0 && !st.eval) return;
     double pe = 0.0, ke = 0.0;
-    for (int c = threadIdx.x; c < sp.nch; c += END_THREADS) {
-        if (mode != 2) pe += P.pe_part[sp.ch0 + c];
-        if (mode != 1) ke += P.ke_part[sp.ch0 + c];
-    }
+    const int F = P.pe_stride;
+    if (mode != 2)
+        for (int c = threadIdx.x; c < sp.nch * F; c += END_THREADS) pe += P.pe_part[(int64_t)sp.ch0 * F + c];
+    if (mode != 1)
+        for (int c = threadIdx.x; c < sp.nch; c += END_THREADS) ke += P.ke_part[sp.ch0 + c];
     pe = block_sum<END_THREADS>(pe, sh);
     ke = block_sum<END_THREADS>(ke, sh);
     double w[9];
@@ -791,6 +931,10 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
             st.rebuilds += 1;
             st.rebuild = 0;
         }
+        if (mode == 2) {
+            st.eval = 0;
+            st.want_virial = 0;
+        }
         if (mode == 0) {
             P.pe_hist[(int64_t)s * P.hist + (st.steps_done % P.hist)] = pe;
             st.steps_done += 1;
@@ -799,17 +943,22 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
     }
 }
 
-// Host request for a rebuild of every active slot (force evaluation after new positions).
-__global__ void k_mark_rebuild(const DP P) {
+// Mark slots for an evaluation (all active slots, or only `only` when >= 0); with `rebuild` the
+// neighbour list is rebuilt first (new positions).
+__global__ void k_mark_eval(const DP P, int only, int rebuild, int virial) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= P.max_slots || !P.sp[s].active) return;
-    P.st[s].rebuild = 1;
+    if (only >= 0 && s != only) return;
+    P.st[s].eval = 1;
+    P.st[s].want_virial = virial;
+    if (rebuild) P.st[s].rebuild = 1;
 }
 
 __global__ void k_zero_forces(const DP P) {
     int s, i;
     if (!atom_of(P, s, i)) return;
-    P.frc[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+    if (!P.st[s].eval) return;
+    P.frc[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
 }
 
 // Exact cutoff test of every list entry of one slot with the reference arithmetic (min-image,
@@ -819,12 +968,13 @@ __global__ void k_keep(const DP P, int slot) {
     if (!atom_of(P, s, i) || s != slot) return;
     const SysParams& sp = P.sp[s];
     const int cur = P.st[s].cur;
-    const double4 pi = P.pos[cur][i];
+    const double4_32a pi = P.pos[cur][i];
     const LJDev* tab = P.tab + sp.tab0 + type_of(pi.w) * sp.nt;
+    const int L = P.pe_stride;
     for (int k = 0; k < P.nn[i]; ++k) {
-        int64_t q = (int64_t)k * P.npad + i;
+        const int64_t q = (int64_t)(k / L) * (P.npad * L) + (int64_t)i * L + k % L;
         int j = (int)(P.nbr[q] & JMASK);
-        double4 pj = P.pos[cur][j];
+        double4_32a pj = P.pos[cur][j];
         double rx = min_image_axis(__dsub_rn(pj.x, pi.x), sp.h[0], sp.hinv[0]);
         double ry = min_image_axis(__dsub_rn(pj.y, pi.y), sp.h[1], sp.hinv[1]);
         double rz = min_image_axis(__dsub_rn(pj.z, pi.z), sp.h[2], sp.hinv[2]);
@@ -839,11 +989,11 @@ __global__ void k_scale_vel(const DP P, int slot, double m0, double m1, double m
     int s, i;
     if (!atom_of(P, s, i) || s != slot) return;
     const int cur = P.st[s].cur;
-    double4 v = P.vel[cur][i];
+    double4_32a v = P.vel[cur][i];
     double x = m0 * v.x + m1 * v.y + m2 * v.z;
     double y = m3 * v.x + m4 * v.y + m5 * v.z;
     double z = m6 * v.x + m7 * v.y + m8 * v.z;
-    P.vel[cur][i] = make_double4(x, y, z, v.w);
+    P.vel[cur][i] = make_double4_32a(x, y, z, v.w);
 }
 
 // Atoms::scale_box (src/atoms/transformations.rs:5-16) for a diagonal box and diagonal M:
@@ -853,7 +1003,7 @@ __global__ void k_scale_pos(const DP P, int slot, double oh0, double oh1, double
     int s, i;
     if (!atom_of(P, s, i) || s != slot) return;
     const int cur = P.st[s].cur;
-    double4 p = P.pos[cur][i];
+    double4_32a p = P.pos[cur][i];
     p.x = nh0 * (oh0 * p.x);
     p.y = nh1 * (oh1 * p.y);
     p.z = nh2 * (oh2 * p.z);
@@ -901,6 +1051,10 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         err = "chunk size must be 256";
         return PIS_ERR_INVALID_ARGUMENT;
     }
+    if (opt.lpa != 1 && opt.lpa != 4 && opt.lpa != 8 && opt.lpa != 16 && opt.lpa != 32) {
+        err = "lanes per atom must be 1, 4, 8, 16 or 32";
+        return PIS_ERR_INVALID_ARGUMENT;
+    }
     half_ = opt.list_kind == PIS_LIST_HALF ||
             (opt.list_kind == PIS_LIST_DEFAULT && opt.precision == PIS_PRECISION_FP64);
     if (opt.precision == PIS_PRECISION_MIXED && half_) {
@@ -912,6 +1066,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         return PIS_ERR_UNSUPPORTED;
     }
     cap_ = opt.list_cap > 0 ? opt.list_cap : 192;
+    cap_ = (cap_ + 31) / 32 * 32;  // whole row groups for every lanes-per-atom choice
     npad_ = (int64_t)align_up((size_t)opt.max_atoms, 32);
     max_chunks_ = (opt.max_atoms + opt.blk - 1) / opt.blk + opt.max_slots;
     int64_t max_cells = opt.max_cells > 0 ? opt.max_cells : opt.max_atoms + opt.max_slots;
@@ -938,7 +1093,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         {(void**)&d_->cell_sys, 4 * NC}, {(void**)&d_->blk_sys, 4 * NCH},
         {(void**)&d_->blk_first, 4 * NCH}, {(void**)&d_->sp, sizeof(SysParams) * NS},
         {(void**)&d_->st, sizeof(SysState) * NS}, {(void**)&d_->tab, sizeof(LJDev) * (size_t)opt.max_types_total},
-        {(void**)&d_->pe_part, 8 * NCH}, {(void**)&d_->ke_part, 8 * NCH}, {(void**)&d_->vir_part, 72 * NCH},
+        {(void**)&d_->pe_part, 8 * NCH * 32}, {(void**)&d_->ke_part, 8 * NCH}, {(void**)&d_->vir_part, 72 * NCH},
         {(void**)&d_->pe_hist, 8 * NS * (size_t)opt.hist},
     };
     size_t total = 0;
@@ -958,6 +1113,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     d_->max_slots = opt.max_slots;
     d_->zero_forces = half_ ? 1 : 0;
     d_->full_list = half_ ? 0 : 1;
+    d_->pe_stride = opt_.lpa;
     st = check(cudaMemsetAsync(mem_, 0, total, stream_), "memset", err);
     if (st) return st;
     st = check(cudaMemsetAsync(d_->cell_sys, 0xff, 4 * NC, stream_), "memset", err);
@@ -1196,8 +1352,8 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     hp_[slot] = p;
     slot_rlist_[slot] = rlist;
 
-    // atom state: AoS (x,y,z per atom) -> double4 with the type (pos.w) and mass (vel.w)
-    std::vector<double4> hpos(d.n), hvel(d.n), hfrc(d.n), hacc(d.n);
+    // atom state: AoS (x,y,z per atom) -> double4_32a with the type (pos.w) and mass (vel.w)
+    std::vector<double4_32a> hpos(d.n), hvel(d.n), hfrc(d.n), hacc(d.n);
     std::vector<int32_t> hid(d.n);
     for (int64_t k = 0; k < d.n; ++k) {
         int t0 = type_ids[k] - 1;
@@ -1205,12 +1361,12 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
         int32_t hi = t0, lo = 0;
         uint64_t bits = ((uint64_t)(uint32_t)hi << 32) | (uint32_t)lo;
         std::memcpy(&w, &bits, 8);
-        hpos[k] = make_double4(pos[3 * k], pos[3 * k + 1], pos[3 * k + 2], w);
+        hpos[k] = make_double4_32a(pos[3 * k], pos[3 * k + 1], pos[3 * k + 2], w);
         double m = d.masses[t0];
-        hvel[k] = vel ? make_double4(vel[3 * k], vel[3 * k + 1], vel[3 * k + 2], m) : make_double4(0, 0, 0, m);
-        hfrc[k] = force ? make_double4(force[3 * k], force[3 * k + 1], force[3 * k + 2], 0.0) : make_double4(0, 0, 0, 0);
+        hvel[k] = vel ? make_double4_32a(vel[3 * k], vel[3 * k + 1], vel[3 * k + 2], m) : make_double4_32a(0, 0, 0, m);
+        hfrc[k] = force ? make_double4_32a(force[3 * k], force[3 * k + 1], force[3 * k + 2], 0.0) : make_double4_32a(0, 0, 0, 0);
         // acc = 0 + F/m (Atoms::current_acceleration) and 1/m for the mixed path
-        hacc[k] = make_double4(0.0 + hfrc[k].x / m, 0.0 + hfrc[k].y / m, 0.0 + hfrc[k].z / m, 1.0 / m);
+        hacc[k] = make_double4_32a(0.0 + hfrc[k].x / m, 0.0 + hfrc[k].y / m, 0.0 + hfrc[k].z / m, 1.0 / m);
         hid[k] = (int32_t)k;
     }
     SysState ss;
@@ -1295,6 +1451,19 @@ pis_status Engine::rebuild_block_map(std::string& err) {
     // host staging vectors must outlive the async copies
     st = check(cudaStreamSynchronize(stream_), "block map", err);
     dirty_map_ = false;
+    // the force kernel variant depends on whether every slot is single-type; captured graphs
+    // bake that choice in, so they are dropped when it flips
+    bool one = true;
+    for (int s = 0; s < opt_.max_slots; ++s)
+        if (hp_[s].active && hp_[s].nt != 1) one = false;
+    if (one != single_type_) {
+        single_type_ = one;
+        for (auto& kv : graphs_) {
+            cudaGraphExecDestroy(kv.second.exec);
+            for (auto e : kv.second.ev) cudaEventDestroy(e);
+        }
+        graphs_.clear();
+    }
     return st;
 }
 
@@ -1326,31 +1495,74 @@ void Engine::enqueue_rebuild(bool respect) {
     LAUNCH(k_scatter, (unsigned)max_chunks_, opt_.blk, P, r);
     unsigned gcells = (unsigned)((opt_.max_cells * 32 + 255) / 256);
     LAUNCH(k_gather, gcells, 256, P, (int64_t)opt_.max_cells, r);
-    if (half_)
-        LAUNCH(k_build<true>, (unsigned)max_chunks_, opt_.blk, P, r);
+    launch_build(r);
+}
+
+// Lanes-per-atom kernels are templates; these dispatch on the pool's runtime choice. Their grid
+// has lpa blocks per chunk.
+template <int L>
+static void launch_build_t(const DP& P, bool half, unsigned chunks, cudaStream_t st, int r) {
+    if (half)
+        k_build<true, L><<<chunks * L, 256, 0, st>>>(P, r);
     else
-        LAUNCH(k_build<false>, (unsigned)max_chunks_, opt_.blk, P, r);
+        k_build<false, L><<<chunks * L, 256, 0, st>>>(P, r);
+    g_launches.fetch_add(1);
+}
+
+template <int L>
+static void launch_mixed_t(const DP& P, bool kahan, bool one, unsigned chunks, cudaStream_t st, int r) {
+    if (kahan && one)
+        k_force_mixed<1, L, true><<<chunks * L, 256, 0, st>>>(P, r);
+    else if (kahan)
+        k_force_mixed<1, L, false><<<chunks * L, 256, 0, st>>>(P, r);
+    else if (one)
+        k_force_mixed<0, L, true><<<chunks * L, 256, 0, st>>>(P, r);
+    else
+        k_force_mixed<0, L, false><<<chunks * L, 256, 0, st>>>(P, r);
+    g_launches.fetch_add(1);
+}
+
+template <int L>
+static void launch_fp64_t(const DP& P, bool half, bool fast, unsigned chunks, cudaStream_t st, int r) {
+    if (half && !fast)
+        k_force_fp64<false, false, L><<<chunks * L, 256, 0, st>>>(P, r);
+    else if (half)
+        k_force_fp64<false, true, L><<<chunks * L, 256, 0, st>>>(P, r);
+    else if (!fast)
+        k_force_fp64<true, false, L><<<chunks * L, 256, 0, st>>>(P, r);
+    else
+        k_force_fp64<true, true, L><<<chunks * L, 256, 0, st>>>(P, r);
+    g_launches.fetch_add(1);
+}
+
+#define PIS_LPA_DISPATCH(lpa, CALL) \
+    switch (lpa) {                  \
+        case 4: CALL(4); break;     \
+        case 8: CALL(8); break;     \
+        case 16: CALL(16); break;   \
+        case 32: CALL(32); break;   \
+        default: CALL(1); break;    \
+    }
+
+void Engine::launch_build(int r) {
+    const unsigned ch = (unsigned)max_chunks_;
+#define PIS_CALL(L) launch_build_t<L>(*d_, half_, ch, stream_, r)
+    PIS_LPA_DISPATCH(opt_.lpa, PIS_CALL)
+#undef PIS_CALL
 }
 
 void Engine::launch_force_mixed(int r) {
-    const DP& P = *d_;
-    if (opt_.mixed_kahan)
-        LAUNCH(k_force_mixed<1>, (unsigned)max_chunks_, opt_.blk, P, r);
-    else
-        LAUNCH(k_force_mixed<0>, (unsigned)max_chunks_, opt_.blk, P, r);
+    const unsigned ch = (unsigned)max_chunks_;
+#define PIS_CALL(L) launch_mixed_t<L>(*d_, opt_.mixed_kahan, single_type_, ch, stream_, r)
+    PIS_LPA_DISPATCH(opt_.lpa, PIS_CALL)
+#undef PIS_CALL
 }
 
 void Engine::launch_force_fp64(int r) {
-    const DP& P = *d_;
-    const bool fast = opt_.fp64_fast;
-    if (half_ && !fast)
-        LAUNCH((k_force_fp64<false, false>), (unsigned)max_chunks_, opt_.blk, P, r);
-    else if (half_)
-        LAUNCH((k_force_fp64<false, true>), (unsigned)max_chunks_, opt_.blk, P, r);
-    else if (!fast)
-        LAUNCH((k_force_fp64<true, false>), (unsigned)max_chunks_, opt_.blk, P, r);
-    else
-        LAUNCH((k_force_fp64<true, true>), (unsigned)max_chunks_, opt_.blk, P, r);
+    const unsigned ch = (unsigned)max_chunks_;
+#define PIS_CALL(L) launch_fp64_t<L>(*d_, half_, opt_.fp64_fast, ch, stream_, r)
+    PIS_LPA_DISPATCH(opt_.lpa, PIS_CALL)
+#undef PIS_CALL
 }
 
 void Engine::enqueue_step(bool respect, cudaEvent_t* ev) {
@@ -1379,9 +1591,10 @@ void Engine::enqueue_step(bool respect, cudaEvent_t* ev) {
     if (ev) cudaEventRecordWithFlags(ev[5], stream_, cudaEventRecordExternal);
 }
 
-void Engine::enqueue_potential() {
+void Engine::enqueue_potential(int only) {
     const DP& P = *d_;
-    LAUNCH(k_mark_rebuild, (unsigned)((opt_.max_slots + 127) / 128), 128, P);
+    const unsigned sg = (unsigned)((opt_.max_slots + 127) / 128);
+    LAUNCH(k_mark_eval, sg, 128, P, only, 1, 0);
     LAUNCH(k_zero_forces, (unsigned)max_chunks_, opt_.blk, P);
     enqueue_rebuild(false);
     if (opt_.precision == PIS_PRECISION_MIXED)
@@ -1391,36 +1604,30 @@ void Engine::enqueue_potential() {
     LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 1);
 }
 
-pis_status Engine::compute_potential(std::string& err) {
+pis_status Engine::compute_potential(std::string& err) { return compute_potential_slot(-1, err); }
+
+pis_status Engine::compute_potential_slot(int only, std::string& err) {
     pis_status st = rebuild_block_map(err);
     if (st) return st;
-    enqueue_potential();
+    enqueue_potential(only);
     st = check(cudaGetLastError(), "launch", err);
     if (st) return st;
-    return reduce_state(true, err);
+    return reduce_state_slot(true, only, err);
 }
 
-pis_status Engine::reduce_state(bool virial, std::string& err) {
+pis_status Engine::reduce_state(bool virial, std::string& err) { return reduce_state_slot(virial, -1, err); }
+
+pis_status Engine::reduce_state_slot(bool virial, int only, std::string& err) {
     pis_status st = rebuild_block_map(err);
     if (st) return st;
     const DP& P = *d_;
-    std::vector<int32_t> wv(opt_.max_slots, virial ? 1 : 0);
-    for (int s = 0; s < opt_.max_slots; ++s)
-        if (hp_[s].active) {
-            st = check(cudaMemcpyAsync(&d_->st[s].want_virial, &wv[s], 4, cudaMemcpyHostToDevice, stream_), "flag", err);
-            if (st) return st;
-        }
+    const unsigned sg = (unsigned)((opt_.max_slots + 127) / 128);
+    LAUNCH(k_mark_eval, sg, 128, P, only, 0, virial ? 1 : 0);
     if (opt_.precision == PIS_PRECISION_MIXED)
         LAUNCH((k_integrate2<false, false>), (unsigned)max_chunks_, opt_.blk, P, 0);
     else
         LAUNCH((k_integrate2<false, true>), (unsigned)max_chunks_, opt_.blk, P, 0);
     LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 2);
-    int32_t zero = 0;
-    for (int s = 0; s < opt_.max_slots; ++s)
-        if (hp_[s].active) {
-            st = check(cudaMemcpyAsync(&d_->st[s].want_virial, &zero, 4, cudaMemcpyHostToDevice, stream_), "flag", err);
-            if (st) return st;
-        }
     st = check(cudaGetLastError(), "launch", err);
     if (st) return st;
     return sync(err);
@@ -1490,7 +1697,7 @@ pis_status Engine::download(int slot, double* pos, double* vel, double* force, s
     pis_status st = read_state(slot, ss, err);
     if (st) return st;
     const int cur = ss.cur;
-    std::vector<double4> hp(p.n), hv(p.n), hf(p.n);
+    std::vector<double4_32a> hp(p.n), hv(p.n), hf(p.n);
     std::vector<int32_t> hid(p.n);
     st = check(cudaMemcpyAsync(hid.data(), d_->id[cur] + p.a0, 4 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "download", err);
     if (st) return st;
@@ -1595,14 +1802,16 @@ pis_status Engine::neighbour_sets(int slot, std::vector<int64_t>& offsets, std::
     st = sync(err);
     if (st) return st;
     for (int32_t v : nn) maxnn = std::max(maxnn, v);
-    std::vector<uint32_t> ent((size_t)maxnn * p.n);
-    std::vector<uint8_t> kp((size_t)maxnn * p.n);
-    for (int k = 0; k < maxnn; ++k) {
-        st = check(cudaMemcpyAsync(ent.data() + (size_t)k * p.n, d_->nbr + (int64_t)k * npad_ + p.a0, 4 * (size_t)p.n,
-                                   cudaMemcpyDeviceToHost, stream_), "nbr", err);
+    const int L = opt_.lpa;
+    const int groups = (maxnn + L - 1) / L;
+    const size_t gsz = (size_t)p.n * L;  // words of one row group for this slot's atoms
+    std::vector<uint32_t> ent((size_t)groups * gsz);
+    std::vector<uint8_t> kp((size_t)groups * gsz);
+    for (int r = 0; r < groups; ++r) {
+        const int64_t off = (int64_t)r * npad_ * L + p.a0 * L;
+        st = check(cudaMemcpyAsync(ent.data() + r * gsz, d_->nbr + off, 4 * gsz, cudaMemcpyDeviceToHost, stream_), "nbr", err);
         if (st) return st;
-        st = check(cudaMemcpyAsync(kp.data() + (size_t)k * p.n, d_->keep + (int64_t)k * npad_ + p.a0, (size_t)p.n,
-                                   cudaMemcpyDeviceToHost, stream_), "keep", err);
+        st = check(cudaMemcpyAsync(kp.data() + r * gsz, d_->keep + off, gsz, cudaMemcpyDeviceToHost, stream_), "keep", err);
         if (st) return st;
     }
     st = sync(err);
@@ -1610,7 +1819,7 @@ pis_status Engine::neighbour_sets(int slot, std::vector<int64_t>& offsets, std::
     std::vector<std::vector<int32_t>> sets(p.n);
     for (int i = 0; i < p.n; ++i)
         for (int k = 0; k < nn[i]; ++k) {
-            size_t q = (size_t)k * p.n + i;
+            const size_t q = (size_t)(k / L) * gsz + (size_t)i * L + k % L;
             if (!kp[q]) continue;
             int j = (int)(ent[q] & JMASK) - (int)p.a0;
             sets[id[i]].push_back(id[j]);

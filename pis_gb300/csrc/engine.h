@@ -71,6 +71,8 @@ struct SysState {
     int32_t rebuild;      // neighbour list must be rebuilt in this step
     int32_t flags;        // FLAG_* bits
     int32_t want_virial;  // compute sum_i r_i F_i^T in the next reductions
+    int32_t eval;         // slot takes part in the next host-requested evaluation / reduction
+    int32_t pad_;
     int64_t steps_left;   // steps still to take; a slot at 0 is frozen during run()
     int64_t steps_done;
     int64_t rebuilds;
@@ -92,6 +94,7 @@ struct PoolOptions {
     int hist = 1024;           // per-slot energy history ring
     bool fp64_fast = false;    // FP64 force kernel with FMAs and Newton reciprocal (variant)
     bool mixed_kahan = false;  // mixed force kernel with compensated FP32 sums (variant)
+    int lpa = 1;               // lanes per atom in the list build and force kernels (1,4,8,16,32)
 };
 
 class Engine {
@@ -116,10 +119,13 @@ class Engine {
     pis_status set_steps(int slot, int64_t steps, std::string& err);
     // Zero forces, rebuild lists, evaluate forces + PE (+ KE and virial) for every active slot.
     pis_status compute_potential(std::string& err);
+    // The same for one slot only (the others keep their state untouched).
+    pis_status compute_potential_slot(int slot, std::string& err);
     // Run k velocity-Verlet steps on every active slot with steps_left > 0 (graph chunks).
     pis_status run(int64_t k, std::string& err);
     // KE and virial of every active slot at the current state.
     pis_status reduce_state(bool virial, std::string& err);
+    pis_status reduce_state_slot(bool virial, int slot, std::string& err);
     pis_status sync(std::string& err);
 
     pis_status download(int slot, double* pos, double* vel, double* force, std::string& err);
@@ -154,9 +160,10 @@ class Engine {
     pis_status rebuild_block_map(std::string& err);
     void enqueue_step(bool respect_steps, cudaEvent_t* ev);
     void enqueue_rebuild(bool respect_steps);
-    void enqueue_potential();
+    void enqueue_potential(int only);
     void launch_force_fp64(int respect_steps);
     void launch_force_mixed(int respect_steps);
+    void launch_build(int respect_steps);
     pis_status check(cudaError_t e, const char* what, std::string& err);
 
     PoolOptions opt_;
@@ -187,6 +194,7 @@ class Engine {
     int64_t stage_steps_ = 0;
     int64_t kernels_per_step_ = 0;
     bool dirty_map_ = true;
+    bool single_type_ = true;  // every active slot has one atom type (selects the force kernel)
 };
 
 }  // namespace pis

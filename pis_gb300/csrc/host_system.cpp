@@ -1,0 +1,407 @@
+// host_system.cpp - the reference's System / Simulation driver restated on the GPU manager
+// (include/pis_host.h): System::read (src/system.rs:49-94) parses the command file,
+// System::contextualize (:100-175) builds the velocities and the LJ table, Simulation::run
+// (src/simulation.rs:8-88) steps the ensemble, prints thermo lines and writes .lammpstrj dumps
+// (src/writers/dump_traj.rs:18-74). NVE and the Nose-Hoover-chain NVT (src/ensemble/nvt.rs) run;
+// NPT needs a triclinic box update, which the GPU engine does not support.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "host_io.h"
+#include "pis_host.h"
+
+namespace {
+
+using pis::format_f64;
+using pis::parse_f64;
+using pis::parse_i32;
+
+constexpr double KB = 0.0083144621;  // src/constants.rs:3
+
+struct StartVelocity {
+    bool present = false;
+    bool start = true;
+    bool has_t = false, has_seed = false;
+    double t = 0.0;
+    int64_t seed = 0;
+};
+
+struct NhcArgs {
+    bool present = false;
+    double t_start = 0, t_end = 0, tau = 0;
+};
+
+struct MtkArgs {
+    bool present = false;
+    double p_start = 0, tau = 0;
+};
+
+// Nose-Hoover chain of length 3 (src/ensemble/nvt.rs:4-124), literally.
+struct Nhc {
+    int m = 3;
+    double t_start = 0, t_end = 0, t_target = 0;
+    double xi[3] = {0, 0, 0}, eta[3] = {0, 0, 0}, g[3] = {0, 0, 0}, q[3] = {0, 0, 0};
+    void init(double t0, double t1, double tau) {
+        t_start = t0;
+        t_end = t1;
+        t_target = t0;
+        double qv = KB * t_target * (tau * tau);
+        double p = 1.0;
+        for (int i = 0; i < m; ++i) {
+            q[i] = qv / p;
+            p *= 10.0;
+        }
+    }
+    void compute_forces(double ke, int64_t n) {
+        g[0] = 2.0 * ke - ((double)(n * 3)) * KB * t_target;
+        for (int j = 1; j < m; ++j) g[j] = q[j - 1] * (xi[j - 1] * xi[j - 1]) - KB * t_target;
+    }
+    void propagate_half_step(double dt) {
+        int j = m - 1;
+        xi[j] = 0.5 * dt * g[j] / q[j];
+        for (int l = j - 1; l >= 0; --l) xi[l] = (0.5 * dt * g[l] / q[l]) * std::exp(-0.25 * dt * xi[l + 1]);
+    }
+    double kinetic_energy() const {
+        double e = 0.0;
+        for (int i = 0; i < m; ++i) e += 0.5 * q[i] * (xi[i] * xi[i]);
+        return e;
+    }
+    double potential_energy(int64_t n) const {
+        double e = (double)(n * 3) * KB * t_target * eta[0];
+        for (int i = 1; i < m; ++i) e += KB * t_target * eta[i];
+        return e;
+    }
+    void target(int64_t step, int64_t steps) {
+        t_target = t_start + ((t_end - t_start) / (double)steps) * (double)step;
+    }
+};
+
+}  // namespace
+
+struct pis_system {
+    std::string err;
+    // SimulationContext (src/readers/simulation_context.rs:105-131) and its defaults
+    double timestep = 0.01;
+    int64_t steps = 100;
+    bool have_atoms = false;
+    pis::DataFile data;
+    StartVelocity sv;
+    bool have_style = false;
+    std::vector<std::string> style_args;
+    std::vector<std::vector<std::string>> coeff_args;
+    NhcArgs nhc;
+    MtkArgs mtk;
+    int64_t dump_step = 1;
+    std::string dump_file = "dump.lammpstrj";
+    // contextualized state
+    std::vector<pis_lj_pair> table;
+    int32_t n_types = 0;
+    int precision = PIS_PRECISION_FP64;
+    double skin = 0.3;
+    pis_gpu_ctx* ctx = nullptr;
+    ~pis_system() {
+        if (ctx) pis_gpu_destroy(ctx);
+    }
+};
+
+namespace {
+
+pis_status sfail(pis_system* s, pis_status st, const std::string& m) {
+    s->err = m;
+    return st;
+}
+
+// One command line (src/readers/input_file/commands.rs:25-63, 66-144, 387-496).
+pis_status run_command(pis_system* s, const std::string& cmd, const std::vector<std::string>& a, int line) {
+    auto missing = [&]() { return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Missing argument on line " + std::to_string(line)); };
+    auto bad_f = [&](const std::string& t) { return sfail(s, PIS_ERR_PARSE, "Error parsing floating number from string " + t); };
+    auto bad_i = [&](const std::string& t) { return sfail(s, PIS_ERR_PARSE, "Error parsing integer number from string " + t); };
+    if (cmd == "timestep") {
+        if (a.empty()) return missing();
+        if (!parse_f64(a[0], s->timestep)) return bad_f(a[0]);
+    } else if (cmd == "run") {
+        int32_t v;
+        if (a.empty()) return missing();
+        if (!parse_i32(a[0], v)) return bad_i(a[0]);
+        if (v < 0) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Negative value not allowed on line " + std::to_string(line));
+        s->steps = v;
+    } else if (cmd == "velocity") {
+        if (a.size() < 2) return missing();
+        if (a[1] != "create") return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Invalid argument: " + a[1]);
+        StartVelocity v;
+        v.present = true;
+        size_t k = 2;
+        if (k >= a.size()) return missing();
+        if (!parse_f64(a[k], v.t)) return bad_f(a[k]);
+        v.has_t = true;
+        ++k;
+        int32_t seed;
+        v.has_seed = true;
+        v.seed = 0;
+        if (k < a.size() && parse_i32(a[k], seed)) {
+            if (seed < 0) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Negative value not allowed");
+            v.seed = seed;
+            ++k;
+        }
+        while (k < a.size()) {
+            const std::string& kw = a[k++];
+            if (kw != "dist") return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Invalid argument: " + kw);
+            if (k >= a.size()) return missing();
+            const std::string& d = a[k++];
+            if (d != "uniform" && d != "gaussian") return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Invalid argument: " + d);
+        }
+        s->sv = v;  // replaces whatever read_data set (commands.rs:139)
+    } else if (cmd == "read_data") {
+        if (a.empty()) return missing();
+        std::string e;
+        pis_status st = pis::read_data_file(a[0], s->data, e);
+        if (st) return sfail(s, st, e);
+        s->have_atoms = true;
+        if (s->sv.present) {
+            s->sv.start = !s->data.has_velocities;
+        } else {
+            s->sv = StartVelocity();
+            s->sv.present = true;
+            s->sv.start = !s->data.has_velocities;
+        }
+    } else if (cmd == "fix") {
+        if (a.size() < 3) return missing();
+        const std::string& style = a[2];
+        size_t k = 3;
+        while (k < a.size()) {
+            const std::string& kw = a[k++];
+            double x[3];
+            if (kw != "temp" && kw != "iso") return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Invalid argument: " + kw);
+            for (int q = 0; q < 3; ++q) {
+                if (k >= a.size()) return missing();
+                if (!parse_f64(a[k], x[q])) return bad_f(a[k]);
+                ++k;
+            }
+            if (kw == "temp" && (style == "npt" || style == "nvt")) {
+                s->nhc.present = true;
+                s->nhc.t_start = x[0];
+                s->nhc.t_end = x[1];
+                s->nhc.tau = x[2];
+            }
+            if (kw == "iso" && style == "npt") {
+                s->mtk.present = true;
+                s->mtk.p_start = x[0];
+                s->mtk.tau = x[2];
+            }
+        }
+    } else if (cmd == "pair_style") {
+        s->have_style = true;
+        s->style_args = a;
+        s->coeff_args.clear();
+    } else if (cmd == "pair_coeff") {
+        if (!s->have_style)
+            return sfail(s, PIS_ERR_MISSING_POTENTIAL,
+                         "Potential manager not initialized - missing pair_style or pair_coeff commands");
+        s->coeff_args.push_back(a);
+    } else if (cmd == "dump") {
+        if (a.size() < 4) return missing();
+        int32_t v;
+        if (!parse_i32(a[3], v)) return bad_i(a[3]);
+        if (v < 0) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Negative value not allowed");
+        if (a.size() < 5) return missing();
+        s->dump_step = v;
+        s->dump_file = a[4];
+    } else {
+        return sfail(s, PIS_ERR_PARSE, "Invalid command " + cmd + " found line: " + std::to_string(line));
+    }
+    return PIS_OK;
+}
+
+// System::contextualize (src/system.rs:100-175).
+pis_status contextualize(pis_system* s) {
+    if (s->have_atoms) {
+        if (s->data.n == 0) return sfail(s, PIS_ERR_NO_ATOMS, "No atoms defined in input file");
+        if (s->sv.present && s->sv.start) {
+            const double t = s->sv.has_t ? s->sv.t : 300.0;
+            const uint64_t seed = s->sv.has_seed ? (uint64_t)s->sv.seed : 0;
+            std::vector<double> m(s->data.n);
+            for (int64_t i = 0; i < s->data.n; ++i) {
+                int32_t ty = s->data.type_ids[i];
+                if (ty < 1 || ty > (int32_t)s->data.masses.size())
+                    return sfail(s, PIS_ERR_INVALID_ATOM_TYPE, "Atom type " + std::to_string(ty) + " out of range");
+                m[i] = s->data.masses[ty - 1];
+            }
+            pis::maxwell_boltzmann(s->data.n, m.data(), t, seed, s->data.vel.data());
+        }
+    }
+    s->table = s->data.pairs;  // the data file's PairCoeffs manager (commands.rs:367-369)
+    if (s->have_style) {
+        if (s->style_args.empty()) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Missing argument");
+        if (s->style_args[0] != "lj/cut")
+            return sfail(s, PIS_ERR_UNKNOWN_PAIR_STYLE, "Unknown pair style: '" + s->style_args[0] + "'");
+        double rc_global;
+        if (s->style_args.size() < 2) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Missing argument");
+        if (!parse_f64(s->style_args[1], rc_global))
+            return sfail(s, PIS_ERR_PARSE, "Error parsing floating number from string " + s->style_args[1]);
+        s->table.clear();
+        for (const auto& c : s->coeff_args) {
+            int32_t i, j;
+            double eps, sigma, rc;
+            if (c.size() < 4) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Missing argument");
+            if (!parse_i32(c[0], i) || !parse_i32(c[1], j)) return sfail(s, PIS_ERR_PARSE, "Error parsing integer");
+            if (i < 0 || j < 0) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Negative value not allowed");
+            if (!parse_f64(c[2], eps) || !parse_f64(c[3], sigma)) return sfail(s, PIS_ERR_PARSE, "Error parsing float");
+            if (c.size() < 5 || !parse_f64(c[4], rc)) rc = rc_global;
+            // the reference keys the table by (i, j) as written and looks pairs up by (min, max):
+            // a row written with i > j is never found, so it is not entered here either
+            if (i > j) continue;
+            pis_lj_pair p{i, j, eps, sigma, rc, 1};
+            bool replaced = false;
+            for (auto& q : s->table)
+                if (q.ti == i && q.tj == j) {
+                    q = p;
+                    replaced = true;
+                }
+            if (!replaced) s->table.push_back(p);
+        }
+    }
+    // two-type PairCoeffs rows written "i j ..." with i > j are unreachable likewise
+    std::vector<pis_lj_pair> t2;
+    for (const auto& p : s->table)
+        if (p.ti <= p.tj) t2.push_back(p);
+    s->table = t2;
+    s->n_types = (int32_t)s->data.masses.size();
+    return PIS_OK;
+}
+
+void write_dump(std::ofstream& o, int64_t step, int64_t n, const int32_t* types, const double* pos, const double h[3]) {
+    o << "ITEM: TIMESTEP\n" << step << "\nITEM: NUMBER OF ATOMS\n" << n << "\nITEM: BOX BOUNDS pp pp pp\n";
+    for (int a = 0; a < 3; ++a) o << "0 " << format_f64(h[a]) << "\n";
+    o << "ITEM: ATOMS id type x y z\n";
+    for (int64_t i = 0; i < n; ++i)
+        o << (i + 1) << " " << types[i] << " " << format_f64(pos[3 * i]) << " " << format_f64(pos[3 * i + 1]) << " "
+          << format_f64(pos[3 * i + 2]) << "\n";
+}
+
+}  // namespace
+
+extern "C" {
+
+pis_status pis_system_open(const char* infile, int32_t precision, double skin, pis_system** out) {
+    if (!infile || !out) return PIS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    auto s = std::make_unique<pis_system>();
+    s->precision = precision;
+    s->skin = skin;
+    std::ifstream in(infile);
+    if (!in) return PIS_ERR_IO;
+    std::string raw;
+    int line = 0;
+    while (std::getline(in, raw)) {
+        ++line;
+        std::string l = pis::trim(raw);
+        if (l.empty() || l[0] == '#') continue;
+        size_t h = l.find('#');
+        if (h != std::string::npos) l = pis::trim(l.substr(0, h));
+        std::vector<std::string> sp = pis::split_ws(l);
+        if (sp.size() < 2) continue;
+        std::vector<std::string> args(sp.begin() + 1, sp.end());
+        pis_status st = run_command(s.get(), sp[0], args, line);
+        if (st) {
+            *out = s.release();
+            return st;
+        }
+    }
+    pis_status st = contextualize(s.get());
+    *out = s.release();
+    return st;
+}
+
+int64_t pis_system_steps(const pis_system* s) { return s ? s->steps : 0; }
+double pis_system_timestep(const pis_system* s) { return s ? s->timestep : 0.0; }
+int32_t pis_system_ensemble(const pis_system* s) {
+    if (!s) return -1;
+    if (s->nhc.present && s->mtk.present) return 2;
+    return s->nhc.present ? 1 : 0;
+}
+const char* pis_system_last_error(const pis_system* s) { return s ? s->err.c_str() : "null system"; }
+void pis_system_close(pis_system* s) { delete s; }
+
+pis_status pis_system_state(pis_system* s, double* pos, double* vel, double* force) {
+    if (!s || !s->ctx) return PIS_ERR_STATE;
+    return pis_gpu_get_state(s->ctx, pos, vel, force);
+}
+
+pis_status pis_system_run(pis_system* s, const char* thermo_path) {
+    if (!s) return PIS_ERR_INVALID_ARGUMENT;
+    if (!s->have_atoms) return sfail(s, PIS_ERR_NO_ATOMS, "No atoms defined in input file");
+    if (s->table.empty())
+        return sfail(s, PIS_ERR_MISSING_POTENTIAL, "Potential manager not initialized - missing pair_style or pair_coeff commands");
+    const int ens = pis_system_ensemble(s);
+    if (ens == 2)
+        return sfail(s, PIS_ERR_UNSUPPORTED, "NPT needs a triclinic box update, which the GPU engine does not support");
+    FILE* th = thermo_path ? std::fopen(thermo_path, "w") : stdout;
+    if (!th) return sfail(s, PIS_ERR_IO, "cannot open thermo output");
+    std::unique_ptr<FILE, int (*)(FILE*)> th_guard(thermo_path ? th : nullptr, [](FILE* f) { return f ? std::fclose(f) : 0; });
+    std::ofstream dump(s->dump_file);
+    if (!dump) return sfail(s, PIS_ERR_IO, "Failed to create trajectory file '" + s->dump_file + "'");
+    const pis::DataFile& d = s->data;
+    const int64_t n = d.n;
+    pis_status st = pis_gpu_create(s->table.data(), (int32_t)s->table.size(), s->n_types, s->skin, s->precision, &s->ctx);
+    if (st) return sfail(s, st, "pis_gpu_create failed");
+    const double h[3] = {d.bounds[1] - d.bounds[0], d.bounds[3] - d.bounds[2], d.bounds[5] - d.bounds[4]};
+    const double hc[9] = {h[0], 0, 0, 0, h[1], 0, 0, 0, h[2]};
+    const uint8_t pbc[3] = {1, 1, 1};
+    st = pis_gpu_set_state(s->ctx, n, d.type_ids.data(), d.masses.data(), d.pos.data(), d.vel.data(), nullptr, hc, pbc);
+    if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
+    const double vol = std::fabs(h[0] * (h[1] * h[2]));
+    std::vector<double> pos(3 * n);
+    write_dump(dump, 0, n, d.type_ids.data(), d.pos.data(), h);
+    double pe = 0.0;
+    st = pis_gpu_compute_potential(s->ctx, &pe, nullptr);
+    if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
+    std::fprintf(th, "%d %s\n", 0, format_f64(pe).c_str());
+    Nhc nhc;
+    if (ens == 1) nhc.init(s->nhc.t_start, s->nhc.t_end, s->nhc.tau);
+    const double dt = s->timestep;
+    for (int64_t i = 0; i < s->steps; ++i) {
+        double ke = 0.0, w[9];
+        if (ens == 1) {
+            // verlet_step_nvt_nhc (src/potentials/potential.rs:35-58)
+            st = pis_gpu_reductions(s->ctx, &ke, nullptr);
+            if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
+            nhc.compute_forces(ke, n);
+            nhc.propagate_half_step(dt);
+            const double scale = std::exp(-0.5 * dt * nhc.xi[0]);
+            const double m[9] = {scale, 0, 0, 0, scale, 0, 0, 0, scale};
+            st = pis_gpu_scale_velocities(s->ctx, m);
+            if (!st) st = pis_gpu_verlet_step_nve(s->ctx, dt, 1, &pe);
+            if (!st) st = pis_gpu_scale_velocities(s->ctx, m);
+            if (!st) st = pis_gpu_reductions(s->ctx, &ke, nullptr);
+            if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
+            nhc.compute_forces(ke, n);
+            nhc.propagate_half_step(dt);
+            nhc.target(i, s->steps);
+        } else {
+            st = pis_gpu_verlet_step_nve(s->ctx, dt, 1, &pe);
+            if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
+        }
+        // Simulation::output (src/simulation.rs:66-88)
+        if (s->dump_step > 0 && ((i + 1) % s->dump_step) == 0) {
+            st = pis_gpu_get_state(s->ctx, pos.data(), nullptr, nullptr);
+            if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
+            write_dump(dump, i + 1, n, d.type_ids.data(), pos.data(), h);
+        }
+        st = pis_gpu_reductions(s->ctx, &ke, w);
+        if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
+        double ham = pe + ke;
+        if (ens == 1) ham += nhc.kinetic_energy() + nhc.potential_energy(n);
+        const double temp = (2.0 * ke) / ((double)(3 * n) * KB);
+        const double press = (2.0 * ke + (w[0] + w[4] + w[8])) / (3.0 * vol);
+        std::fprintf(th, "%lld %.3f %.3f %.3f %.3f %.3f\n", (long long)(i + 1), pe, ke, ham, temp, press);
+    }
+    std::fflush(th);
+    return dump.good() ? PIS_OK : sfail(s, PIS_ERR_IO, "Failed to write trajectory file");
+}
+
+}  // extern "C"

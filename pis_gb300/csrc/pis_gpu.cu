@@ -20,6 +20,7 @@ struct pis_gpu_ctx {
     int list_kind = PIS_LIST_DEFAULT;
     bool fp64_fast = false;
     bool mixed_kahan = false;
+    int lpa = 1;
     std::unique_ptr<pis::Engine> eng;
     int slot = -1;
     int64_t n = 0;
@@ -94,8 +95,12 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
     if (!ctx) return PIS_ERR_INVALID_ARGUMENT;
     if (list_kind < PIS_LIST_DEFAULT || list_kind > PIS_LIST_FULL)
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown list kind");
-    if (flags & ~(PIS_OPT_FP64_FAST | PIS_OPT_MIXED_KAHAN))
+    if (flags & ~(PIS_OPT_FP64_FAST | PIS_OPT_MIXED_KAHAN | PIS_OPT_LANES(0xff)))
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown option flag");
+    const int lanes = (flags >> 8) & 0xff;
+    if (lanes != 0 && lanes != 1 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+        return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "lanes per atom must be 1, 4, 8, 16 or 32");
+    ctx->lpa = lanes ? lanes : 1;
     ctx->fp64_fast = (flags & PIS_OPT_FP64_FAST) != 0;
     ctx->mixed_kahan = (flags & PIS_OPT_MIXED_KAHAN) != 0;
     if (ctx->precision == PIS_PRECISION_MIXED && list_kind == PIS_LIST_HALF)
@@ -135,6 +140,7 @@ pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_id
     opt.list_kind = ctx->list_kind;
     opt.fp64_fast = ctx->fp64_fast;
     opt.mixed_kahan = ctx->mixed_kahan;
+    opt.lpa = ctx->lpa;
     opt.max_atoms = n;
     opt.max_slots = 1;
     int64_t ncell = 1;

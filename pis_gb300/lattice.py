@@ -5,16 +5,16 @@ velocities.
   (src/bin/sapphire/main.rs:17-24, 61-76): cells ix -> iy -> iz, then the basis
   (0,0,0), (0,1/2,1/2), (1/2,0,1/2), (1/2,1/2,0), positions = a * (cell + basis).
 * ``maxwell_boltzmann`` draws N(0, sqrt(KB T / m)) components (src/atoms/velocities.rs:17-33)
-  from this project's own seeded generator (numpy PCG64 + standard normal), then removes the
-  centre-of-mass drift and rescales to T exactly as src/atoms/velocities.rs:35-59 do. The
-  reference's own random stream (rand SmallRng + rand_distr Normal) is not reproduced; states
-  are exchanged with it through the data file's Velocities section instead.
+  from this project's own seeded generator (SplitMix64 + Box-Muller, in the C++ host library),
+  then removes the centre-of-mass drift and rescales to T as src/atoms/velocities.rs:35-59 do.
+  The reference's own random stream (rand SmallRng + rand_distr Normal) is not reproduced;
+  states are exchanged with it through the data file's Velocities section instead.
 """
 from __future__ import annotations
 
 import numpy as np
 
-from .atoms import KB_KJPERMOLEKELVIN
+from .atoms import KB_KJPERMOLEKELVIN  # noqa: F401
 
 FCC_BASIS = np.array([[0.0, 0.0, 0.0], [0.0, 0.5, 0.5], [0.5, 0.0, 0.5], [0.5, 0.5, 0.0]])
 
@@ -32,23 +32,10 @@ def fcc_lattice_constant(rho: float) -> float:
 
 
 def maxwell_boltzmann(masses_per_atom: np.ndarray, temperature: float, seed: int) -> np.ndarray:
-    m = np.asarray(masses_per_atom, dtype=np.float64)
-    n = m.shape[0]
-    rng = np.random.Generator(np.random.PCG64(seed))
-    sigma = np.sqrt(KB_KJPERMOLEKELVIN * temperature / m)
-    v = rng.standard_normal((n, 3)) * sigma[:, None]
-    # remove_drift: v -= (sum m v) / (sum m)
-    total_mass = 0.0
-    p = np.zeros(3)
-    for i in range(0, n, 65536):
-        total_mass += float(np.sum(m[i:i + 65536]))
-        p += np.sum(v[i:i + 65536] * m[i:i + 65536, None], axis=0)
-    v -= p / total_mass
-    # rescale_to_temperature: lambda = sqrt(T / T_current)
-    ke = float(np.sum(0.5 * m * np.sum(v * v, axis=1)))
-    t_now = 2.0 * ke / (3 * n * KB_KJPERMOLEKELVIN)
-    v *= np.sqrt(temperature / t_now)
-    return v
+    """Seeded Maxwell-Boltzmann velocities, drift removed and rescaled to T (the library's
+    generator, include/pis_host.h: pis_maxwell_boltzmann)."""
+    from .io import maxwell_boltzmann as mb
+    return mb(masses_per_atom, temperature, seed)
 
 
 def reduced_temperature(t_star: float) -> float:

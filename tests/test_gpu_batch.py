@@ -1,0 +1,141 @@
+"""Batched replicas and the served-job loop (pis_batch_*, pis_serve_run) through the C ABI.
+
+Each slot's arithmetic is independent of every other slot's, so a job must give bit-identical
+results alone and in any mix (mixed precision: the full-list path has no atomics). FP64 replicas
+are checked against the oracle, and a replica with injected NaN velocities must fail alone.
+"""
+import numpy as np
+import pytest
+
+from systems import liquid, to_oracle
+
+pytestmark = pytest.mark.gpu
+
+JOBS = [(5, 0.95, 0.5, 11), (6, 0.80, 1.2, 12), (7, 0.70, 0.9, 13), (5, 0.85, 1.5, 14), (8, 0.8442, 0.72, 15)]
+
+
+def _batch(precision="mixed", atoms=20000, slots=8):
+    from pis_gb300.batch import Batch
+    return Batch(atoms, slots, 0, precision=precision)
+
+
+def _run_alone(k, rho, t, seed, steps):
+    from pis_gb300.batch import lj_job
+    b = _batch()
+    s = b.admit_lj(lj_job(k, rho, t, steps, seed))
+    b.advance(steps)
+    r = b.result(s, 4 * k ** 3)
+    b.close()
+    return r
+
+
+def test_alone_equals_mix_bitwise(cuda_lib):
+    from pis_gb300.batch import lj_job
+    steps = 120
+    alone = [_run_alone(k, rho, t, seed, steps) for (k, rho, t, seed) in JOBS]
+    b = _batch()
+    slots = {}
+    # staggered admission: three jobs first, the rest join while those are running
+    for q in (0, 1, 2):
+        k, rho, t, seed = JOBS[q]
+        slots[q] = b.admit_lj(lj_job(k, rho, t, steps, seed))
+    b.advance(37)
+    for q in (3, 4):
+        k, rho, t, seed = JOBS[q]
+        slots[q] = b.admit_lj(lj_job(k, rho, t, steps, seed))
+    b.advance(steps)  # the early jobs stop at their own step count
+    assert sorted(b.poll()) == sorted(slots.values())
+    for q, (k, rho, t, seed) in enumerate(JOBS):
+        r = b.result(slots[q], 4 * k ** 3)
+        assert r["steps"] == steps
+        assert np.array_equal(r["pos"], alone[q]["pos"]), q
+        assert np.array_equal(r["vel"], alone[q]["vel"]), q
+        assert r["pe"] == alone[q]["pe"] and r["ke"] == alone[q]["ke"], q
+    b.close()
+
+
+def test_batch_matches_single_context(cuda_lib):
+    from pis_gb300.batch import Batch
+    from pis_gb300.potentials import GpuContext
+    s = liquid(nc=6, seed=8)
+    b = Batch(4000, 2, 0, precision="mixed")
+    slot = b.admit(s["pos"], s["types"], s["masses"], s["h"], s["table"], 60, velocities=s["vel"])
+    b.advance(60)
+    r = b.result(slot, len(s["pos"]))
+    g = GpuContext(s["table"], 1, precision="mixed")
+    g.set_state(s["pos"], s["types"], s["masses"], s["h"], velocities=s["vel"])
+    g.compute_potential(False)
+    g.verlet_step_nve(0.005, 60)
+    pos, vel, _ = g.get_state()
+    assert np.array_equal(pos, r["pos"]) and np.array_equal(vel, r["vel"])
+
+
+def test_fp64_replicas_match_oracle(oracle_lib, cuda_lib):
+    from pis_gb300.batch import Batch
+    systems = [liquid(nc=6, rho=0.8442, seed=21), liquid(nc=7, rho=0.8, seed=22)]
+    b = Batch(6000, 4, 0, precision="fp64")
+    slots = [b.admit(s["pos"], s["types"], s["masses"], s["h"], s["table"], 40, velocities=s["vel"]) for s in systems]
+    b.advance(40)
+    for s, slot in zip(systems, slots):
+        o = to_oracle(s)
+        pe_ref, _ = o.run_nve(0.005, 40)
+        r = b.result(slot, len(s["pos"]))
+        d = r["pos"] - o.pos
+        d -= s["h"][0, 0] * np.round(d / s["h"][0, 0])
+        assert np.abs(d).max() <= 1e-9
+        hist = b.pe_history(slot, 40)
+        assert np.max(np.abs(hist - pe_ref[1:]) / np.abs(pe_ref[1:])) <= 1e-11
+
+
+def test_served_stream_results_match_alone(cuda_lib):
+    from pis_gb300.batch import lj_job
+    reqs = [(0.00, lj_job(5, 0.9, 0.8, 80, 31)), (0.00, lj_job(6, 0.8, 1.0, 150, 32)),
+            (0.02, lj_job(5, 0.75, 1.3, 60, 33)), (0.05, lj_job(7, 0.85, 0.6, 100, 34)),
+            (0.05, lj_job(6, 0.95, 1.1, 40, 35)), (0.08, lj_job(5, 0.8442, 0.72, 120, 36))]
+    b = _batch(atoms=4500, slots=3)  # too small for all at once: later requests wait for releases
+    res, wall = b.serve(reqs, graph_steps=25)
+    assert wall > 0
+    for (t, job), r in zip(reqs, res):
+        assert r["status"] == 0
+        assert r["steps"] == job.steps
+        assert r["admitted_s"] >= t - 1e-9 and r["finished_s"] >= r["admitted_s"]
+        alone = _run_alone(job.k, job.rho, job.t_star, job.seed, job.steps)
+        assert r["pe"] == alone["pe"] and r["ke"] == alone["ke"]
+    b.close()
+
+
+def test_admission_refuses_what_does_not_fit(cuda_lib):
+    from pis_gb300 import PisError
+    from pis_gb300.batch import lj_job
+    b = _batch(atoms=1000, slots=2)
+    big = lj_job(8, 0.8, 1.0, 10, 1)  # 2048 atoms
+    assert not b.fits_lj(big)
+    with pytest.raises(PisError) as e:
+        b.admit_lj(big)
+    assert e.value.name == "PIS_ERR_NO_MEMORY"
+    small = lj_job(5, 0.8, 1.0, 10, 1)
+    assert b.fits_lj(small)
+    b.admit_lj(small)
+    b.close()
+
+
+def test_nan_replica_fails_alone(cuda_lib):
+    from pis_gb300 import PisError
+    from pis_gb300.batch import Batch
+    good = liquid(nc=6, seed=41)
+    bad = liquid(nc=6, seed=42)
+    bad["vel"] = bad["vel"].copy()
+    bad["vel"][17] = np.nan
+    b = Batch(4000, 2, 0, precision="mixed")
+    sg = b.admit(good["pos"], good["types"], good["masses"], good["h"], good["table"], 50, velocities=good["vel"])
+    sb = b.admit(bad["pos"], bad["types"], bad["masses"], bad["h"], bad["table"], 50, velocities=bad["vel"])
+    b.advance(50)
+    with pytest.raises(PisError) as e:
+        b.result(sb, len(bad["pos"]))
+    assert e.value.name == "PIS_ERR_NAN_DETECTED"
+    r = b.result(sg, len(good["pos"]))
+    ref = Batch(2000, 1, 0, precision="mixed")
+    s2 = ref.admit(good["pos"], good["types"], good["masses"], good["h"], good["table"], 50, velocities=good["vel"])
+    ref.advance(50)
+    r2 = ref.result(s2, len(good["pos"]))
+    assert np.array_equal(r["pos"], r2["pos"])

@@ -56,12 +56,13 @@ def test_force_pe_virial_argon_fp64(argon_c1, list_kind):
     assert np.abs(w - w_ref).max() <= FP64_TOL * scale
 
 
+@pytest.mark.parametrize("lanes", [1, 8, 16])
 @pytest.mark.parametrize("fast", [False, True])
 @pytest.mark.parametrize("list_kind", ["half", "full"])
-def test_force_pe_liquid_fp64(liquid_melt, list_kind, fast):
+def test_force_pe_liquid_fp64(liquid_melt, list_kind, fast, lanes):
     o = to_oracle(liquid_melt)
     pe_ref = o.compute_potential()
-    g = to_gpu(liquid_melt, "fp64", list_kind=list_kind, fp64_fast=fast)
+    g = to_gpu(liquid_melt, "fp64", list_kind=list_kind, fp64_fast=fast, lanes=lanes)
     pe, f = g.compute_potential()
     assert abs(pe - pe_ref) <= FP64_TOL * abs(pe_ref)
     assert rel_norm(f, o.force) <= FP64_TOL
@@ -83,11 +84,12 @@ def test_neighbour_sets_exact_argon_example_lattice(oracle_lib, cuda_lib):
     assert _sets(off, idx) == ref_sets
 
 
+@pytest.mark.parametrize("lanes", [1, 4, 8, 32])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_neighbour_sets_exact_liquid(liquid_melt, precision):
+def test_neighbour_sets_exact_liquid(liquid_melt, precision, lanes):
     o = to_oracle(liquid_melt)
     off_r, idx_r = o.full_list()
-    g = to_gpu(liquid_melt, precision)
+    g = to_gpu(liquid_melt, precision, lanes=lanes)
     off, idx = g.neighbour_list()
     ref_sets = [tuple(sorted(x)) for x in _sets(off_r, idx_r)]
     assert _sets(off, idx) == ref_sets
@@ -123,11 +125,12 @@ def test_trajectory_100_steps_liquid(liquid_melt, fast):
     assert st["rebuilds"] >= 2  # the skin test fired during the run
 
 
+@pytest.mark.parametrize("lanes", [1, 4, 8, 32])
 @pytest.mark.parametrize("kahan", [False, True])
-def test_mixed_force_error(liquid_melt, kahan):
+def test_mixed_force_error(liquid_melt, kahan, lanes):
     o = to_oracle(liquid_melt)
     pe_ref = o.compute_potential()
-    g = to_gpu(liquid_melt, "mixed", mixed_kahan=kahan)
+    g = to_gpu(liquid_melt, "mixed", mixed_kahan=kahan, lanes=lanes)
     pe, f = g.compute_potential()
     rms = np.sqrt(np.sum((f - o.force) ** 2) / np.sum(o.force ** 2))
     assert rms <= 1e-5, rms

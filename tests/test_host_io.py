@@ -1,0 +1,107 @@
+"""The C++ host side (include/pis_host.h) without a GPU: data-file reader parity with the oracle's
+restatement of the reference reader, Rust-style float formatting, restart round trip, velocity
+generator, and input-file parsing."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import reference_file
+
+
+@pytest.fixture(scope="module")
+def io(oracle_lib):
+    from pis_gb300 import build
+    build.build()
+    from pis_gb300 import io as pio
+    return pio
+
+
+@pytest.mark.parametrize("name", ["argon4000.txt", "example.txt", "example2.txt", "data.txt", "data_run.txt"])
+def test_reader_matches_oracle_reader(io, name):
+    import oracle
+    path = reference_file("example", name)
+    a = io.read_data(path)
+    b = oracle.read_data(path)
+    for k in ("n_atoms", "xlo", "xhi", "ylo", "yhi", "zlo", "zhi", "start_velocities", "table"):
+        assert a[k] == b[k], k
+    assert np.array_equal(a["masses"], b["masses"])
+    assert np.array_equal(a["type_ids"], b["type_ids"])
+    assert np.array_equal(a["positions"], b["positions"])
+    assert np.array_equal(a["velocities"], b["velocities"])
+
+
+def test_reader_errors(io, tmp_path):
+    from pis_gb300 import PisError
+    p = tmp_path / "bad.txt"
+    p.write_text("2 atoms\n1 atom types\n\nMasses\n1 1.0\n\nAtoms\n1 1 0 0 0\n3 1 1 1 1\n")
+    with pytest.raises(PisError) as e:
+        io.read_data(str(p))
+    assert e.value.name == "PIS_ERR_ATOM_COUNT"
+    p.write_text("1 atoms\n1 atom types\n\nAtoms\n1 1 0 x 0\n")
+    with pytest.raises(PisError) as e:
+        io.read_data(str(p))
+    assert e.value.name == "PIS_ERR_PARSE"
+    with pytest.raises(PisError) as e:
+        io.read_data(str(tmp_path / "missing.txt"))
+    assert e.value.name == "PIS_ERR_IO"
+
+
+@pytest.mark.parametrize("v,s", [(1.0, "1"), (0.1, "0.1"), (-0.0, "-0"), (0.0, "0"), (1e21, "1000000000000000000000"),
+                                 (1e-7, "0.0000001"), (2.705, "2.705"), (18.935000000000002, "18.935000000000002"),
+                                 (float("nan"), "NaN"), (float("inf"), "inf"), (-1.5e-3, "-0.0015")])
+def test_format_like_rust(io, v, s):
+    assert io.format_f64(v) == s
+
+
+def test_format_round_trips(io):
+    rng = np.random.default_rng(0)
+    for v in np.concatenate([rng.normal(0, 10, 200), rng.normal(0, 1e-5, 50), rng.normal(0, 1e8, 50)]):
+        assert float(io.format_f64(v)) == v
+
+
+def test_restart_round_trip(io, tmp_path):
+    rng = np.random.default_rng(3)
+    n = 50
+    pos = rng.uniform(0, 10, (n, 3))
+    vel = rng.normal(0, 1, (n, 3))
+    types = rng.integers(1, 3, n).astype(np.int32)
+    path = str(tmp_path / "restart.txt")
+    io.write_data(path, pos, types, [1.0, 2.5], [0, 10, 0, 10, 0, 10], {(1, 1): (1.0, 1.0, 2.5)}, vel)
+    d = io.read_data(path)
+    assert np.array_equal(d["positions"], pos) and np.array_equal(d["velocities"], vel)
+    assert np.array_equal(d["type_ids"], types) and not d["start_velocities"]
+    assert d["table"] == {(1, 1): (1.0, 1.0, 2.5)}
+
+
+def test_maxwell_boltzmann(io):
+    m = np.full(1000, 39.948)
+    v = io.maxwell_boltzmann(m, 100.0, 5)
+    assert np.array_equal(v, io.maxwell_boltzmann(m, 100.0, 5))
+    assert not np.array_equal(v, io.maxwell_boltzmann(m, 100.0, 6))
+    assert np.abs((m[:, None] * v).sum(0)).max() < 1e-9
+    ke = 0.5 * np.sum(m[:, None] * v * v)
+    assert 2 * ke / (3 * 1000 * 0.0083144621) == pytest.approx(100.0, rel=1e-12)
+    assert abs(np.std(v) / np.sqrt(0.0083144621 * 100 / 39.948) - 1) < 0.05
+
+
+def test_input_file_parsing(io, tmp_path):
+    from pis_gb300 import PisError
+    d = tmp_path / "d.txt"
+    d.write_text("4 atoms\n1 atom types\n0 10 xlo xhi\n0 10 ylo yhi\n0 10 zlo zhi\nMasses\n1 1.0\n"
+                 "Atoms\n1 1 1 1 1\n2 1 2 2 2\n3 1 5 5 5\n4 1 6 6 6\n")
+    inp = tmp_path / "in.pis"
+    inp.write_text(f"timestep 0.002 # comment\nread_data {d}\nvelocity all create 50.0 7\n"
+                   "pair_style lj/cut 2.5\npair_coeff 1 1 1.0 1.0\nfix f all nvt temp 1.0 2.0 0.5\n"
+                   f"dump d all atom 5 {tmp_path / 'x.lammpstrj'}\nrun 30\n")
+    s = io.System(str(inp))
+    assert s.steps == 30 and s.timestep == 0.002 and s.ensemble == "NVT"
+    s.close()
+    inp.write_text("frobnicate 1 2\n")
+    with pytest.raises(PisError) as e:
+        io.System(str(inp))
+    assert e.value.name == "PIS_ERR_PARSE"
+    inp.write_text("pair_coeff 1 1 1.0 1.0\n")
+    with pytest.raises(PisError) as e:
+        io.System(str(inp))
+    assert e.value.name == "PIS_ERR_MISSING_POTENTIAL"
