@@ -94,6 +94,8 @@ pis_status pis_gpu_create(const pis_lj_pair* table, int32_t n_pairs, int32_t n_t
 #define PIS_OPT_MIXED_KAHAN 2 /* mixed path: compensated FP32 sums instead of FP64 batch sums */
 #define PIS_OPT_LANES(n) ((n) << 8) /* lanes per atom in the list build and force kernels:
                                      * 1 (thread per atom, default), 4, 8, 16 or 32 (warp per atom) */
+#define PIS_OPT_BATCH(n) ((n) << 16) /* mixed path, thread per atom: list entries loaded per gather
+                                      * batch, 4 (default), 8 or 16 */
 
 /* Select a measured variant: list kind (pis_list_kind) and PIS_OPT_* flags. Takes effect at the
  * next set_state. */

@@ -132,6 +132,13 @@ __device__ __forceinline__ bool lj_fp64(const LJ64& P, double r2, double& u, dou
     return true;
 }
 
+// Single hardware reciprocal approximation (rcp.approx.ftz.f32); ~1 ulp, flushes denormals.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
@@ -464,7 +471,7 @@ __device__ __forceinline__ int wrapc(int c, int n) {
 }
 
 template <bool HALF, int LPA>
-__global__ void __launch_bounds__(256) k_build(const DP P, int step_mode) {
+__device__ __forceinline__ void k_build_body(const DP& P, int step_mode) {
     auto tile = cg::tiled_partition<LPA>(cg::this_thread_block());
     int s, i;
     const bool live = group_atom_of<LPA>(P, s, i);
@@ -565,6 +572,96 @@ __global__ void __launch_bounds__(256) k_build(const DP P, int step_mode) {
         if (cnt > cap) atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
         P.nn[i] = cnt > cap ? cap : cnt;
     }
+}
+
+template <bool HALF, int LPA>
+__global__ void __launch_bounds__(256) k_build(const DP P, int step_mode) {
+    k_build_body<HALF, LPA>(P, step_mode);
+}
+
+// Thread-per-atom list build (the default shape). Same contents and order as k_build<HALF, 1>;
+// the inner loop is kept minimal: the home cell (the only one holding i) is walked separately,
+// the capacity test is hoisted to once per neighbour cell when the cell cannot overflow the row,
+// and cells whose nearest face is beyond the list radius for this atom are skipped.
+template <bool HALF>
+__device__ __forceinline__ void scan_cell(const float4* __restrict__ pp, int j, int jend, float sx, float sy,
+                                          float sz, float rl2, uint32_t codebits, int i, bool home,
+                                          uint32_t*& out, int& cnt, int64_t npad, int cap) {
+    const bool roomy = cnt + (jend - j) <= cap;
+    for (; j < jend; ++j, ++pp) {
+        const float4 pj = *pp;
+        const float dx = pj.x + sx, dy = pj.y + sy, dz = pj.z + sz;
+        bool take = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= rl2;
+        if (HALF)
+            take = take && j > i;
+        else if (home)
+            take = take && j != i;
+        if (take) {
+            if (roomy || cnt < cap) *out = (uint32_t)j | codebits;
+            out += npad;
+            ++cnt;
+        }
+    }
+}
+
+template <bool HALF>
+__global__ void __launch_bounds__(256) k_build1(const DP P, int step_mode) {
+    int s, i;
+    if (!atom_of(P, s, i)) return;
+    if (!slot_runs(P, s, step_mode)) return;
+    const SysParams& sp = P.sp[s];
+    SysState& st = P.st[s];
+    if (!st.rebuild) return;
+    const int nx = sp.nc[0], ny = sp.nc[1], nz = sp.nc[2];
+    if (nx < 3 || ny < 3 || nz < 3) return;  // two-cell axes: the generic kernel handles the slot
+    const int lc = P.cellof[i];
+    const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
+    const float4 pi = P.prel[i];
+    const float csx = sp.fcs[0], csy = sp.fcs[1], csz = sp.fcs[2];
+    const float rl2 = sp.frlist2;
+    const int64_t npad = P.npad;
+    const int cap = P.cap;
+    const int32_t* __restrict__ cstart = P.cell_start + sp.c0;
+    const float4* __restrict__ prel = P.prel;
+    uint32_t* out = P.nbr + i;
+    int cnt = 0;
+    const float gxm = fmaxf(pi.x + 0.5f * csx, 0.f), gxp = fmaxf(0.5f * csx - pi.x, 0.f);
+    const float gym = fmaxf(pi.y + 0.5f * csy, 0.f), gyp = fmaxf(0.5f * csy - pi.y, 0.f);
+    const float gzm = fmaxf(pi.z + 0.5f * csz, 0.f), gzp = fmaxf(0.5f * csz - pi.z, 0.f);
+    for (int oz = -1; oz <= 1; ++oz) {
+        const int z2 = wrapc(cz + oz, nz);
+        const float ez = oz < 0 ? gzm : (oz > 0 ? gzp : 0.f);
+        for (int oy = -1; oy <= 1; ++oy) {
+            const int y2 = wrapc(cy + oy, ny);
+            const float ey = oy < 0 ? gym : (oy > 0 ? gyp : 0.f);
+            const float eyz = fmaf(ey, ey, ez * ez);
+            for (int ox = -1; ox <= 1; ++ox) {
+                const float ex = ox < 0 ? gxm : (ox > 0 ? gxp : 0.f);
+                if (fmaf(ex, ex, eyz) > rl2) continue;
+                const int x2 = wrapc(cx + ox, nx);
+                const int nb = (z2 * ny + y2) * nx + x2;
+                const int b0 = cstart[nb], b1 = cstart[nb + 1];
+                const uint32_t codebits = (((uint32_t)(ox < 0 ? 2 : ox)) | ((uint32_t)(oy < 0 ? 2 : oy) << 2) |
+                                           ((uint32_t)(oz < 0 ? 2 : oz) << 4))
+                                          << JBITS;
+                const bool home = ox == 0 && oy == 0 && oz == 0;
+                scan_cell<HALF>(prel + b0, b0, b1, ox * csx - pi.x, oy * csy - pi.y, oz * csz - pi.z, rl2, codebits,
+                                i, home, out, cnt, npad, cap);
+            }
+        }
+    }
+    if (cnt > cap) atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
+    P.nn[i] = cnt > cap ? cap : cnt;
+}
+
+// Slots with a two-cell axis: the group kernel's generic path, one lane per atom.
+template <bool HALF>
+__global__ void __launch_bounds__(256) k_build1_generic(const DP P, int step_mode) {
+    int s = P.blk_sys[blockIdx.x];
+    if (s < 0) return;
+    const SysParams& sp = P.sp[s];
+    if (sp.nc[0] >= 3 && sp.nc[1] >= 3 && sp.nc[2] >= 3) return;
+    k_build_body<HALF, 1>(P, step_mode);
 }
 
 // FP64 forces: the pair evaluation of LJVOffsetManager (src/potentials/lennard_jones.rs:214-235),
@@ -700,7 +797,7 @@ __global__ void __launch_bounds__(256) k_force_fp64(const DP P, int respect_step
 // sums are added in FP64 (ACC = 0), or kept as compensated FP32 sums (ACC = 1, a measured variant)
 // and converted once at the end; the group's lanes are then reduced in FP64 with tile shuffles.
 // PE = sum_i sum_j u_ij, halved at the reduction.
-template <int ACC, int LPA, bool ONE>
+template <int ACC, int LPA, bool ONE, int MIX_BATCH>
 __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) {
     __shared__ double sh[32];
     __shared__ float4 shift[64];
@@ -723,7 +820,6 @@ __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) 
     }
     __syncthreads();
     const int gl = (int)tile.thread_rank();
-    constexpr int MIX_BATCH = LPA >= 8 ? 4 : 8;
     constexpr int FLUSH = 32;  // entries per lane between FP64 (or compensated) folds
     double e = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
     if (live) {
@@ -790,16 +886,19 @@ __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) 
                     fe4 = L.feps4;
                     fuc = L.fucut;
                 }
-                if (r2 <= frc2) {
-                    const float inv = __fdividef(1.0f, r2);
-                    const float s2 = fs2 * inv;
-                    const float s6 = s2 * s2 * s2;
-                    const float c = fe24 * s6 * fmaf(2.0f, s6, -1.0f) * inv;
-                    px = fmaf(-c, dx, px);
-                    py = fmaf(-c, dy, py);
-                    pz = fmaf(-c, dz, pz);
-                    pe += fmaf(fe4 * s6, s6 - 1.0f, -fuc);
-                }
+                // evaluated for every entry and masked, so the warp never splits on the cutoff
+                // (padding entries have r2 ~ 1e36: 1/r2 -> 0, masked anyway)
+                const bool in = r2 <= frc2;
+                const float inv = rcp_approx(r2);
+                const float s2 = fs2 * inv;
+                const float s6 = s2 * s2 * s2;
+                // 24 eps s6 (2 s6 - 1) / r^2 and 4 eps (s6^2 - s6) - u(rc)
+                const float c = in ? (s6 * fmaf(2.0f, s6, -1.0f)) * (fe24 * inv) : 0.f;
+                const float u = in ? fmaf(fe4, fmaf(s6, s6, -s6), -fuc) : 0.f;
+                px = fmaf(-c, dx, px);
+                py = fmaf(-c, dy, py);
+                pz = fmaf(-c, dz, pz);
+                pe += u;
             }
             since += MIX_BATCH;
             if (since >= FLUSH) {
@@ -1502,6 +1601,18 @@ void Engine::enqueue_rebuild(bool respect) {
 // has lpa blocks per chunk.
 template <int L>
 static void launch_build_t(const DP& P, bool half, unsigned chunks, cudaStream_t st, int r) {
+    if (L == 1) {
+        // lean kernel for slots with >= 3 cells per axis, generic kernel for the rest
+        if (half) {
+            k_build1<true><<<chunks, 256, 0, st>>>(P, r);
+            k_build1_generic<true><<<chunks, 256, 0, st>>>(P, r);
+        } else {
+            k_build1<false><<<chunks, 256, 0, st>>>(P, r);
+            k_build1_generic<false><<<chunks, 256, 0, st>>>(P, r);
+        }
+        g_launches.fetch_add(2);
+        return;
+    }
     if (half)
         k_build<true, L><<<chunks * L, 256, 0, st>>>(P, r);
     else
@@ -1509,17 +1620,33 @@ static void launch_build_t(const DP& P, bool half, unsigned chunks, cudaStream_t
     g_launches.fetch_add(1);
 }
 
-template <int L>
-static void launch_mixed_t(const DP& P, bool kahan, bool one, unsigned chunks, cudaStream_t st, int r) {
+template <int L, int B>
+static void launch_mixed_tb(const DP& P, bool kahan, bool one, unsigned chunks, cudaStream_t st, int r) {
     if (kahan && one)
-        k_force_mixed<1, L, true><<<chunks * L, 256, 0, st>>>(P, r);
+        k_force_mixed<1, L, true, B><<<chunks * L, 256, 0, st>>>(P, r);
     else if (kahan)
-        k_force_mixed<1, L, false><<<chunks * L, 256, 0, st>>>(P, r);
+        k_force_mixed<1, L, false, B><<<chunks * L, 256, 0, st>>>(P, r);
     else if (one)
-        k_force_mixed<0, L, true><<<chunks * L, 256, 0, st>>>(P, r);
+        k_force_mixed<0, L, true, B><<<chunks * L, 256, 0, st>>>(P, r);
     else
-        k_force_mixed<0, L, false><<<chunks * L, 256, 0, st>>>(P, r);
+        k_force_mixed<0, L, false, B><<<chunks * L, 256, 0, st>>>(P, r);
     g_launches.fetch_add(1);
+}
+
+// Entries per batch (list words loaded before their gathers): a tuning knob for thread-per-atom;
+// groups of lanes always use 4.
+template <int L>
+static void launch_mixed_t(const DP& P, bool kahan, bool one, int batch, unsigned chunks, cudaStream_t st, int r) {
+    if (L == 1 && batch == 4)
+        launch_mixed_tb<L, 4>(P, kahan, one, chunks, st, r);
+    else if (L == 1 && batch == 16)
+        launch_mixed_tb<L, 16>(P, kahan, one, chunks, st, r);
+    else if (L == 1 && batch == 8)
+        launch_mixed_tb<L, 8>(P, kahan, one, chunks, st, r);
+    else if (L == 1)
+        launch_mixed_tb<L, 4>(P, kahan, one, chunks, st, r);
+    else
+        launch_mixed_tb<L, 4>(P, kahan, one, chunks, st, r);
 }
 
 template <int L>
@@ -1546,6 +1673,7 @@ static void launch_fp64_t(const DP& P, bool half, bool fast, unsigned chunks, cu
 
 void Engine::launch_build(int r) {
     const unsigned ch = (unsigned)max_chunks_;
+
 #define PIS_CALL(L) launch_build_t<L>(*d_, half_, ch, stream_, r)
     PIS_LPA_DISPATCH(opt_.lpa, PIS_CALL)
 #undef PIS_CALL
@@ -1553,7 +1681,7 @@ void Engine::launch_build(int r) {
 
 void Engine::launch_force_mixed(int r) {
     const unsigned ch = (unsigned)max_chunks_;
-#define PIS_CALL(L) launch_mixed_t<L>(*d_, opt_.mixed_kahan, single_type_, ch, stream_, r)
+#define PIS_CALL(L) launch_mixed_t<L>(*d_, opt_.mixed_kahan, single_type_, opt_.mix_batch, ch, stream_, r)
     PIS_LPA_DISPATCH(opt_.lpa, PIS_CALL)
 #undef PIS_CALL
 }

@@ -95,6 +95,7 @@ struct PoolOptions {
     bool fp64_fast = false;    // FP64 force kernel with FMAs and Newton reciprocal (variant)
     bool mixed_kahan = false;  // mixed force kernel with compensated FP32 sums (variant)
     int lpa = 1;               // lanes per atom in the list build and force kernels (1,4,8,16,32)
+    int mix_batch = 4;         // list entries per gather batch in the mixed force kernel (4, 8, 16)
 };
 
 class Engine {

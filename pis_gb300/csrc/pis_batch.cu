@@ -145,6 +145,8 @@ pis_status pis_batch_create(int64_t max_atoms, int32_t max_slots, int64_t max_ce
     b->opt.mixed_kahan = (flags & PIS_OPT_MIXED_KAHAN) != 0;
     const int lanes = (flags >> 8) & 0xff;
     b->opt.lpa = lanes ? lanes : 1;
+    const int batch = (flags >> 16) & 0xff;
+    b->opt.mix_batch = batch ? batch : 4;
     b->opt.list_cap = 224;  // density up to 0.95 at rc + skin = 2.8 (expected ~88 full-list entries)
     b->opt.hist = 1024;
     std::string err;

@@ -21,6 +21,7 @@ struct pis_gpu_ctx {
     bool fp64_fast = false;
     bool mixed_kahan = false;
     int lpa = 1;
+    int mix_batch = 4;
     std::unique_ptr<pis::Engine> eng;
     int slot = -1;
     int64_t n = 0;
@@ -95,8 +96,12 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
     if (!ctx) return PIS_ERR_INVALID_ARGUMENT;
     if (list_kind < PIS_LIST_DEFAULT || list_kind > PIS_LIST_FULL)
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown list kind");
-    if (flags & ~(PIS_OPT_FP64_FAST | PIS_OPT_MIXED_KAHAN | PIS_OPT_LANES(0xff)))
+    if (flags & ~(PIS_OPT_FP64_FAST | PIS_OPT_MIXED_KAHAN | PIS_OPT_LANES(0xff) | PIS_OPT_BATCH(0xff)))
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown option flag");
+    const int batch = (flags >> 16) & 0xff;
+    if (batch != 0 && batch != 4 && batch != 8 && batch != 16)
+        return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "batch must be 4, 8 or 16");
+    ctx->mix_batch = batch ? batch : 4;
     const int lanes = (flags >> 8) & 0xff;
     if (lanes != 0 && lanes != 1 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "lanes per atom must be 1, 4, 8, 16 or 32");
@@ -141,6 +146,7 @@ pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_id
     opt.fp64_fast = ctx->fp64_fast;
     opt.mixed_kahan = ctx->mixed_kahan;
     opt.lpa = ctx->lpa;
+    opt.mix_batch = ctx->mix_batch;
     opt.max_atoms = n;
     opt.max_slots = 1;
     int64_t ncell = 1;

@@ -125,12 +125,12 @@ def test_trajectory_100_steps_liquid(liquid_melt, fast):
     assert st["rebuilds"] >= 2  # the skin test fired during the run
 
 
-@pytest.mark.parametrize("lanes", [1, 4, 8, 32])
+@pytest.mark.parametrize("lanes,batch", [(1, 4), (1, 8), (1, 16), (4, 0), (8, 0), (32, 0)])
 @pytest.mark.parametrize("kahan", [False, True])
-def test_mixed_force_error(liquid_melt, kahan, lanes):
+def test_mixed_force_error(liquid_melt, kahan, lanes, batch):
     o = to_oracle(liquid_melt)
     pe_ref = o.compute_potential()
-    g = to_gpu(liquid_melt, "mixed", mixed_kahan=kahan, lanes=lanes)
+    g = to_gpu(liquid_melt, "mixed", mixed_kahan=kahan, lanes=lanes, batch=batch)
     pe, f = g.compute_potential()
     rms = np.sqrt(np.sum((f - o.force) ** 2) / np.sum(o.force ** 2))
     assert rms <= 1e-5, rms
