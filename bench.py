@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--batch-steps", type=int, default=200)
     p.add_argument("--no-serve", action="store_true", help="skip the served-stream measurement")
     p.add_argument("--serve-jobs", type=int, default=32)
+    p.add_argument("--no-drift", action="store_true", help="skip the 10^4-step energy-drift runs")
+    p.add_argument("--drift-steps", type=int, default=10000)
     return p.parse_args()
 
 
@@ -225,16 +227,23 @@ def main():
     mix.compute_potential(want_forces=False)
     mix.run_timed(DT, max(args.equil, 1))          # melt (unreported)
     melt_pos, melt_vel, _ = mix.get_state()
+    mix.close()
+    # kernel shape from the project's autotuner (cached per GPU / precision / size class)
+    from pis_gb300.autotune import tune_system
+    tuned = tune_system(TABLE, 1, melt_pos, types, [1.0], h, melt_vel, precision="mixed", skin=SKIN, dt=DT)
+    mix = GpuContext(TABLE, 1, skin=SKIN, precision="mixed", **tuned)
     mix.set_state(melt_pos, types, [1.0], h, velocities=melt_vel)
     mix.compute_potential(want_forces=False)
     mix.run_timed(DT, max(args.warmup, 3))         # warm-up
     barrier(world)
+    st0 = mix.stats()
     launches0 = kernel_launches()
     with ClockSampler(local) as clk:
         ms, _ = mix.run_timed(DT, args.steps)
     launches = kernel_launches() - launches0
     ms = max_over_ranks(ms, world)
     st = mix.stats()
+    rebuilds_per_step = (st["rebuilds"] - st0["rebuilds"]) / args.steps
     value = world * n * args.steps / (ms * 1e-3)
     # stage breakdown (events captured in the graphs), separate pass of the same length
     ms_s, stages = mix.run_timed(DT, args.steps, stages=True)
@@ -288,6 +297,7 @@ def main():
     d2h = n * 3 * 8 * 3 + k_e2e * 8
     mix.close()
 
+    drift = None if args.no_drift else run_drift(args, melt_pos, melt_vel, types, h, tuned)
     batched = None if args.no_batch else run_batched(args, rank, world)
     served = None if (args.no_serve or rank != 0) else run_served(args)
 
@@ -319,7 +329,9 @@ def main():
             "error_vs_fp64": {"force_rms_rel": force_rms, "pe_rel": pe_rel},
             "stages_ms_per_step": {"integrate1": stages_per[0], "rebuild": stages_per[1], "force": stages_per[2],
                                    "integrate2": stages_per[3], "reduce": stages_per[4]},
-            "rebuilds_per_step": None,
+            "rebuilds_per_step": rebuilds_per_step,
+            "tuned_options": tuned,
+            "drift": drift,
             "list_entries_per_atom": list_per_atom,
             "roofline": {"bound": "hbm", "kernel": "k_force_mixed", "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_src,
@@ -358,7 +370,10 @@ def run_batched(args, rank, world):
     atoms = sum(4 * j.k ** 3 for j in jobs)
     cells = sum(lj_pool_cells(j.k, j.rho) for j in jobs)
     out = {"replicas": len(jobs), "atoms": atoms, "steps": args.batch_steps}
-    for prec, kw in (("mixed", {}), ("fp64", {}), ("fp64_fast", {"fp64_fast": True})):
+    from pis_gb300.autotune import tune_batch
+    tuned = tune_batch(jobs, precision="mixed")
+    out["tuned_options"] = tuned
+    for prec, kw in (("mixed", tuned), ("fp64", {}), ("fp64_fast", {"fp64_fast": True})):
         precision = "mixed" if prec == "mixed" else "fp64"
         k = args.batch_steps if prec == "mixed" else max(3, args.batch_steps // 5)
         b = Batch(atoms + 1024, len(jobs), cells + 1024, precision=precision, **kw)
@@ -370,6 +385,51 @@ def run_batched(args, rank, world):
         out[prec] = world * atoms * k / (ms * 1e-3)
         b.close()
     out["mixed_over_fp64"] = out["mixed"] / out["fp64"]
+    return out
+
+
+def energy_series(ctx, steps, chunk):
+    """Total energy every `chunk` steps (PE from the step, KE from the device reductions)."""
+    pe0, _ = ctx.compute_potential(want_forces=False)
+    ke0, _ = ctx.reductions()
+    e = [pe0 + ke0]
+    for _ in range(steps // chunk):
+        pe = ctx.verlet_step_nve(DT, chunk)
+        ke, _ = ctx.reductions()
+        e.append(pe[-1] + ke)
+    return np.array(e)
+
+
+def drift_stats(e, n, chunk):
+    t = np.arange(len(e)) * chunk
+    slope = np.polyfit(t, e, 1)[0]
+    return {"drift_per_atom_per_1e4_steps": float(slope * 1e4 / n), "max_abs_dev_per_atom": float(np.abs(e - e[0]).max() / n)}
+
+
+def run_drift(args, melt_pos, melt_vel, types, h, tuned):
+    """NVE energy drift over 10^4 steps: the mixed path on the 2.048M-atom liquid, and the mixed and
+    plain FP64 paths on a 4,000-atom liquid (the FP64 path at 2M atoms would take minutes)."""
+    from pis_gb300.potentials import GpuContext
+    from pis_gb300.lattice import lj_liquid
+    out = {"steps": args.drift_steps}
+    n = len(melt_pos)
+    g = GpuContext(TABLE, 1, skin=SKIN, precision="mixed", **tuned)
+    g.set_state(melt_pos, types, [1.0], h, velocities=melt_vel)
+    out["mixed_2m"] = drift_stats(energy_series(g, args.drift_steps, 1000), n, 1000)
+    g.close()
+    pos, vel, L = lj_liquid(10, RHO, TSTAR, 4)
+    ns = len(pos)
+    g = GpuContext(TABLE, 1, skin=SKIN, precision="fp64")
+    g.set_state(pos, np.ones(ns, np.int32), [1.0], np.eye(3) * L, velocities=vel)
+    g.compute_potential(want_forces=False)
+    g.verlet_step_nve(DT, 1000)  # melt
+    p4, v4, _ = g.get_state()
+    g.close()
+    for name, kw in (("fp64_4k", {"precision": "fp64"}), ("mixed_4k", {"precision": "mixed"})):
+        g = GpuContext(TABLE, 1, skin=SKIN, **kw)
+        g.set_state(p4, np.ones(ns, np.int32), [1.0], np.eye(3) * L, velocities=v4)
+        out[name] = drift_stats(energy_series(g, args.drift_steps, 100), ns, 100)
+        g.close()
     return out
 
 
