@@ -859,14 +859,22 @@ __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) 
             }
             px = py = pz = pe = 0.f;
         };
+        // list words are addressed with 32-bit offsets from the lane's first word (the pool's list
+        // is below 2^32 words, checked at init); full batches load unconditionally, the last
+        // partial batch pads with an out-of-range entry
+        const uint32_t row32 = (uint32_t)row;
+        uint32_t qoff = 0;
         for (int k0 = 0; k0 < nn; k0 += LPA * MIX_BATCH) {
             uint32_t ent[MIX_BATCH];
-            const uint32_t* q = nbp + (int64_t)(k0 / LPA) * row;
+            if (k0 + LPA * MIX_BATCH <= nn) {
 #pragma unroll
-            for (int b = 0; b < MIX_BATCH; ++b) {
-                ent[b] = (k0 + b * LPA + gl < nn) ? __ldg(q) : pad;
-                q += row;
+                for (int b = 0; b < MIX_BATCH; ++b) ent[b] = __ldg(nbp + qoff + (uint32_t)b * row32);
+            } else {
+#pragma unroll
+                for (int b = 0; b < MIX_BATCH; ++b)
+                    ent[b] = (k0 + b * LPA + gl < nn) ? __ldg(nbp + qoff + (uint32_t)b * row32) : pad;
             }
+            qoff += (uint32_t)MIX_BATCH * row32;
             float4 pj[MIX_BATCH];
 #pragma unroll
             for (int b = 0; b < MIX_BATCH; ++b) pj[b] = __ldg(prel + (ent[b] & JMASK));
@@ -1167,6 +1175,10 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     cap_ = opt.list_cap > 0 ? opt.list_cap : 192;
     cap_ = (cap_ + 31) / 32 * 32;  // whole row groups for every lanes-per-atom choice
     npad_ = (int64_t)align_up((size_t)opt.max_atoms, 32);
+    if ((double)npad_ * (double)cap_ >= 4294967296.0) {
+        err = "neighbour list of the pool exceeds 2^32 entries (atoms x capacity)";
+        return PIS_ERR_NO_MEMORY;
+    }
     max_chunks_ = (opt.max_atoms + opt.blk - 1) / opt.blk + opt.max_slots;
     int64_t max_cells = opt.max_cells > 0 ? opt.max_cells : opt.max_atoms + opt.max_slots;
     opt_.max_cells = max_cells;

@@ -144,7 +144,7 @@ class Engine {
     cudaStream_t stream() const { return stream_; }
     // Kernel launches issued (graph launches count every captured kernel).
     static int64_t launches();
-    // Per-kernel-name launch counts (for bench accounting).
+    // Kernels launched per captured step (for launch accounting).
     int64_t graph_kernels_per_step() const { return kernels_per_step_; }
     // Stage timing with CUDA events captured into the step graphs (integrate1, list rebuild,
     // force, integrate2, reductions); costs one host sync per graph launch while enabled.
@@ -157,7 +157,6 @@ class Engine {
     struct DevPtrs;  // device pointer bundle passed by value to every kernel
 
   private:
-    pis_status upload_tables(std::string& err);
     pis_status rebuild_block_map(std::string& err);
     void enqueue_step(bool respect_steps, cudaEvent_t* ev);
     void enqueue_rebuild(bool respect_steps);
@@ -174,7 +173,6 @@ class Engine {
     int64_t max_chunks_ = 0;
     cudaStream_t stream_ = nullptr;
     std::vector<SysParams> hp_;
-    std::vector<LJHost> slot_tables_flat_;
     std::vector<int> slot_tab_size_;
     std::vector<double> slot_rlist_;
     // free-space bookkeeping (first fit over atom and cell index ranges)
