@@ -45,7 +45,8 @@ typedef enum {
     PIS_ERR_LIST_OVERFLOW = 23,    /* a neighbour or cell list outgrew its capacity */
     PIS_ERR_CUDA = 24,             /* any CUDA runtime error */
     PIS_ERR_STATE = 25,            /* call out of order (e.g. no atoms uploaded yet) */
-    PIS_ERR_UNSUPPORTED = 26       /* e.g. non-orthorhombic box */
+    PIS_ERR_UNSUPPORTED = 26,      /* e.g. non-orthorhombic box */
+    PIS_ERR_TIMEOUT = 27           /* a bounded device-side wait expired (the kernel stopped early) */
 } pis_status;
 
 /* One pair_coeff / PairCoeffs row: LennardJones::new(epsilon, sigma, rcut, shift)
@@ -96,6 +97,16 @@ pis_status pis_gpu_create(const pis_lj_pair* table, int32_t n_pairs, int32_t n_t
                                      * 1 (thread per atom, default), 4, 8, 16 or 32 (warp per atom) */
 #define PIS_OPT_BATCH(n) ((n) << 16) /* mixed path, thread per atom: list entries loaded per gather
                                       * batch, 4 (default), 8 or 16 */
+#define PIS_OPT_LIST_TMA 4 /* mixed path, thread per atom: the neighbour list is streamed into shared
+                            * memory by bulk (TMA) copies several batches ahead of the pair loop;
+                            * PIS_OPT_BATCH(8 or 16) sets the rows per copy stage (4 counts as 8) */
+#define PIS_OPT_CLUSTER(m) ((m) << 24) /* mixed path, neighbour-list shape: 1 = one list per atom,
+                                        * 2 or 4 = one list per cluster of m spatially adjacent atoms
+                                        * of a cell (each neighbour read serves m pairs);
+                                        * PIS_OPT_BATCH(4 or 8) sets the entries per gather batch */
+#define PIS_OPT_SCAN(m) ((m) << 28) /* per-atom lists, one thread per atom: the list build scans the
+                                     * candidates of m spatially adjacent atoms of a cell per thread
+                                     * (2 or 4) or of one atom (1); the lists are the same either way */
 
 /* Select a measured variant: list kind (pis_list_kind) and PIS_OPT_* flags. Takes effect at the
  * next set_state. */

@@ -16,10 +16,16 @@ STATUS_NAMES = {
     4: "PIS_ERR_MISSING_POTENTIAL", 5: "PIS_ERR_IO", 6: "PIS_ERR_PARSE", 7: "PIS_ERR_ATOM_COUNT",
     8: "PIS_ERR_UNKNOWN_PAIR_STYLE", 20: "PIS_ERR_NAN_DETECTED", 21: "PIS_ERR_BOX_TOO_SMALL",
     22: "PIS_ERR_NO_MEMORY", 23: "PIS_ERR_LIST_OVERFLOW", 24: "PIS_ERR_CUDA", 25: "PIS_ERR_STATE",
-    26: "PIS_ERR_UNSUPPORTED",
+    26: "PIS_ERR_UNSUPPORTED", 27: "PIS_ERR_TIMEOUT",
 }
 PRECISION = {"fp64": 0, "mixed": 1}
 LIST_KIND = {"default": 0, "half": 1, "full": 2}
+
+
+def option_flags(fp64_fast=False, mixed_kahan=False, lanes=0, batch=0, tma=False, cluster=0, scan=0) -> int:
+    """PIS_OPT_* bits of include/pis_gpu.h for the variant knobs."""
+    return ((1 if fp64_fast else 0) | (2 if mixed_kahan else 0) | (4 if tma else 0) | (int(lanes) << 8)
+            | (int(batch) << 16) | (int(cluster) << 24) | (int(scan) << 28))
 
 
 class PisError(RuntimeError):

@@ -75,6 +75,18 @@ struct Engine::DevPtrs {
     int32_t zero_forces;  // half list: integrate1 clears F for the atomic scatter
     int32_t full_list;
     int32_t pe_stride;    // force-kernel blocks per chunk (lanes per atom)
+    // cluster-list path (clm = atoms per cluster, 0 when the per-atom list is used)
+    int32_t* cl_atom;     // per cluster: first atom | (members - 1) << JBITS
+    int32_t* cl_start;    // per cell entry: first cluster of the cell (same indexing as cell_start)
+    int32_t* cl_nn;       // per cluster: list length
+    uint32_t* cl_nbr;     // column-major cluster list: entry k of cluster c at k * clpad + c
+    int32_t* cblk_sys;    // per cluster chunk: slot (-1 unused)
+    int32_t* cblk_first;  // per cluster chunk: first cluster
+    int64_t clpad;
+    int32_t ccap;
+    int32_t clm;          // atoms per cluster of the cluster table (0: no table)
+    int32_t cl_force;     // forces run over cluster lists (else per-atom lists)
+    int32_t* ctl;         // ctl[0]: some slot rebuilds its list in the current step or evaluation
 };
 using DP = Engine::DevPtrs;
 
@@ -139,6 +151,47 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return y;
 }
 
+// ---- mbarrier / bulk-copy (TMA) helpers ----------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// arrive (count 1) and announce `bytes` of bulk-copy transactions for the current phase
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for the phase of the given parity: false after `limit` unsuccessful polls (each
+// poll may suspend the warp for a short hardware-defined time), so a wait can never hang.
+constexpr uint32_t MBAR_WAIT_LIMIT = 1u << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (uint32_t it = 0; it < MBAR_WAIT_LIMIT; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// Bulk copy global -> shared (no tensor map): both addresses 16-byte aligned, bytes a multiple of
+// 16; completion is signalled on the mbarrier as transaction bytes.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
@@ -162,26 +215,38 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
     return r;
 }
 
-// Which atom this thread owns. Returns false for padding threads; s < 0 for unused chunks.
-__device__ __forceinline__ bool atom_of(const DP& P, int& s, int& i) {
-    s = P.blk_sys[blockIdx.x];
+// Which atom this thread owns in atom chunk `blk`. Returns false for padding threads; s < 0 for
+// unused chunks.
+__device__ __forceinline__ bool atom_of_blk(const DP& P, int blk, int& s, int& i) {
+    s = P.blk_sys[blk];
     if (s < 0) return false;
-    i = P.blk_first[blockIdx.x] + (int)threadIdx.x;
+    i = P.blk_first[blk] + (int)threadIdx.x;
     const SysParams& sp = P.sp[s];
     return i < (int)(sp.a0 + sp.n);
 }
+__device__ __forceinline__ bool atom_of(const DP& P, int& s, int& i) { return atom_of_blk(P, blockIdx.x, s, i); }
 
 // Lanes-per-atom kernels: LPA consecutive lanes (a cooperative-groups tile) share one atom and
-// the grid has LPA blocks per chunk. Returns false for padding groups; s < 0 for unused chunks.
+// there are LPA blocks per chunk. Returns false for padding groups; s < 0 for unused chunks.
 template <int LPA>
-__device__ __forceinline__ bool group_atom_of(const DP& P, int& s, int& i) {
-    const int chunk = blockIdx.x / LPA, sub = blockIdx.x % LPA;
+__device__ __forceinline__ bool group_atom_of_blk(const DP& P, int blk, int& s, int& i) {
+    const int chunk = blk / LPA, sub = blk % LPA;
     s = P.blk_sys[chunk];
     if (s < 0) return false;
     i = P.blk_first[chunk] + sub * (256 / LPA) + (int)(threadIdx.x / LPA);
     const SysParams& sp = P.sp[s];
     return i < (int)(sp.a0 + sp.n);
 }
+template <int LPA>
+__device__ __forceinline__ bool group_atom_of(const DP& P, int& s, int& i) {
+    return group_atom_of_blk<LPA>(P, blockIdx.x, s, i);
+}
+
+// The neighbour-list rebuild kernels run on a grid capped at a whole number of waves and stride
+// over their chunks. Their first test is the device-wide "some slot rebuilds this step" word, so
+// on the ~9 steps in 10 without a rebuild each costs one short wave rather than a full grid.
+__device__ __forceinline__ bool rebuild_pending(const DP& P) { return *(volatile const int32_t*)P.ctl != 0; }
+#define PIS_FOR_CHUNKS(n) for (int blk = blockIdx.x; blk < (n); blk += gridDim.x)
 
 // Neighbour-list layout: entry k of atom i lives at (k / LPA) * (npad * LPA) + i * LPA + k % LPA.
 // The LPA lanes of one atom read or write one contiguous run of LPA words, and consecutive atoms'
@@ -225,6 +290,7 @@ __global__ void k_integrate1(const DP P) {
     if (!slot_runs(P, s, true)) return;
     const SysParams& sp = P.sp[s];
     SysState& st = P.st[s];
+    if (threadIdx.x == 0 && st.rebuild) P.ctl[0] = 1;  // a rebuild requested before this step
     const int cur = st.cur;
     const double4_32a p = P.pos[cur][i];
     const double4_32a v = P.vel[cur][i];
@@ -262,7 +328,10 @@ __global__ void k_integrate1(const DP P) {
         dy = min_image_axis(dy, sp.h[1], sp.hinv[1]);
         dz = min_image_axis(dz, sp.h[2], sp.hinv[2]);
         d2 = fma(dx, dx, fma(dy, dy, dz * dz));
-        if (!(d2 <= sp.half_skin2)) st.rebuild = 1;  // NaN also requests a rebuild
+        if (!(d2 <= sp.half_skin2)) {  // NaN also requests a rebuild
+            st.rebuild = 1;
+            P.ctl[0] = 1;
+        }
         if (x != x || y != y || z != z) atomicOr(&st.flags, FLAG_NAN);
     }
     if (MIXED) {
@@ -275,9 +344,9 @@ __global__ void k_integrate1(const DP P) {
 // Counting sort, pass 1: cell of every atom (reference binning of src/atoms/neighbour_list.rs:
 // 9-42 at rcut + skin, with a Euclidean modulo so atoms outside the box fold back in) and its
 // slot inside the cell.
-__global__ void k_bin(const DP P, int respect_steps) {
+__device__ __forceinline__ void bin_chunk(const DP& P, int blk, int respect_steps) {
     int s, i;
-    if (!atom_of(P, s, i)) return;
+    if (!atom_of_blk(P, blk, s, i)) return;
     if (!slot_runs(P, s, respect_steps)) return;
     const SysParams& sp = P.sp[s];
     const SysState& st = P.st[s];
@@ -297,26 +366,20 @@ __global__ void k_bin(const DP P, int respect_steps) {
     P.lcell[i] = lc;
     P.slotin[i] = atomicAdd(&P.cell_count[sp.c0 + lc], 1);
 }
+__global__ void k_bin(const DP P, int respect_steps, int nblk) {
+    if (!rebuild_pending(P)) return;
+    PIS_FOR_CHUNKS(nblk) bin_chunk(P, blk, respect_steps);
+}
 
-// Counting sort, pass 2: exclusive scan of the cell counts of one slot (one block per slot),
-// writing absolute atom indices; also flips the slot's buffer set. Counts are staged through
-// shared memory so global loads and stores stay coalesced while each thread scans SCAN_ITEMS
-// consecutive cells.
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan(const DP P, int step_mode) {
-    int s = blockIdx.x;
-    const SysParams& sp = P.sp[s];
-    if (!sp.active) return;
-    if (!slot_runs(P, s, step_mode)) return;
-    SysState& st = P.st[s];
-    if (!st.rebuild) return;
-    __shared__ int buf[SCAN_THREADS * SCAN_ITEMS];
-    __shared__ int warp_tot[SCAN_THREADS / 32];
-    __shared__ int carry_sh;
-    const int ncell = sp.nc[0] * sp.nc[1] * sp.nc[2];
-    int32_t* __restrict__ cnt_g = P.cell_count + sp.c0;
-    int32_t* __restrict__ start_g = P.cell_start + sp.c0;
-    int carry = (int)sp.a0;
+// One exclusive scan over a slot's cells: of the atom counts (CL = 0, the last pass, which also
+// clears the counts) or of the cluster counts ceil(count / clm) (CL = 1). Writes absolute indices
+// starting at `carry` and returns the total. Counts are staged through shared memory so global
+// loads and stores stay coalesced while each thread scans SCAN_ITEMS consecutive cells.
+template <bool CL>
+__device__ __forceinline__ int scan_cells(int32_t* __restrict__ cnt_g, int32_t* __restrict__ start_g, int ncell,
+                                          int carry, int clm, int* buf, int* warp_tot, int* carry_sh) {
     const int t = threadIdx.x, l = t & 31, w = t >> 5;
+    const int carry0 = carry;
     for (int base = 0; base < ncell; base += SCAN_THREADS * SCAN_ITEMS) {
 #pragma unroll
         for (int k = 0; k < SCAN_ITEMS; ++k) {
@@ -324,7 +387,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const DP P, int step_mode
             int v = 0;
             if (c < ncell) {
                 v = cnt_g[c];
-                cnt_g[c] = 0;
+                if (CL)
+                    v = (v + clm - 1) / clm;
+                else
+                    cnt_g[c] = 0;
             }
             buf[k * SCAN_THREADS + t] = v;
         }
@@ -352,7 +418,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const DP P, int step_mode
                 if (l >= o) xi += y;
             }
             warp_tot[l] = xi - x;  // exclusive warp offsets
-            if (l == 31) carry_sh = xi;
+            if (l == 31) *carry_sh = xi;
         }
         __syncthreads();
         int run = carry + warp_tot[w] + incl - sum;
@@ -367,33 +433,75 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const DP P, int step_mode
             const int c = base + k * SCAN_THREADS + t;
             if (c < ncell) start_g[c] = buf[k * SCAN_THREADS + t];
         }
-        carry += carry_sh;
+        carry += *carry_sh;
         __syncthreads();
     }
-    if (t == 0) {
-        start_g[ncell] = carry;
+    if (t == 0) start_g[ncell] = carry;
+    return carry - carry0;
+}
+
+// Counting sort, pass 2: exclusive scans of the cell counts of one slot (one block per slot) -
+// cluster starts (cluster table) and atom starts - and the flip of the slot's buffer set.
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan(const DP P, int step_mode) {
+    if (!rebuild_pending(P)) return;
+    int s = blockIdx.x;
+    const SysParams& sp = P.sp[s];
+    if (!sp.active) return;
+    if (!slot_runs(P, s, step_mode)) return;
+    SysState& st = P.st[s];
+    if (!st.rebuild) return;
+    __shared__ int buf[SCAN_THREADS * SCAN_ITEMS];
+    __shared__ int warp_tot[SCAN_THREADS / 32];
+    __shared__ int carry_sh;
+    const int ncell = sp.nc[0] * sp.nc[1] * sp.nc[2];
+    int32_t* __restrict__ cnt_g = P.cell_count + sp.c0;
+    int ncl = 0;
+    if (P.clm) ncl = scan_cells<true>(cnt_g, P.cl_start + sp.c0, ncell, sp.cl0, P.clm, buf, warp_tot, &carry_sh);
+    scan_cells<false>(cnt_g, P.cell_start + sp.c0, ncell, (int)sp.a0, 1, buf, warp_tot, &carry_sh);
+    if (threadIdx.x == 0) {
+        st.ncl = ncl;
         st.cur ^= 1;
     }
 }
 
 // Counting sort, pass 3: destination of every atom.
-__global__ void k_scatter(const DP P, int respect_steps) {
+__device__ __forceinline__ void scatter_chunk(const DP& P, int blk, int respect_steps) {
     int s, i;
-    if (!atom_of(P, s, i)) return;
+    if (!atom_of_blk(P, blk, s, i)) return;
     if (!slot_runs(P, s, respect_steps)) return;
     if (!P.st[s].rebuild) return;
     const SysParams& sp = P.sp[s];
     int dst = P.cell_start[sp.c0 + P.lcell[i]] + P.slotin[i];
     P.perm[dst] = i;
 }
+__global__ void k_scatter(const DP P, int respect_steps, int nblk) {
+    if (!rebuild_pending(P)) return;
+    PIS_FOR_CHUNKS(nblk) scatter_chunk(P, blk, respect_steps);
+}
 
-// One warp per cell: order the cell's atoms by original id (so the layout depends only on the
-// physical state, not on atomics), then move every per-atom array into the new buffer set and
-// record the build snapshot and cell-relative coordinates.
-__global__ void k_gather(const DP P, int64_t max_cells, int respect_steps) {
-    int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Order key of an atom inside its cell: the Morton index of its sub-cell on a 4 x 4 x 4 grid over
+// the cell (6 bits, coarse bits high) above its original id (26 bits). Atoms that are consecutive
+// in memory are then near each other in space, so the lanes of a warp own nearby atoms whose
+// neighbour lists hold nearly the same atoms in the same order: their position gathers share cache
+// sectors, and the list build's per-atom cell pruning agrees across the warp. The key depends only
+// on the physical state, never on atomics.
+__device__ __forceinline__ uint32_t cell_order_key(const SysParams& sp, const float4& q, uint32_t id) {
+    uint32_t b[3];
+    const float r[3] = {q.x / sp.fcs[0], q.y / sp.fcs[1], q.z / sp.fcs[2]};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const int v = __float2int_rd((r[d] + 0.5f) * 4.0f);
+        b[d] = (uint32_t)(v < 0 ? 0 : (v > 3 ? 3 : v));
+    }
+    const uint32_t m = (b[0] & 1u) | ((b[1] & 1u) << 1) | ((b[2] & 1u) << 2) | ((b[0] >> 1) << 3) |
+                       ((b[1] >> 1) << 4) | ((b[2] >> 1) << 5);
+    return (m << JBITS) | id;
+}
+
+// One warp per cell: order the cell's atoms by cell_order_key, then move every per-atom array into
+// the new buffer set and record the build snapshot and cell-relative coordinates.
+__device__ __forceinline__ void gather_cell(const DP& P, int64_t g, int respect_steps) {
     int lane = threadIdx.x & 31;
-    if (g >= max_cells) return;
     int s = P.cell_sys[g];
     if (s < 0) return;
     if (!slot_runs(P, s, respect_steps)) return;
@@ -405,54 +513,82 @@ __global__ void k_gather(const DP P, int64_t max_cells, int respect_steps) {
     const int dst_set = st.cur, src_set = st.cur ^ 1;
     const int beg = P.cell_start[g], end = P.cell_start[g + 1];
     const int cnt = end - beg;
-    // rank of every member by original id: ids held in lane registers for cells of up to 64
-    // atoms (one or two per lane), compared through warp shuffles; larger cells re-read ids
-    int rk[2] = {0, 0}, srcs[2] = {-1, -1}, ids[2] = {0x7fffffff, 0x7fffffff};
+    // rank of every member by its order key: keys held in lane registers for cells of up to 64
+    // atoms (one or two per lane), compared through warp shuffles; larger cells recompute keys
+    auto key_of = [&](int src) {
+        const double4_32a p = P.pos[src_set][src];
+        return cell_order_key(sp, cell_relative(sp, p, lc, 0), (uint32_t)P.id[src_set][src]);
+    };
+    int rk[2] = {0, 0}, srcs[2] = {-1, -1};
+    uint32_t keys[2] = {0xffffffffu, 0xffffffffu};
+    double4_32a ps[2];
+    float4 qs[2];
     if (cnt <= 64) {
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int k = lane + 32 * h;
             if (k < cnt) {
                 srcs[h] = P.perm[beg + k];
-                ids[h] = P.id[src_set][srcs[h]];
+                ps[h] = P.pos[src_set][srcs[h]];
+                qs[h] = cell_relative(sp, ps[h], lc, type_of(ps[h].w));
+                keys[h] = cell_order_key(sp, qs[h], (uint32_t)P.id[src_set][srcs[h]]);
             }
         }
         const int n0 = cnt < 32 ? cnt : 32;
         for (int q = 0; q < n0; ++q) {
-            const int v = __shfl_sync(0xffffffffu, ids[0], q);
-            rk[0] += v < ids[0];
-            rk[1] += v < ids[1];
+            const uint32_t v = __shfl_sync(0xffffffffu, keys[0], q);
+            rk[0] += v < keys[0];
+            rk[1] += v < keys[1];
         }
         for (int q = 32; q < cnt; ++q) {
-            const int v = __shfl_sync(0xffffffffu, ids[1], q - 32);
-            rk[0] += v < ids[0];
-            rk[1] += v < ids[1];
+            const uint32_t v = __shfl_sync(0xffffffffu, keys[1], q - 32);
+            rk[0] += v < keys[0];
+            rk[1] += v < keys[1];
         }
     }
     for (int k = lane; k < cnt; k += 32) {
-        int src, myid, rank = 0;
+        int src, rank = 0;
+        double4_32a p;
+        float4 q;
         if (cnt <= 64) {
             const bool hi = k >= 32;
             src = hi ? srcs[1] : srcs[0];
-            myid = hi ? ids[1] : ids[0];
             rank = hi ? rk[1] : rk[0];
+            p = hi ? ps[1] : ps[0];
+            q = hi ? qs[1] : qs[0];
         } else {
             src = P.perm[beg + k];
-            myid = P.id[src_set][src];
-            for (int q = 0; q < cnt; ++q) rank += P.id[src_set][P.perm[beg + q]] < myid;
+            const uint32_t mine = key_of(src);
+            for (int r = 0; r < cnt; ++r) rank += key_of(P.perm[beg + r]) < mine;
+            p = P.pos[src_set][src];
+            q = cell_relative(sp, p, lc, type_of(p.w));
         }
         int dst = beg + rank;
-        double4_32a p = P.pos[src_set][src];
         P.pos[dst_set][dst] = p;
         P.vel[dst_set][dst] = P.vel[src_set][src];
         P.acc[dst_set][dst] = P.acc[src_set][src];
-        P.id[dst_set][dst] = myid;
+        P.id[dst_set][dst] = P.id[src_set][src];
         P.posb[dst] = p;
         P.cellof[dst] = lc;
-        const float4 q = cell_relative(sp, p, lc, type_of(p.w));
         P.prel[dst] = q;
         P.prelb[dst] = q;
     }
+    // cluster table: runs of clm consecutive atoms of the cell (the last run may be shorter)
+    if (P.clm) {
+        const int M = P.clm;
+        const int nclu = (cnt + M - 1) / M;
+        const int cb = P.cl_start[g];
+        for (int q = lane; q < nclu; q += 32) {
+            const int m = min(M, cnt - q * M);
+            P.cl_atom[cb + q] = (beg + q * M) | ((m - 1) << JBITS);
+        }
+    }
+}
+__global__ void k_gather(const DP P, int64_t max_cells, int respect_steps) {
+    if (!rebuild_pending(P)) return;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < max_cells; g += nw)
+        gather_cell(P, g, respect_steps);
 }
 
 // Neighbour-list build at rcut + skin. LPA lanes share one home atom (atoms in cell order, so
@@ -471,10 +607,10 @@ __device__ __forceinline__ int wrapc(int c, int n) {
 }
 
 template <bool HALF, int LPA>
-__device__ __forceinline__ void k_build_body(const DP& P, int step_mode) {
+__device__ __forceinline__ void k_build_body(const DP& P, int blk, int step_mode) {
     auto tile = cg::tiled_partition<LPA>(cg::this_thread_block());
     int s, i;
-    const bool live = group_atom_of<LPA>(P, s, i);
+    const bool live = group_atom_of_blk<LPA>(P, blk, s, i);
     if (s < 0 || !live) return;  // uniform over the group (one atom per group)
     if (!slot_runs(P, s, step_mode)) return;
     const SysParams& sp = P.sp[s];
@@ -575,8 +711,9 @@ __device__ __forceinline__ void k_build_body(const DP& P, int step_mode) {
 }
 
 template <bool HALF, int LPA>
-__global__ void __launch_bounds__(256) k_build(const DP P, int step_mode) {
-    k_build_body<HALF, LPA>(P, step_mode);
+__global__ void __launch_bounds__(256) k_build(const DP P, int step_mode, int nblk) {
+    if (!rebuild_pending(P)) return;
+    PIS_FOR_CHUNKS(nblk) k_build_body<HALF, LPA>(P, blk, step_mode);
 }
 
 // Thread-per-atom list build (the default shape). Same contents and order as k_build<HALF, 1>;
@@ -605,9 +742,9 @@ __device__ __forceinline__ void scan_cell(const float4* __restrict__ pp, int j, 
 }
 
 template <bool HALF>
-__global__ void __launch_bounds__(256) k_build1(const DP P, int step_mode) {
+__device__ __forceinline__ void build1_chunk(const DP& P, int blk, int step_mode) {
     int s, i;
-    if (!atom_of(P, s, i)) return;
+    if (!atom_of_blk(P, blk, s, i)) return;
     if (!slot_runs(P, s, step_mode)) return;
     const SysParams& sp = P.sp[s];
     SysState& st = P.st[s];
@@ -653,15 +790,23 @@ __global__ void __launch_bounds__(256) k_build1(const DP P, int step_mode) {
     if (cnt > cap) atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
     P.nn[i] = cnt > cap ? cap : cnt;
 }
+template <bool HALF>
+__global__ void __launch_bounds__(256) k_build1(const DP P, int step_mode, int nblk) {
+    if (!rebuild_pending(P)) return;
+    PIS_FOR_CHUNKS(nblk) build1_chunk<HALF>(P, blk, step_mode);
+}
 
 // Slots with a two-cell axis: the group kernel's generic path, one lane per atom.
 template <bool HALF>
-__global__ void __launch_bounds__(256) k_build1_generic(const DP P, int step_mode) {
-    int s = P.blk_sys[blockIdx.x];
-    if (s < 0) return;
-    const SysParams& sp = P.sp[s];
-    if (sp.nc[0] >= 3 && sp.nc[1] >= 3 && sp.nc[2] >= 3) return;
-    k_build_body<HALF, 1>(P, step_mode);
+__global__ void __launch_bounds__(256) k_build1_generic(const DP P, int step_mode, int nblk) {
+    if (!rebuild_pending(P)) return;
+    PIS_FOR_CHUNKS(nblk) {
+        const int s = P.blk_sys[blk];
+        if (s < 0) continue;
+        const SysParams& sp = P.sp[s];
+        if (sp.nc[0] >= 3 && sp.nc[1] >= 3 && sp.nc[2] >= 3) continue;
+        k_build_body<HALF, 1>(P, blk, step_mode);
+    }
 }
 
 // FP64 forces: the pair evaluation of LJVOffsetManager (src/potentials/lennard_jones.rs:214-235),
@@ -797,6 +942,115 @@ __global__ void __launch_bounds__(256) k_force_fp64(const DP P, int respect_step
 // sums are added in FP64 (ACC = 0), or kept as compensated FP32 sums (ACC = 1, a measured variant)
 // and converted once at the end; the group's lanes are then reduced in FP64 with tile shuffles.
 // PE = sum_i sum_j u_ij, halved at the reduction.
+// Image-shift table of the mixed kernels: code -> cell offset * cell edge; a 3 in any field marks
+// a padding entry and sends it out of range.
+__device__ __forceinline__ void fill_shift_table(float4* shift, const SysParams& sp) {
+    if (threadIdx.x < 64) {
+        const int c = threadIdx.x;
+        const int bx = c & 3, by = (c >> 2) & 3, bz = (c >> 4) & 3;
+        const float fx = bx == 1 ? 1.f : (bx == 2 ? -1.f : 0.f);
+        const float fy = by == 1 ? 1.f : (by == 2 ? -1.f : 0.f);
+        const float fz = bz == 1 ? 1.f : (bz == 2 ? -1.f : 0.f);
+        const bool pad = bx == 3 || by == 3 || bz == 3;
+        shift[c] = pad ? make_float4(1e18f, 1e18f, 1e18f, 0.f)
+                       : make_float4(fx * sp.fcs[0], fy * sp.fcs[1], fz * sp.fcs[2], 0.f);
+    }
+}
+
+// Per-atom accumulator of the mixed kernels: FP32 pair terms summed over a batch, batch sums
+// added in FP64 (ACC = 0) or kept as compensated FP32 sums (ACC = 1) and converted at the end.
+template <int ACC>
+struct MixAcc {
+    double fx = 0.0, fy = 0.0, fz = 0.0, e = 0.0;
+    float px = 0.f, py = 0.f, pz = 0.f, pe = 0.f;  // current batch sums
+    float cx = 0.f, cy = 0.f, cz = 0.f, ce = 0.f;  // Kahan compensation (ACC = 1)
+    float sx = 0.f, sy = 0.f, sz = 0.f, se = 0.f;  // Kahan sums (ACC = 1)
+    __device__ __forceinline__ void fold() {
+        if (ACC == 0) {
+            fx += (double)px;
+            fy += (double)py;
+            fz += (double)pz;
+            e += (double)pe;
+        } else {
+            float y = px - cx, t = sx + y;
+            cx = (t - sx) - y;
+            sx = t;
+            y = py - cy, t = sy + y;
+            cy = (t - sy) - y;
+            sy = t;
+            y = pz - cz, t = sz + y;
+            cz = (t - sz) - y;
+            sz = t;
+            y = pe - ce, t = se + y;
+            ce = (t - se) - y;
+            se = t;
+        }
+        px = py = pz = pe = 0.f;
+    }
+    __device__ __forceinline__ void finish() {
+        fold();
+        if (ACC == 1) {
+            fx = (double)sx - (double)cx;
+            fy = (double)sy - (double)cy;
+            fz = (double)sz - (double)cz;
+            e = (double)se - (double)ce;
+        }
+    }
+};
+
+// Pair constants of atom i's type row (the single-type case reads entry 0 once).
+struct MixLJ {
+    float frc2, fs2, fe24, fe4, fuc;
+};
+
+// The FP32 LJ terms of one batch of list entries against atom i (cell-relative coordinates pi):
+// gathers of every neighbour's prel first (all in flight together), then the pair math, summed
+// into the accumulator's batch sums.
+template <bool ONE, int NB, int ACC>
+__device__ __forceinline__ void mixed_pairs(const uint32_t (&ent)[NB], const float4* __restrict__ prel,
+                                            const float4& pi, const float4* shift, const LJDev* tab,
+                                            const MixLJ& P0, MixAcc<ACC>& a) {
+    float4 pj[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) pj[b] = __ldg(prel + (ent[b] & JMASK));
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const float4 sv = shift[ent[b] >> JBITS];
+        const float dx = (pj[b].x - pi.x) + sv.x;
+        const float dy = (pj[b].y - pi.y) + sv.y;
+        const float dz = (pj[b].z - pi.z) + sv.z;
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        float frc2 = P0.frc2, fs2 = P0.fs2, fe24 = P0.fe24, fe4 = P0.fe4, fuc = P0.fuc;
+        if (!ONE) {
+            const LJDev& L = tab[__float_as_int(pj[b].w)];
+            frc2 = L.present ? L.frc2 : -1.f;
+            fs2 = L.fsigma2;
+            fe24 = L.feps24;
+            fe4 = L.feps4;
+            fuc = L.fucut;
+        }
+        // evaluated for every entry and masked, so the warp never splits on the cutoff
+        // (padding entries have r2 ~ 1e36: 1/r2 -> 0, masked anyway)
+        const bool in = r2 <= frc2;
+        const float inv = rcp_approx(r2);
+        const float s2 = fs2 * inv;
+        const float s6 = s2 * s2 * s2;
+        // 24 eps s6 (2 s6 - 1) / r^2 and 4 eps (s6^2 - s6) - u(rc)
+        const float c = in ? (s6 * fmaf(2.0f, s6, -1.0f)) * (fe24 * inv) : 0.f;
+        const float u = in ? fmaf(fe4, fmaf(s6, s6, -s6), -fuc) : 0.f;
+        a.px = fmaf(-c, dx, a.px);
+        a.py = fmaf(-c, dy, a.py);
+        a.pz = fmaf(-c, dz, a.pz);
+        a.pe += u;
+    }
+}
+
+__device__ __forceinline__ MixLJ mix_lj_load(const LJDev& L) {
+    return MixLJ{L.frc2, L.fsigma2, L.feps24, L.feps4, L.fucut};
+}
+
+constexpr int MIX_FLUSH = 32;  // entries per lane between FP64 (or compensated) folds
+
 template <int ACC, int LPA, bool ONE, int MIX_BATCH>
 __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) {
     __shared__ double sh[32];
@@ -807,58 +1061,21 @@ __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) 
     if (s < 0) return;
     if (!slot_runs(P, s, step_mode)) return;
     const SysParams& sp = P.sp[s];
-    if (threadIdx.x < 64) {
-        // code -> image shift; a 3 in any field marks a padding entry and sends it out of range
-        const int c = threadIdx.x;
-        const int bx = c & 3, by = (c >> 2) & 3, bz = (c >> 4) & 3;
-        const float fx = bx == 1 ? 1.f : (bx == 2 ? -1.f : 0.f);
-        const float fy = by == 1 ? 1.f : (by == 2 ? -1.f : 0.f);
-        const float fz = bz == 1 ? 1.f : (bz == 2 ? -1.f : 0.f);
-        const bool pad = bx == 3 || by == 3 || bz == 3;
-        shift[c] = pad ? make_float4(1e18f, 1e18f, 1e18f, 0.f)
-                       : make_float4(fx * sp.fcs[0], fy * sp.fcs[1], fz * sp.fcs[2], 0.f);
-    }
+    fill_shift_table(shift, sp);
     __syncthreads();
     const int gl = (int)tile.thread_rank();
-    constexpr int FLUSH = 32;  // entries per lane between FP64 (or compensated) folds
-    double e = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
+    MixAcc<ACC> acc;
     if (live) {
         const float4* __restrict__ prel = P.prel;
         const float4 pi = prel[i];
         const int ti = __float_as_int(pi.w);
         const LJDev* tab = P.tab + sp.tab0 + ti * sp.nt;
-        const float frc2_0 = tab[0].frc2, fs2_0 = tab[0].fsigma2, fe24_0 = tab[0].feps24, fe4_0 = tab[0].feps4,
-                    fuc_0 = tab[0].fucut;
-        float cx = 0.f, cy = 0.f, cz = 0.f, ce = 0.f;  // Kahan compensation (ACC = 1)
-        float sx = 0.f, sy = 0.f, sz = 0.f, se = 0.f;  // Kahan sums (ACC = 1)
+        const MixLJ P0 = mix_lj_load(tab[0]);
         const int nn = P.nn[i];
         const int64_t row = P.npad * LPA;
         const uint32_t* __restrict__ nbp = P.nbr + (int64_t)i * LPA + gl;
         const uint32_t pad = (uint32_t)i | (63u << JBITS);
-        float px = 0.f, py = 0.f, pz = 0.f, pe = 0.f;
         int since = 0;
-        auto fold = [&]() {
-            if (ACC == 0) {
-                fx += (double)px;
-                fy += (double)py;
-                fz += (double)pz;
-                e += (double)pe;
-            } else {
-                float y = px - cx, t = sx + y;
-                cx = (t - sx) - y;
-                sx = t;
-                y = py - cy, t = sy + y;
-                cy = (t - sy) - y;
-                sy = t;
-                y = pz - cz, t = sz + y;
-                cz = (t - sz) - y;
-                sz = t;
-                y = pe - ce, t = se + y;
-                ce = (t - se) - y;
-                se = t;
-            }
-            px = py = pz = pe = 0.f;
-        };
         // list words are addressed with 32-bit offsets from the lane's first word (the pool's list
         // is below 2^32 words, checked at init); full batches load unconditionally, the last
         // partial batch pads with an out-of-range entry
@@ -875,53 +1092,16 @@ __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) 
                     ent[b] = (k0 + b * LPA + gl < nn) ? __ldg(nbp + qoff + (uint32_t)b * row32) : pad;
             }
             qoff += (uint32_t)MIX_BATCH * row32;
-            float4 pj[MIX_BATCH];
-#pragma unroll
-            for (int b = 0; b < MIX_BATCH; ++b) pj[b] = __ldg(prel + (ent[b] & JMASK));
-#pragma unroll
-            for (int b = 0; b < MIX_BATCH; ++b) {
-                const float4 sv = shift[ent[b] >> JBITS];
-                const float dx = (pj[b].x - pi.x) + sv.x;
-                const float dy = (pj[b].y - pi.y) + sv.y;
-                const float dz = (pj[b].z - pi.z) + sv.z;
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                float frc2 = frc2_0, fs2 = fs2_0, fe24 = fe24_0, fe4 = fe4_0, fuc = fuc_0;
-                if (!ONE) {
-                    const LJDev& L = tab[__float_as_int(pj[b].w)];
-                    frc2 = L.present ? L.frc2 : -1.f;
-                    fs2 = L.fsigma2;
-                    fe24 = L.feps24;
-                    fe4 = L.feps4;
-                    fuc = L.fucut;
-                }
-                // evaluated for every entry and masked, so the warp never splits on the cutoff
-                // (padding entries have r2 ~ 1e36: 1/r2 -> 0, masked anyway)
-                const bool in = r2 <= frc2;
-                const float inv = rcp_approx(r2);
-                const float s2 = fs2 * inv;
-                const float s6 = s2 * s2 * s2;
-                // 24 eps s6 (2 s6 - 1) / r^2 and 4 eps (s6^2 - s6) - u(rc)
-                const float c = in ? (s6 * fmaf(2.0f, s6, -1.0f)) * (fe24 * inv) : 0.f;
-                const float u = in ? fmaf(fe4, fmaf(s6, s6, -s6), -fuc) : 0.f;
-                px = fmaf(-c, dx, px);
-                py = fmaf(-c, dy, py);
-                pz = fmaf(-c, dz, pz);
-                pe += u;
-            }
+            mixed_pairs<ONE, MIX_BATCH, ACC>(ent, prel, pi, shift, tab, P0, acc);
             since += MIX_BATCH;
-            if (since >= FLUSH) {
-                fold();
+            if (since >= MIX_FLUSH) {
+                acc.fold();
                 since = 0;
             }
         }
-        fold();
-        if (ACC == 1) {
-            fx = (double)sx - (double)cx;
-            fy = (double)sy - (double)cy;
-            fz = (double)sz - (double)cz;
-            e = (double)se - (double)ce;
-        }
+        acc.finish();
     }
+    double fx = acc.fx, fy = acc.fy, fz = acc.fz, e = acc.e;
 #pragma unroll
     for (int o = LPA / 2; o > 0; o >>= 1) {
         fx += tile.shfl_down(fx, o);
@@ -931,6 +1111,488 @@ __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) 
     if (live && gl == 0) P.frc[i] = make_double4_32a(fx, fy, fz, 0.0);
     double tot = block_sum<256>(e, sh);
     if (threadIdx.x == 0) P.pe_part[blockIdx.x] = tot;
+}
+
+// Mixed precision forces, thread per atom, with the neighbour list streamed into shared memory by
+// bulk copies (cp.async.bulk, the TMA engine's untiled mode). In the column-major list, row k of a
+// 256-atom chunk is one contiguous run of 256 words, so the chunk's list is a stack of 1 KB rows.
+// Thread 0 keeps MIX_TMA_STAGES batches of KB rows in flight in a shared-memory ring (one
+// mbarrier per stage counts the copied bytes); the threads read their entries from shared memory
+// instead of waiting on DRAM for each batch, then gather neighbour positions and do the same pair
+// arithmetic as k_force_mixed. A stage is refilled once all 8 warps have released it (a second
+// mbarrier per stage). Every wait is bounded: on expiry the block sets FLAG_TIMEOUT and stops.
+// A row copy starts at the chunk's first atom rounded down to 4 (16-byte alignment) and covers
+// the chunk's atoms rounded up to 4, which stays inside the list row (npad is a multiple of 32).
+constexpr int MIX_TMA_STAGES = 4;
+constexpr int MIX_TMA_ROW = 260;  // words per ring row: 256 atoms + up to 3 of alignment offset
+
+template <int KB>
+constexpr size_t mix_tma_smem_bytes() {
+    return (size_t)MIX_TMA_STAGES * KB * MIX_TMA_ROW * sizeof(uint32_t);
+}
+
+template <int ACC, bool ONE, int KB>
+__global__ void __launch_bounds__(256, KB <= 8 ? 4 : 2) k_force_mixed_tma(const DP P, int step_mode) {
+    constexpr int S = MIX_TMA_STAGES;
+    extern __shared__ __align__(128) uint32_t ring[];  // S * KB * MIX_TMA_ROW words
+    __shared__ double sh[32];
+    __shared__ float4 shift[64];
+    __shared__ __align__(8) uint64_t full[S];
+    __shared__ __align__(8) uint64_t empty[S];
+    __shared__ int wmax[8];
+    int s, i;
+    const bool live = atom_of(P, s, i);
+    if (s < 0) return;                             // uniform per block (one slot per chunk)
+    if (!slot_runs(P, s, step_mode)) return;
+    const SysParams& sp = P.sp[s];
+    SysState& st = P.st[s];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    fill_shift_table(shift, sp);
+    const int first = P.blk_first[blockIdx.x];
+    const int cnt = min(256, (int)(sp.a0 + sp.n) - first);
+    const int off = first & 3;
+    const uint32_t row_bytes = (uint32_t)((off + cnt + 3) & ~3) * 4u;
+    const int nn = live ? P.nn[i] : 0;
+    const int m = __reduce_max_sync(0xffffffffu, nn);
+    if (lane == 0) wmax[w] = m;
+    if (t == 0) {
+        for (int q = 0; q < S; ++q) {
+            mbar_init(&full[q], 1);
+            mbar_init(&empty[q], 8);
+        }
+        mbar_fence_init();
+    }
+    __syncthreads();
+    int nmax = wmax[0];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) nmax = max(nmax, wmax[q]);
+    const int R = (nmax + KB - 1) / KB;
+    const uint32_t* __restrict__ src0 = P.nbr + (first - off);
+    const int64_t npad = P.npad;
+    auto issue = [&](int r) {
+        const int q0 = r % S, k0 = r * KB;
+        const int rows = min(KB, nmax - k0);
+        mbar_arrive_tx(&full[q0], (uint32_t)rows * row_bytes);
+        for (int q = 0; q < rows; ++q)
+            bulk_g2s(ring + (q0 * KB + q) * MIX_TMA_ROW, src0 + (int64_t)(k0 + q) * npad, row_bytes, &full[q0]);
+    };
+    int issued = 0;
+    if (t == 0)
+        for (; issued < min(S, R); ++issued) issue(issued);
+
+    MixAcc<ACC> acc;
+    const float4* __restrict__ prel = P.prel;
+    const float4 pi = live ? prel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const LJDev* tab = P.tab + sp.tab0 + (live ? __float_as_int(pi.w) : 0) * sp.nt;
+    const MixLJ P0 = mix_lj_load(tab[0]);
+    const uint32_t pad = (uint32_t)(live ? i : first) | (63u << JBITS);
+    const int col = off + t;
+    // A thread whose wait expires stops waiting (and thread 0 stops issuing) but keeps running the
+    // loop, so every lane still reaches each warp-level sync; its remaining entries are skipped.
+    bool failed = false;
+    int done = 0;  // batches this thread has seen arrive
+    for (int r = 0; r < R; ++r) {
+        const int q0 = r % S;
+        const uint32_t par = (uint32_t)(r / S) & 1u;
+        if (!failed && !mbar_wait(&full[q0], par)) failed = true;
+        if (!failed) {
+            done = r + 1;
+            const int k0 = r * KB;
+            if (k0 < nn) {
+                uint32_t ent[KB];
+                const uint32_t* rp = ring + q0 * KB * MIX_TMA_ROW + col;
+#pragma unroll
+                for (int b = 0; b < KB; ++b) ent[b] = (k0 + b < nn) ? rp[b * MIX_TMA_ROW] : pad;
+                mixed_pairs<ONE, KB, ACC>(ent, prel, pi, shift, tab, P0, acc);
+                if (((r + 1) * KB) % MIX_FLUSH == 0) acc.fold();
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[q0]);
+        if (t == 0 && !failed && issued < R) {
+            // refill this stage with batch r + S once every warp has released batch r
+            if (mbar_wait(&empty[q0], par))
+                issue(issued++);
+            else
+                failed = true;
+        }
+    }
+    if (failed) {
+        atomicOr(&st.flags, FLAG_TIMEOUT);
+        // no copies are left in flight into shared memory: thread 0 waits (bounded) for every
+        // batch it issued and has not seen arrive
+        if (t == 0)
+            for (int r = done; r < issued; ++r) mbar_wait(&full[r % S], (uint32_t)(r / S) & 1u);
+    }
+    acc.finish();
+    if (live) P.frc[i] = make_double4_32a(acc.fx, acc.fy, acc.fz, 0.0);
+    double tot = block_sum<256>(acc.e, sh);
+    if (threadIdx.x == 0) P.pe_part[blockIdx.x] = tot;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Cluster-list path (mixed precision). A cluster is a run of up to M consecutive atoms of one
+// cell; atoms are ordered inside each cell along a Morton curve, so a cluster's members are close
+// in space. One thread owns a cluster: its members' coordinates live in registers, and its list
+// holds every atom within the list radius of ANY member. Each list word and each neighbour
+// gather then serves M pair evaluations instead of one, which cuts the scattered cache traffic
+// that bounds the per-atom kernel; the price is the pairs of the union that a given member does
+// not need (masked by the cutoff test).
+// ---------------------------------------------------------------------------------------------
+constexpr int CL_THREADS = 128;
+
+// Build: thread per cluster. Every one of the 27 neighbour cell images whose box lies within the
+// list radius of the members' bounding box is scanned, and an atom is appended when it is within
+// the list radius of any member (FP32 on cell-relative coordinates, radius padded so the list is
+// a superset). Lanes of one home cell walk the same cells in the same order, so their candidate
+// loads coincide. On an axis with two cells the -1 and +1 images are the same cell at two shifts:
+// both are scanned and an atom may be listed once per image; for any one member at most one image
+// lies within the radius (the box is longer than twice the radius), so no pair counts twice.
+template <int M>
+__device__ __forceinline__ void build_cl_chunk(const DP& P, int blk, int step_mode) {
+    const int s = P.cblk_sys[blk];
+    if (s < 0) return;
+    if (!slot_runs(P, s, step_mode)) return;
+    const SysParams& sp = P.sp[s];
+    SysState& st = P.st[s];
+    if (!st.rebuild) return;
+    const int c = P.cblk_first[blk] + (int)threadIdx.x;
+    if (c >= sp.cl0 + st.ncl) return;
+    const uint32_t pk = (uint32_t)P.cl_atom[c];
+    const int first = (int)(pk & JMASK), n = (int)(pk >> JBITS) + 1;
+    const int nx = sp.nc[0], ny = sp.nc[1], nz = sp.nc[2];
+    const int lc = P.cellof[first];
+    const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
+    const float4* __restrict__ prel = P.prel;
+    float mx[M], my[M], mz[M];
+    float lox = 1e30f, loy = 1e30f, loz = 1e30f, hix = -1e30f, hiy = -1e30f, hiz = -1e30f;
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        if (m < n) {
+            const float4 q = prel[first + m];
+            mx[m] = q.x;
+            my[m] = q.y;
+            mz[m] = q.z;
+            lox = fminf(lox, q.x);
+            loy = fminf(loy, q.y);
+            loz = fminf(loz, q.z);
+            hix = fmaxf(hix, q.x);
+            hiy = fmaxf(hiy, q.y);
+            hiz = fmaxf(hiz, q.z);
+        } else {
+            mx[m] = my[m] = mz[m] = 1e18f;  // padding member: never within the radius
+        }
+    }
+    const float csx = sp.fcs[0], csy = sp.fcs[1], csz = sp.fcs[2];
+    const float rl2 = sp.frlist2;
+    const int64_t clpad = P.clpad;
+    const int cap = P.ccap;
+    const int32_t* __restrict__ cstart = P.cell_start + sp.c0;
+    uint32_t* out = P.cl_nbr + c;
+    int cnt = 0;
+    for (int oz = -1; oz <= 1; ++oz) {
+        const int z2 = wrapc(cz + oz, nz);
+        // gap between the members' extent and the neighbour image's extent (home-cell frame)
+        const float gz = fmaxf(fmaxf((oz - 0.5f) * csz - hiz, loz - (oz + 0.5f) * csz), 0.f);
+        for (int oy = -1; oy <= 1; ++oy) {
+            const int y2 = wrapc(cy + oy, ny);
+            const float gy = fmaxf(fmaxf((oy - 0.5f) * csy - hiy, loy - (oy + 0.5f) * csy), 0.f);
+            const float gyz = fmaf(gy, gy, gz * gz);
+            if (gyz > rl2) continue;
+            for (int ox = -1; ox <= 1; ++ox) {
+                const float gx = fmaxf(fmaxf((ox - 0.5f) * csx - hix, lox - (ox + 0.5f) * csx), 0.f);
+                if (fmaf(gx, gx, gyz) > rl2) continue;
+                const int x2 = wrapc(cx + ox, nx);
+                const int nb = (z2 * ny + y2) * nx + x2;
+                const int b0 = cstart[nb], b1 = cstart[nb + 1];
+                const uint32_t codebits = (((uint32_t)(ox < 0 ? 2 : ox)) | ((uint32_t)(oy < 0 ? 2 : oy) << 2) |
+                                           ((uint32_t)(oz < 0 ? 2 : oz) << 4))
+                                          << JBITS;
+                // the members in the frame of this neighbour image
+                float qx[M], qy[M], qz[M];
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    qx[m] = mx[m] - ox * csx;
+                    qy[m] = my[m] - oy * csy;
+                    qz[m] = mz[m] - oz * csz;
+                }
+                const bool roomy = cnt + (b1 - b0) <= cap;
+                for (int j = b0; j < b1; ++j) {
+                    const float4 pj = prel[j];
+                    bool take = false;
+#pragma unroll
+                    for (int m = 0; m < M; ++m) {
+                        const float dx = pj.x - qx[m], dy = pj.y - qy[m], dz = pj.z - qz[m];
+                        take |= fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= rl2;
+                    }
+                    if (take) {
+                        if (roomy || cnt < cap) *out = (uint32_t)j | codebits;
+                        out += clpad;
+                        ++cnt;
+                    }
+                }
+            }
+        }
+    }
+    if (cnt > cap) atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
+    P.cl_nn[c] = cnt > cap ? cap : cnt;
+}
+template <int M>
+__global__ void __launch_bounds__(CL_THREADS) k_build_cl(const DP P, int step_mode, int nblk) {
+    if (!rebuild_pending(P)) return;
+    PIS_FOR_CHUNKS(nblk) build_cl_chunk<M>(P, blk, step_mode);
+}
+
+// Per-atom lists built per cluster (the default build of the thread-per-atom layout): one thread
+// scans the candidates of a cluster's M members and writes each member's own list. Every member
+// gets exactly the list k_build1 gives it - the same neighbour cells in the same order, skipped by
+// the same per-atom face-distance test, the same FP32 distance arithmetic, self / half exclusion
+// and capacity handling - but each candidate position is loaded once for M members, and the lanes
+// of one home cell walk the same cells together. Slots with a two-cell axis are left to
+// k_build1_generic.
+template <bool HALF, int M>
+__device__ __forceinline__ void build1_cl_chunk(const DP& P, int blk, int step_mode) {
+    const int s = P.cblk_sys[blk];
+    if (s < 0) return;
+    if (!slot_runs(P, s, step_mode)) return;
+    const SysParams& sp = P.sp[s];
+    SysState& st = P.st[s];
+    if (!st.rebuild) return;
+    const int nx = sp.nc[0], ny = sp.nc[1], nz = sp.nc[2];
+    if (nx < 3 || ny < 3 || nz < 3) return;
+    const int c = P.cblk_first[blk] + (int)threadIdx.x;
+    if (c >= sp.cl0 + st.ncl) return;
+    const uint32_t pk = (uint32_t)P.cl_atom[c];
+    const int first = (int)(pk & JMASK), n = (int)(pk >> JBITS) + 1;
+    const int lc = P.cellof[first];
+    const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
+    const float4* __restrict__ prel = P.prel;
+    const float csx = sp.fcs[0], csy = sp.fcs[1], csz = sp.fcs[2];
+    const float rl2 = sp.frlist2;
+    const int64_t npad = P.npad;
+    const int cap = P.cap;
+    const int32_t* __restrict__ cstart = P.cell_start + sp.c0;
+    float px[M], py[M], pz[M];
+    uint32_t* out[M];
+    int cnt[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        const float4 q = prel[first + (m < n ? m : 0)];
+        px[m] = q.x;
+        py[m] = q.y;
+        pz[m] = q.z;
+        out[m] = P.nbr + first + m;
+        cnt[m] = 0;
+    }
+    for (int oz = -1; oz <= 1; ++oz) {
+        const int z2 = wrapc(cz + oz, nz);
+        for (int oy = -1; oy <= 1; ++oy) {
+            const int y2 = wrapc(cy + oy, ny);
+            for (int ox = -1; ox <= 1; ++ox) {
+                // per member: k_build1's face-distance skip and its shift to the neighbour image
+                bool use[M];
+                float sx[M], sy[M], sz[M];
+                bool any = false;
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    const float ex = ox < 0 ? fmaxf(px[m] + 0.5f * csx, 0.f) : (ox > 0 ? fmaxf(0.5f * csx - px[m], 0.f) : 0.f);
+                    const float ey = oy < 0 ? fmaxf(py[m] + 0.5f * csy, 0.f) : (oy > 0 ? fmaxf(0.5f * csy - py[m], 0.f) : 0.f);
+                    const float ez = oz < 0 ? fmaxf(pz[m] + 0.5f * csz, 0.f) : (oz > 0 ? fmaxf(0.5f * csz - pz[m], 0.f) : 0.f);
+                    const float eyz = fmaf(ey, ey, ez * ez);
+                    use[m] = m < n && !(fmaf(ex, ex, eyz) > rl2);
+                    any |= use[m];
+                    sx[m] = ox * csx - px[m];
+                    sy[m] = oy * csy - py[m];
+                    sz[m] = oz * csz - pz[m];
+                }
+                if (!any) continue;
+                const int x2 = wrapc(cx + ox, nx);
+                const int nb = (z2 * ny + y2) * nx + x2;
+                const int b0 = cstart[nb], b1 = cstart[nb + 1];
+                const uint32_t codebits = (((uint32_t)(ox < 0 ? 2 : ox)) | ((uint32_t)(oy < 0 ? 2 : oy) << 2) |
+                                           ((uint32_t)(oz < 0 ? 2 : oz) << 4))
+                                          << JBITS;
+                const bool home = ox == 0 && oy == 0 && oz == 0;
+                for (int j = b0; j < b1; ++j) {
+                    const float4 pj = prel[j];
+#pragma unroll
+                    for (int m = 0; m < M; ++m) {
+                        const float dx = pj.x + sx[m], dy = pj.y + sy[m], dz = pj.z + sz[m];
+                        bool take = use[m] && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= rl2;
+                        if (HALF)
+                            take = take && j > first + m;
+                        else if (home)
+                            take = take && j != first + m;
+                        if (take) {
+                            if (cnt[m] < cap) *out[m] = (uint32_t)j | codebits;
+                            out[m] += npad;
+                            ++cnt[m];
+                        }
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        if (m >= n) continue;
+        if (cnt[m] > cap) atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
+        P.nn[first + m] = cnt[m] > cap ? cap : cnt[m];
+    }
+}
+template <bool HALF, int M>
+__global__ void __launch_bounds__(CL_THREADS) k_build1_cl(const DP P, int step_mode, int nblk) {
+    if (!rebuild_pending(P)) return;
+    PIS_FOR_CHUNKS(nblk) build1_cl_chunk<HALF, M>(P, blk, step_mode);
+}
+
+// Forces: thread per cluster. For each batch of NB list entries the words are loaded, then the
+// NB neighbour gathers, then every (member, entry) pair is evaluated with the same FP32
+// arithmetic as the per-atom kernel, masked by the pair's cutoff and by r^2 > 0 (a member meets
+// itself in the list at distance exactly zero). Per member the FP32 batch sums are folded into
+// FP64 every MIX_FLUSH entries (ACC = 0) or kept as compensated FP32 sums (ACC = 1).
+template <int ACC, bool ONE, int M, int NB>
+__global__ void __launch_bounds__(CL_THREADS) k_force_cl(const DP P, int step_mode) {
+    __shared__ double sh[32];
+    __shared__ float4 shift[64];
+    const int s = P.cblk_sys[blockIdx.x];
+    if (s < 0) return;
+    if (!slot_runs(P, s, step_mode)) return;
+    const SysParams& sp = P.sp[s];
+    fill_shift_table(shift, sp);
+    __syncthreads();
+    const int c = P.cblk_first[blockIdx.x] + (int)threadIdx.x;
+    const bool live = c < sp.cl0 + P.st[s].ncl;
+    double etot = 0.0;
+    if (live) {
+        const uint32_t pk = (uint32_t)P.cl_atom[c];
+        const int first = (int)(pk & JMASK), n = (int)(pk >> JBITS) + 1;
+        const float4* __restrict__ prel = P.prel;
+        const LJDev* tab0 = P.tab + sp.tab0;
+        float mx[M], my[M], mz[M];
+        const LJDev* tabm[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            if (m < n) {
+                const float4 q = prel[first + m];
+                mx[m] = q.x;
+                my[m] = q.y;
+                mz[m] = q.z;
+                tabm[m] = tab0 + __float_as_int(q.w) * sp.nt;
+            } else {
+                mx[m] = my[m] = mz[m] = 1e18f;
+                tabm[m] = tab0;
+            }
+        }
+        const MixLJ P0 = mix_lj_load(tab0[0]);
+        MixAcc<ACC> acc[M];
+        const int nn = P.cl_nn[c];
+        const uint32_t* __restrict__ nbp = P.cl_nbr + c;
+        const uint32_t row = (uint32_t)P.clpad;
+        const uint32_t pad = (uint32_t)first | (63u << JBITS);
+        int since = 0;
+        // list words of batch k0 + NB are loaded before batch k0 is evaluated, so the DRAM latency
+        // of the list stream overlaps the pair arithmetic
+        auto load_batch = [&](int k0, uint32_t (&e)[NB]) {
+            const uint32_t q = (uint32_t)k0 * row;
+            if (k0 + NB <= nn) {
+#pragma unroll
+                for (int b = 0; b < NB; ++b) e[b] = __ldg(nbp + q + (uint32_t)b * row);
+            } else {
+#pragma unroll
+                for (int b = 0; b < NB; ++b) e[b] = (k0 + b < nn) ? __ldg(nbp + q + (uint32_t)b * row) : pad;
+            }
+        };
+        uint32_t next[NB];
+        load_batch(0, next);
+        for (int k0 = 0; k0 < nn; k0 += NB) {
+            uint32_t ent[NB];
+#pragma unroll
+            for (int b = 0; b < NB; ++b) ent[b] = next[b];
+            if (k0 + NB < nn) load_batch(k0 + NB, next);
+            float4 pj[NB];
+#pragma unroll
+            for (int b = 0; b < NB; ++b) pj[b] = __ldg(prel + (ent[b] & JMASK));
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                const float4 sv = shift[ent[b] >> JBITS];
+                const float jx = pj[b].x + sv.x, jy = pj[b].y + sv.y, jz = pj[b].z + sv.z;
+                const int tj = __float_as_int(pj[b].w);
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    const float dx = jx - mx[m], dy = jy - my[m], dz = jz - mz[m];
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    float frc2 = P0.frc2, fs2 = P0.fs2, fe24 = P0.fe24, fe4 = P0.fe4, fuc = P0.fuc;
+                    if (!ONE) {
+                        const LJDev& L = tabm[m][tj];
+                        frc2 = L.present ? L.frc2 : -1.f;
+                        fs2 = L.fsigma2;
+                        fe24 = L.feps24;
+                        fe4 = L.feps4;
+                        fuc = L.fucut;
+                    }
+                    const bool in = r2 <= frc2 && r2 > 0.f;
+                    const float inv = rcp_approx(r2);
+                    const float s2 = fs2 * inv;
+                    const float s6 = s2 * s2 * s2;
+                    const float cf = in ? (s6 * fmaf(2.0f, s6, -1.0f)) * (fe24 * inv) : 0.f;
+                    const float u = in ? fmaf(fe4, fmaf(s6, s6, -s6), -fuc) : 0.f;
+                    acc[m].px = fmaf(-cf, dx, acc[m].px);
+                    acc[m].py = fmaf(-cf, dy, acc[m].py);
+                    acc[m].pz = fmaf(-cf, dz, acc[m].pz);
+                    acc[m].pe += u;
+                }
+            }
+            since += NB;
+            if (since >= MIX_FLUSH) {
+#pragma unroll
+                for (int m = 0; m < M; ++m) acc[m].fold();
+                since = 0;
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            acc[m].finish();
+            if (m < n) {
+                P.frc[first + m] = make_double4_32a(acc[m].fx, acc[m].fy, acc[m].fz, 0.0);
+                etot += acc[m].e;
+            }
+        }
+    }
+    double tot = block_sum<CL_THREADS>(etot, sh);
+    if (threadIdx.x == 0) P.pe_part[blockIdx.x] = tot;
+}
+
+// Exact cutoff test of every (member, entry) pair of one slot's cluster lists with the reference
+// arithmetic (min-image, Vector3::norm, `> rcut`), for neighbour-set export: bit m of keep marks
+// member m.
+__global__ void __launch_bounds__(CL_THREADS) k_keep_cl(const DP P, int slot) {
+    const int s = P.cblk_sys[blockIdx.x];
+    if (s != slot) return;
+    const SysParams& sp = P.sp[s];
+    const int c = P.cblk_first[blockIdx.x] + (int)threadIdx.x;
+    if (c >= sp.cl0 + P.st[s].ncl) return;
+    const uint32_t pk = (uint32_t)P.cl_atom[c];
+    const int first = (int)(pk & JMASK), n = (int)(pk >> JBITS) + 1;
+    const int cur = P.st[s].cur;
+    const double4_32a* pos = P.pos[cur];
+    for (int k = 0; k < P.cl_nn[c]; ++k) {
+        const int64_t q = (int64_t)k * P.clpad + c;
+        const int j = (int)(P.cl_nbr[q] & JMASK);
+        const double4_32a pj = pos[j];
+        uint8_t mask = 0;
+        for (int m = 0; m < n; ++m) {
+            const int i = first + m;
+            if (i == j) continue;
+            const double4_32a pi = pos[i];
+            const double rx = min_image_axis(__dsub_rn(pj.x, pi.x), sp.h[0], sp.hinv[0]);
+            const double ry = min_image_axis(__dsub_rn(pj.y, pi.y), sp.h[1], sp.hinv[1]);
+            const double rz = min_image_axis(__dsub_rn(pj.z, pi.z), sp.h[2], sp.hinv[2]);
+            const LJDev& L = P.tab[sp.tab0 + type_of(pi.w) * sp.nt + type_of(pj.w)];
+            if (L.present && !(sqrt(norm2_ref(rx, ry, rz)) > L.rcut)) mask |= (uint8_t)(1u << m);
+        }
+        P.keep[q] = mask;
+    }
 }
 
 // Second half of verlet_step_nve (src/potentials/potential.rs:28-30):
@@ -1002,6 +1664,8 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
 // mode 0: step; mode 1: force evaluation only (PE); mode 2: KE/virial only.
 __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) {
     __shared__ double sh[32];
+    // every rebuild of this step or evaluation is done: lower the device-wide request word
+    if (mode != 2 && blockIdx.x == 0 && threadIdx.x == 0) P.ctl[0] = 0;
     int s = blockIdx.x;
     const SysParams& sp = P.sp[s];
     if (!sp.active) return;
@@ -1010,8 +1674,12 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
     if (mode != 0 && !st.eval) return;
     double pe = 0.0, ke = 0.0;
     const int F = P.pe_stride;
-    if (mode != 2)
-        for (int c = threadIdx.x; c < sp.nch * F; c += END_THREADS) pe += P.pe_part[(int64_t)sp.ch0 * F + c];
+    if (mode != 2) {
+        if (P.cl_force)  // cluster kernels: one partial per cluster chunk
+            for (int c = threadIdx.x; c < sp.ncch; c += END_THREADS) pe += P.pe_part[(int64_t)sp.cch0 + c];
+        else
+            for (int c = threadIdx.x; c < sp.nch * F; c += END_THREADS) pe += P.pe_part[(int64_t)sp.ch0 * F + c];
+    }
     if (mode != 1)
         for (int c = threadIdx.x; c < sp.nch; c += END_THREADS) ke += P.ke_part[sp.ch0 + c];
     pe = block_sum<END_THREADS>(pe, sh);
@@ -1058,7 +1726,10 @@ __global__ void k_mark_eval(const DP P, int only, int rebuild, int virial) {
     if (only >= 0 && s != only) return;
     P.st[s].eval = 1;
     P.st[s].want_virial = virial;
-    if (rebuild) P.st[s].rebuild = 1;
+    if (rebuild) {
+        P.st[s].rebuild = 1;
+        P.ctl[0] = 1;
+    }
 }
 
 __global__ void k_zero_forces(const DP P) {
@@ -1148,6 +1819,14 @@ pis_status Engine::check(cudaError_t e, const char* what, std::string& err) {
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// Grid of a strided rebuild kernel: its chunk count, capped at `per_sm` blocks per SM (one wave
+// of full occupancy for the block size used).
+unsigned Engine::grid_cap(int64_t chunks, int per_sm) const {
+    const int64_t cap = (int64_t)per_sm * num_sms_;
+    return (unsigned)(chunks < cap ? chunks : cap);
+}
+static cudaError_t allow_all_mixed_tma_smem();
+
 pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     opt_ = opt;
     if (opt.max_atoms <= 0 || opt.max_slots <= 0) {
@@ -1168,6 +1847,29 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         err = "the mixed-precision path uses a full list";
         return PIS_ERR_UNSUPPORTED;
     }
+    if (opt.list_tma && (opt.precision != PIS_PRECISION_MIXED || opt.lpa != 1)) {
+        err = "the bulk-copy list stream is a variant of the mixed, thread-per-atom force kernel";
+        return PIS_ERR_UNSUPPORTED;
+    }
+    if (opt.list_tma) {
+        pis_status st0 = check(allow_all_mixed_tma_smem(), "shared-memory attribute", err);
+        if (st0) return st0;
+    }
+    if (opt.cluster != 0 && opt.cluster != 2 && opt.cluster != 4) {
+        err = "atoms per cluster must be 2 or 4";
+        return PIS_ERR_INVALID_ARGUMENT;
+    }
+    if (opt.cluster && (opt.precision != PIS_PRECISION_MIXED || opt.lpa != 1 || opt.list_tma)) {
+        err = "the cluster list is a variant of the mixed path with one thread per cluster";
+        return PIS_ERR_UNSUPPORTED;
+    }
+    if (opt.build_cluster != 0 && opt.build_cluster != 1 && opt.build_cluster != 2 && opt.build_cluster != 4) {
+        err = "atoms per build cluster must be 1, 2 or 4";
+        return PIS_ERR_INVALID_ARGUMENT;
+    }
+    // cluster table: built for the cluster-list force path, and for the per-atom list build when
+    // it scans candidates per cluster (thread-per-atom layout only)
+    clm_ = opt.cluster ? opt.cluster : ((opt.lpa == 1 && opt.build_cluster > 1) ? opt.build_cluster : 0);
     if (opt.max_atoms >= (int64_t)JMASK) {
         err = "a pool holds at most 2^26 - 1 atoms (neighbour entries carry a 26-bit index)";
         return PIS_ERR_UNSUPPORTED;
@@ -1182,11 +1884,35 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     max_chunks_ = (opt.max_atoms + opt.blk - 1) / opt.blk + opt.max_slots;
     int64_t max_cells = opt.max_cells > 0 ? opt.max_cells : opt.max_atoms + opt.max_slots;
     opt_.max_cells = max_cells;
+    if (clm_) {
+        // per slot: ceil(n / M) clusters plus at most one partial cluster per cell
+        const int M = clm_;
+        max_clusters_ = (opt.max_atoms + M - 1) / M + max_cells + opt.max_slots;
+        clpad_ = (int64_t)align_up((size_t)max_clusters_, 32);
+        // union of M members' lists: ~1.4x (M = 2) / ~1.9x (M = 4) one atom's list
+        ccap_ = opt.cluster ? (int64_t)std::ceil((double)cap_ * (M == 2 ? 1.5 : 2.0)) : 0;
+        ccap_ = (ccap_ + 31) / 32 * 32;
+        max_cchunks_ = (max_clusters_ + CL_THREADS - 1) / CL_THREADS + opt.max_slots;
+        if ((double)clpad_ * (double)ccap_ >= 4294967296.0) {
+            err = "cluster list of the pool exceeds 2^32 entries (clusters x capacity)";
+            return PIS_ERR_NO_MEMORY;
+        }
+    }
     pis_status st = check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream", err);
     if (st) return st;
+    {
+        int dev = 0, sms = 0;
+        st = check(cudaGetDevice(&dev), "device", err);
+        if (st) return st;
+        st = check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device", err);
+        if (st) return st;
+        num_sms_ = sms > 0 ? sms : 1;
+    }
 
     const size_t NA = (size_t)opt.max_atoms, NC = (size_t)max_cells, NCH = (size_t)max_chunks_,
-                 NS = (size_t)opt.max_slots;
+                 NS = (size_t)opt.max_slots, NCL = (size_t)max_clusters_, NCC = (size_t)max_cchunks_;
+    // the per-atom list is not used (and kept minimal) when the cluster list is
+    const size_t nbr_bytes = opt.cluster ? 256 : 4 * (size_t)npad_ * cap_;
     struct Item {
         void** p;
         size_t bytes;
@@ -1199,14 +1925,25 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         {(void**)&d_->id[0], 4 * NA},   {(void**)&d_->id[1], 4 * NA},   {(void**)&d_->frc, 32 * NA},
         {(void**)&d_->posb, 32 * NA},   {(void**)&d_->prel, 16 * NA}, {(void**)&d_->prelb, 16 * NA},   {(void**)&d_->cellof, 4 * NA},
         {(void**)&d_->lcell, 4 * NA},   {(void**)&d_->slotin, 4 * NA},  {(void**)&d_->perm, 4 * NA},
-        {(void**)&d_->nn, 4 * NA},      {(void**)&d_->nbr, 4 * (size_t)npad_ * cap_},
+        {(void**)&d_->nn, 4 * NA},      {(void**)&d_->nbr, nbr_bytes},
         {(void**)&d_->cell_count, 4 * NC}, {(void**)&d_->cell_start, 4 * NC},
         {(void**)&d_->cell_sys, 4 * NC}, {(void**)&d_->blk_sys, 4 * NCH},
         {(void**)&d_->blk_first, 4 * NCH}, {(void**)&d_->sp, sizeof(SysParams) * NS},
         {(void**)&d_->st, sizeof(SysState) * NS}, {(void**)&d_->tab, sizeof(LJDev) * (size_t)opt.max_types_total},
-        {(void**)&d_->pe_part, 8 * NCH * 32}, {(void**)&d_->ke_part, 8 * NCH}, {(void**)&d_->vir_part, 72 * NCH},
-        {(void**)&d_->pe_hist, 8 * NS * (size_t)opt.hist},
+        {(void**)&d_->pe_part, 8 * std::max(NCH * 32, NCC)}, {(void**)&d_->ke_part, 8 * NCH},
+        {(void**)&d_->vir_part, 72 * NCH}, {(void**)&d_->pe_hist, 8 * NS * (size_t)opt.hist},
+        {(void**)&d_->ctl, 256},
     };
+    if (clm_) {
+        items.push_back({(void**)&d_->cl_atom, 4 * NCL});
+        items.push_back({(void**)&d_->cl_start, 4 * NC});
+        items.push_back({(void**)&d_->cblk_sys, 4 * NCC});
+        items.push_back({(void**)&d_->cblk_first, 4 * NCC});
+    }
+    if (opt.cluster) {
+        items.push_back({(void**)&d_->cl_nn, 4 * NCL});
+        items.push_back({(void**)&d_->cl_nbr, 4 * (size_t)clpad_ * (size_t)ccap_});
+    }
     size_t total = 0;
     for (auto& it : items) total += align_up(it.bytes, 256);
     st = check(cudaMalloc(&mem_, total), "device allocation", err);
@@ -1225,18 +1962,28 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     d_->zero_forces = half_ ? 1 : 0;
     d_->full_list = half_ ? 0 : 1;
     d_->pe_stride = opt_.lpa;
+    d_->clpad = clpad_;
+    d_->ccap = (int32_t)ccap_;
+    d_->clm = clm_;
+    d_->cl_force = opt.cluster ? 1 : 0;
     st = check(cudaMemsetAsync(mem_, 0, total, stream_), "memset", err);
     if (st) return st;
     st = check(cudaMemsetAsync(d_->cell_sys, 0xff, 4 * NC, stream_), "memset", err);
     if (st) return st;
     st = check(cudaMemsetAsync(d_->blk_sys, 0xff, 4 * NCH, stream_), "memset", err);
     if (st) return st;
+    if (clm_) {
+        st = check(cudaMemsetAsync(d_->cblk_sys, 0xff, 4 * NCC, stream_), "memset", err);
+        if (st) return st;
+    }
     hp_.assign(NS, SysParams{});
     slot_rlist_.assign(NS, 0.0);
     free_atoms_.clear();
     free_cells_.clear();
     free_atoms_[0] = NA;
     free_cells_[0] = NC;
+    free_clusters_.clear();
+    if (clm_) free_clusters_[0] = (int64_t)NCL;
     free_tab_.assign(opt.max_types_total, 1);
     slot_tab_size_.assign(NS, 0);
     dirty_map_ = true;
@@ -1303,7 +2050,13 @@ bool Engine::fits(const SlotDesc& d) const {
     }
     int slots = 0;
     for (auto& p : hp_) slots += !p.active;
-    return a && c && slots > 0 && free_tab >= d.n_types * d.n_types;
+    bool cl = true;
+    if (clm_) {
+        const int64_t need = (d.n + clm_ - 1) / clm_ + ncell;
+        cl = false;
+        for (auto& kv : free_clusters_) cl |= kv.second >= need;
+    }
+    return a && c && cl && slots > 0 && free_tab >= d.n_types * d.n_types;
 }
 
 int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* pos, const double* vel,
@@ -1369,6 +2122,16 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
         err = "not enough free cell capacity in the pool";
         return -PIS_ERR_NO_MEMORY;
     }
+    int64_t cl0 = 0, clcap = 0;
+    if (clm_) {
+        clcap = (d.n + clm_ - 1) / clm_ + ncell;
+        if (!take_range(free_clusters_, clcap, cl0)) {
+            give_range(free_atoms_, a0, d.n);
+            give_range(free_cells_, c0, ncell + 1);
+            err = "not enough free cluster capacity in the pool";
+            return -PIS_ERR_NO_MEMORY;
+        }
+    }
     int tab0 = -1;
     {
         int need = nt * nt, run = 0;
@@ -1382,6 +2145,7 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
         if (tab0 < 0) {
             give_range(free_atoms_, a0, d.n);
             give_range(free_cells_, c0, ncell + 1);
+            if (clm_) give_range(free_clusters_, cl0, clcap);
             err = "pair table capacity exhausted";
             return -PIS_ERR_NO_MEMORY;
         }
@@ -1460,6 +2224,10 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     // chunks
     p.nch = (int32_t)((d.n + opt_.blk - 1) / opt_.blk);
     p.ch0 = 0;  // assigned by the block map
+    p.cl0 = (int32_t)cl0;
+    p.clcap = (int32_t)clcap;
+    p.ncch = (int32_t)((clcap + CL_THREADS - 1) / CL_THREADS);
+    p.cch0 = 0;  // assigned by the block map
     hp_[slot] = p;
     slot_rlist_[slot] = rlist;
 
@@ -1519,6 +2287,7 @@ void Engine::remove_slot(int slot) {
     int64_t ncell = (int64_t)p.nc[0] * p.nc[1] * p.nc[2];
     give_range(free_atoms_, p.a0, p.n);
     give_range(free_cells_, p.c0, ncell + 1);
+    if (clm_) give_range(free_clusters_, p.cl0, p.clcap);
     for (int k = 0; k < slot_tab_size_[slot]; ++k) free_tab_[p.tab0 + k] = 1;
     std::vector<int32_t> csys(ncell + 1, -1);
     cudaMemcpyAsync(d_->cell_sys + p.c0, csys.data(), 4 * (ncell + 1), cudaMemcpyHostToDevice, stream_);
@@ -1556,6 +2325,28 @@ pis_status Engine::rebuild_block_map(std::string& err) {
     st = check(cudaMemcpyAsync(d_->blk_first, bf.data(), 4 * max_chunks_, cudaMemcpyHostToDevice, stream_),
                "block map", err);
     if (st) return st;
+    // cluster kernels: every active slot gets ceil(cluster capacity / CL_THREADS) chunks
+    std::vector<int32_t> cbs, cbf;
+    if (clm_) {
+        cbs.assign(max_cchunks_, -1);
+        cbf.assign(max_cchunks_, 0);
+        int64_t q = 0;
+        for (int s = 0; s < opt_.max_slots; ++s) {
+            SysParams& p = hp_[s];
+            if (!p.active) continue;
+            p.cch0 = (int32_t)q;
+            for (int k = 0; k < p.ncch; ++k, ++q) {
+                cbs[q] = s;
+                cbf[q] = p.cl0 + k * CL_THREADS;
+            }
+        }
+        st = check(cudaMemcpyAsync(d_->cblk_sys, cbs.data(), 4 * max_cchunks_, cudaMemcpyHostToDevice, stream_),
+                   "block map", err);
+        if (st) return st;
+        st = check(cudaMemcpyAsync(d_->cblk_first, cbf.data(), 4 * max_cchunks_, cudaMemcpyHostToDevice, stream_),
+                   "block map", err);
+        if (st) return st;
+    }
     st = check(cudaMemcpyAsync(d_->sp, hp_.data(), sizeof(SysParams) * hp_.size(), cudaMemcpyHostToDevice, stream_),
                "params", err);
     if (st) return st;
@@ -1601,34 +2392,37 @@ pis_status Engine::set_steps(int slot, int64_t steps, std::string& err) {
 void Engine::enqueue_rebuild(bool respect) {
     const DP& P = *d_;
     int r = respect ? 1 : 0;
-    LAUNCH(k_bin, (unsigned)max_chunks_, opt_.blk, P, r);
+    const unsigned ga = grid_cap(max_chunks_, 8);
+    LAUNCH(k_bin, ga, opt_.blk, P, r, (int)max_chunks_);
     LAUNCH(k_scan, (unsigned)opt_.max_slots, SCAN_THREADS, P, r);
-    LAUNCH(k_scatter, (unsigned)max_chunks_, opt_.blk, P, r);
+    LAUNCH(k_scatter, ga, opt_.blk, P, r, (int)max_chunks_);
     unsigned gcells = (unsigned)((opt_.max_cells * 32 + 255) / 256);
-    LAUNCH(k_gather, gcells, 256, P, (int64_t)opt_.max_cells, r);
+    LAUNCH(k_gather, grid_cap(gcells, 8), 256, P, (int64_t)opt_.max_cells, r);
     launch_build(r);
 }
 
 // Lanes-per-atom kernels are templates; these dispatch on the pool's runtime choice. Their grid
 // has lpa blocks per chunk.
+// Rebuild kernels stride over `chunks` (times L for lanes-per-atom blocks) on at most `cap` blocks.
 template <int L>
-static void launch_build_t(const DP& P, bool half, unsigned chunks, cudaStream_t st, int r) {
+static void launch_build_t(const DP& P, bool half, unsigned chunks, unsigned cap, cudaStream_t st, int r) {
+    const unsigned n = chunks * L, g = n < cap ? n : cap;
     if (L == 1) {
         // lean kernel for slots with >= 3 cells per axis, generic kernel for the rest
         if (half) {
-            k_build1<true><<<chunks, 256, 0, st>>>(P, r);
-            k_build1_generic<true><<<chunks, 256, 0, st>>>(P, r);
+            k_build1<true><<<g, 256, 0, st>>>(P, r, (int)n);
+            k_build1_generic<true><<<g, 256, 0, st>>>(P, r, (int)n);
         } else {
-            k_build1<false><<<chunks, 256, 0, st>>>(P, r);
-            k_build1_generic<false><<<chunks, 256, 0, st>>>(P, r);
+            k_build1<false><<<g, 256, 0, st>>>(P, r, (int)n);
+            k_build1_generic<false><<<g, 256, 0, st>>>(P, r, (int)n);
         }
         g_launches.fetch_add(2);
         return;
     }
     if (half)
-        k_build<true, L><<<chunks * L, 256, 0, st>>>(P, r);
+        k_build<true, L><<<g, 256, 0, st>>>(P, r, (int)n);
     else
-        k_build<false, L><<<chunks * L, 256, 0, st>>>(P, r);
+        k_build<false, L><<<g, 256, 0, st>>>(P, r, (int)n);
     g_launches.fetch_add(1);
 }
 
@@ -1683,16 +2477,121 @@ static void launch_fp64_t(const DP& P, bool half, bool fast, unsigned chunks, cu
         default: CALL(1); break;    \
     }
 
+template <int ACC, bool ONE, int M>
+static void launch_cluster_t(const DP& P, int batch, unsigned chunks, cudaStream_t st, int r) {
+    if (batch >= 8)
+        k_force_cl<ACC, ONE, M, 8><<<chunks, CL_THREADS, 0, st>>>(P, r);
+    else
+        k_force_cl<ACC, ONE, M, 4><<<chunks, CL_THREADS, 0, st>>>(P, r);
+}
+
+template <int M>
+static void launch_cluster_m(const DP& P, bool kahan, bool one, int batch, unsigned chunks, cudaStream_t st, int r) {
+    if (kahan)
+        one ? launch_cluster_t<1, true, M>(P, batch, chunks, st, r) : launch_cluster_t<1, false, M>(P, batch, chunks, st, r);
+    else
+        one ? launch_cluster_t<0, true, M>(P, batch, chunks, st, r) : launch_cluster_t<0, false, M>(P, batch, chunks, st, r);
+}
+
+// Cluster-list forces: entries per batch = the batch knob (4 or 8).
+void Engine::launch_force_cluster(int r) {
+    const unsigned ch = (unsigned)max_cchunks_;
+    if (opt_.cluster == 2)
+        launch_cluster_m<2>(*d_, opt_.mixed_kahan, single_type_, opt_.mix_batch, ch, stream_, r);
+    else
+        launch_cluster_m<4>(*d_, opt_.mixed_kahan, single_type_, opt_.mix_batch, ch, stream_, r);
+    g_launches.fetch_add(1);
+}
+
 void Engine::launch_build(int r) {
     const unsigned ch = (unsigned)max_chunks_;
+    const int ncc = (int)max_cchunks_;
+    const unsigned gc = grid_cap(max_cchunks_, 16), ga = grid_cap(max_chunks_, 8);
+    if (opt_.cluster) {
+        if (opt_.cluster == 2)
+            k_build_cl<2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, ncc);
+        else
+            k_build_cl<4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, ncc);
+        g_launches.fetch_add(1);
+        return;
+    }
+    if (clm_ && opt_.lpa == 1) {
+        // per-atom lists scanned per cluster; slots with a two-cell axis use the generic kernel
+        if (half_) {
+            if (clm_ == 2)
+                k_build1_cl<true, 2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, ncc);
+            else
+                k_build1_cl<true, 4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, ncc);
+            k_build1_generic<true><<<ga, 256, 0, stream_>>>(*d_, r, (int)ch);
+        } else {
+            if (clm_ == 2)
+                k_build1_cl<false, 2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, ncc);
+            else
+                k_build1_cl<false, 4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, ncc);
+            k_build1_generic<false><<<ga, 256, 0, stream_>>>(*d_, r, (int)ch);
+        }
+        g_launches.fetch_add(2);
+        return;
+    }
+    const unsigned capb = (unsigned)(8 * num_sms_);
 
-#define PIS_CALL(L) launch_build_t<L>(*d_, half_, ch, stream_, r)
+#define PIS_CALL(L) launch_build_t<L>(*d_, half_, ch, capb, stream_, r)
     PIS_LPA_DISPATCH(opt_.lpa, PIS_CALL)
 #undef PIS_CALL
 }
 
+template <int ACC, bool ONE, int KB>
+static void launch_mixed_tma_t(const DP& P, unsigned chunks, cudaStream_t st, int r) {
+    k_force_mixed_tma<ACC, ONE, KB><<<chunks, 256, mix_tma_smem_bytes<KB>(), st>>>(P, r);
+}
+
+// Bulk-copy-fed variant: rows per stage = the batch knob (8 or 16).
+static void launch_mixed_tma(const DP& P, bool kahan, bool one, int batch, unsigned chunks, cudaStream_t st, int r) {
+    const bool b16 = batch == 16;
+    if (kahan) {
+        if (one)
+            b16 ? launch_mixed_tma_t<1, true, 16>(P, chunks, st, r) : launch_mixed_tma_t<1, true, 8>(P, chunks, st, r);
+        else
+            b16 ? launch_mixed_tma_t<1, false, 16>(P, chunks, st, r) : launch_mixed_tma_t<1, false, 8>(P, chunks, st, r);
+    } else {
+        if (one)
+            b16 ? launch_mixed_tma_t<0, true, 16>(P, chunks, st, r) : launch_mixed_tma_t<0, true, 8>(P, chunks, st, r);
+        else
+            b16 ? launch_mixed_tma_t<0, false, 16>(P, chunks, st, r) : launch_mixed_tma_t<0, false, 8>(P, chunks, st, r);
+    }
+    g_launches.fetch_add(1);
+}
+
+// Dynamic shared memory of the bulk-copy-fed kernels (the 16-row ring exceeds the 48 KB default).
+template <int ACC, bool ONE, int KB>
+static cudaError_t allow_mixed_tma_smem() {
+    return cudaFuncSetAttribute(k_force_mixed_tma<ACC, ONE, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)mix_tma_smem_bytes<KB>());
+}
+
+static cudaError_t allow_all_mixed_tma_smem() {
+    cudaError_t e = cudaSuccess, q;
+    if ((q = allow_mixed_tma_smem<0, true, 8>()) != cudaSuccess) e = q;
+    if ((q = allow_mixed_tma_smem<0, true, 16>()) != cudaSuccess) e = q;
+    if ((q = allow_mixed_tma_smem<0, false, 8>()) != cudaSuccess) e = q;
+    if ((q = allow_mixed_tma_smem<0, false, 16>()) != cudaSuccess) e = q;
+    if ((q = allow_mixed_tma_smem<1, true, 8>()) != cudaSuccess) e = q;
+    if ((q = allow_mixed_tma_smem<1, true, 16>()) != cudaSuccess) e = q;
+    if ((q = allow_mixed_tma_smem<1, false, 8>()) != cudaSuccess) e = q;
+    if ((q = allow_mixed_tma_smem<1, false, 16>()) != cudaSuccess) e = q;
+    return e;
+}
+
 void Engine::launch_force_mixed(int r) {
     const unsigned ch = (unsigned)max_chunks_;
+    if (opt_.cluster) {
+        launch_force_cluster(r);
+        return;
+    }
+    if (opt_.list_tma && opt_.lpa == 1) {
+        launch_mixed_tma(*d_, opt_.mixed_kahan, single_type_, opt_.mix_batch, ch, stream_, r);
+        return;
+    }
 #define PIS_CALL(L) launch_mixed_t<L>(*d_, opt_.mixed_kahan, single_type_, opt_.mix_batch, ch, stream_, r)
     PIS_LPA_DISPATCH(opt_.lpa, PIS_CALL)
 #undef PIS_CALL
@@ -1910,6 +2809,20 @@ pis_status Engine::read_pe_history(int slot, int64_t n, double* out, std::string
 
 pis_status Engine::list_entries(int slot, int64_t& total, std::string& err) {
     const SysParams& p = hp_[slot];
+    if (opt_.cluster) {
+        SysState ss;
+        pis_status st = read_state(slot, ss, err);
+        if (st) return st;
+        std::vector<int32_t> nn(ss.ncl);
+        st = check(cudaMemcpyAsync(nn.data(), d_->cl_nn + p.cl0, 4 * (size_t)ss.ncl, cudaMemcpyDeviceToHost, stream_),
+                   "nn", err);
+        if (st) return st;
+        st = sync(err);
+        if (st) return st;
+        total = 0;
+        for (int32_t v : nn) total += v;
+        return PIS_OK;
+    }
     std::vector<int32_t> nn(p.n);
     pis_status st = check(cudaMemcpyAsync(nn.data(), d_->nn + p.a0, 4 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "nn", err);
     if (st) return st;
@@ -1926,6 +2839,7 @@ pis_status Engine::neighbour_sets(int slot, std::vector<int64_t>& offsets, std::
     SysState ss;
     pis_status st = read_state(slot, ss, err);
     if (st) return st;
+    if (opt_.cluster) return neighbour_sets_cluster(slot, ss, offsets, idx, err);
     if (!d_->keep) {
         st = check(cudaMalloc(&d_->keep, (size_t)npad_ * cap_), "keep mask", err);
         if (st) return st;
@@ -1969,6 +2883,65 @@ pis_status Engine::neighbour_sets(int slot, std::vector<int64_t>& offsets, std::
     idx.clear();
     for (int i = 0; i < p.n; ++i) {
         std::sort(sets[i].begin(), sets[i].end());
+        idx.insert(idx.end(), sets[i].begin(), sets[i].end());
+        offsets[i + 1] = (int64_t)idx.size();
+    }
+    return PIS_OK;
+}
+
+// Per-atom sets from the cluster lists: every (member, entry) pair that passes the exact cutoff
+// test, in original indices, sorted; an atom listed under two images (two-cell axes) counts once.
+pis_status Engine::neighbour_sets_cluster(int slot, const SysState& ss, std::vector<int64_t>& offsets,
+                                          std::vector<int32_t>& idx, std::string& err) {
+    const SysParams& p = hp_[slot];
+    pis_status st;
+    if (!d_->keep) {
+        st = check(cudaMalloc(&d_->keep, (size_t)clpad_ * ccap_), "keep mask", err);
+        if (st) return st;
+    }
+    LAUNCH(k_keep_cl, (unsigned)max_cchunks_, CL_THREADS, *d_, slot);
+    st = check(cudaGetLastError(), "keep", err);
+    if (st) return st;
+    const size_t ncl = (size_t)ss.ncl;
+    std::vector<int32_t> atom(ncl), nn(ncl), id(p.n);
+    st = check(cudaMemcpyAsync(atom.data(), d_->cl_atom + p.cl0, 4 * ncl, cudaMemcpyDeviceToHost, stream_), "clusters", err);
+    if (st) return st;
+    st = check(cudaMemcpyAsync(nn.data(), d_->cl_nn + p.cl0, 4 * ncl, cudaMemcpyDeviceToHost, stream_), "nn", err);
+    if (st) return st;
+    st = check(cudaMemcpyAsync(id.data(), d_->id[ss.cur] + p.a0, 4 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "id", err);
+    if (st) return st;
+    st = sync(err);
+    if (st) return st;
+    int32_t maxnn = 0;
+    for (int32_t v : nn) maxnn = std::max(maxnn, v);
+    std::vector<uint32_t> ent((size_t)maxnn * ncl);
+    std::vector<uint8_t> kp((size_t)maxnn * ncl);
+    for (int r = 0; r < maxnn; ++r) {
+        const int64_t off = (int64_t)r * clpad_ + p.cl0;
+        st = check(cudaMemcpyAsync(ent.data() + r * ncl, d_->cl_nbr + off, 4 * ncl, cudaMemcpyDeviceToHost, stream_), "nbr", err);
+        if (st) return st;
+        st = check(cudaMemcpyAsync(kp.data() + r * ncl, d_->keep + off, ncl, cudaMemcpyDeviceToHost, stream_), "keep", err);
+        if (st) return st;
+    }
+    st = sync(err);
+    if (st) return st;
+    std::vector<std::vector<int32_t>> sets(p.n);
+    for (size_t c = 0; c < ncl; ++c) {
+        const uint32_t pk = (uint32_t)atom[c];
+        const int first = (int)(pk & JMASK) - (int)p.a0, n = (int)(pk >> JBITS) + 1;
+        for (int k = 0; k < nn[c]; ++k) {
+            const uint8_t mask = kp[(size_t)k * ncl + c];
+            if (!mask) continue;
+            const int j = (int)(ent[(size_t)k * ncl + c] & JMASK) - (int)p.a0;
+            for (int m = 0; m < n; ++m)
+                if (mask & (1u << m)) sets[id[first + m]].push_back(id[j]);
+        }
+    }
+    offsets.assign(p.n + 1, 0);
+    idx.clear();
+    for (int i = 0; i < p.n; ++i) {
+        std::sort(sets[i].begin(), sets[i].end());
+        sets[i].erase(std::unique(sets[i].begin(), sets[i].end()), sets[i].end());
         idx.insert(idx.end(), sets[i].begin(), sets[i].end());
         offsets[i + 1] = (int64_t)idx.size();
     }

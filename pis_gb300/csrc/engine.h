@@ -48,6 +48,8 @@ struct SysParams {
     int32_t nc[3];     // cells per axis
     int32_t pbc[3];
     int32_t ch0, nch;  // chunk range of the slot
+    int32_t cl0, clcap;  // cluster-list path: first cluster entry of the slot and its capacity
+    int32_t cch0, ncch;  // cluster-list path: chunk range of the slot's cluster kernels
     double h[3];       // diagonal of h
     double hinv[3];    // diagonal of h^-1 (adjugate / determinant, as the reference)
     double cs[3];      // cell edge
@@ -72,7 +74,7 @@ struct SysState {
     int32_t flags;        // FLAG_* bits
     int32_t want_virial;  // compute sum_i r_i F_i^T in the next reductions
     int32_t eval;         // slot takes part in the next host-requested evaluation / reduction
-    int32_t pad_;
+    int32_t ncl;          // clusters of the current build (cluster-list path)
     int64_t steps_left;   // steps still to take; a slot at 0 is frozen during run()
     int64_t steps_done;
     int64_t rebuilds;
@@ -80,7 +82,7 @@ struct SysState {
     double virial[9];
 };
 
-enum : int32_t { FLAG_NAN = 1, FLAG_LIST_OVERFLOW = 2, FLAG_CELL_OVERFLOW = 4 };
+enum : int32_t { FLAG_NAN = 1, FLAG_LIST_OVERFLOW = 2, FLAG_CELL_OVERFLOW = 4, FLAG_TIMEOUT = 8 };
 
 struct PoolOptions {
     int precision = PIS_PRECISION_FP64;
@@ -96,6 +98,10 @@ struct PoolOptions {
     bool mixed_kahan = false;  // mixed force kernel with compensated FP32 sums (variant)
     int lpa = 1;               // lanes per atom in the list build and force kernels (1,4,8,16,32)
     int mix_batch = 4;         // list entries per gather batch in the mixed force kernel (4, 8, 16)
+    bool list_tma = false;     // mixed, thread per atom: list rows streamed to shared memory by bulk copies
+    int cluster = 0;           // mixed: atoms per cluster of the cluster-list kernels (2 or 4); 0 = per-atom list
+    int build_cluster = 0;     // per-atom list, thread per atom: build scans candidates per cluster of this
+                               // many atoms (2 or 4; 0 or 1 = per atom)
 };
 
 class Engine {
@@ -112,7 +118,8 @@ class Engine {
     void remove_slot(int slot);
     // Ask whether a system of this shape fits in the free space right now.
     bool fits(const SlotDesc& d) const;
-    int64_t list_cap() const { return cap_; }
+    int64_t list_cap() const { return opt_.cluster ? ccap_ : cap_; }
+    int cluster_size() const { return opt_.cluster; }
     int precision() const { return opt_.precision; }
     bool half_list() const { return half_; }
 
@@ -164,19 +171,26 @@ class Engine {
     void launch_force_fp64(int respect_steps);
     void launch_force_mixed(int respect_steps);
     void launch_build(int respect_steps);
+    void launch_force_cluster(int respect_steps);
     pis_status check(cudaError_t e, const char* what, std::string& err);
+    pis_status neighbour_sets_cluster(int slot, const SysState& ss, std::vector<int64_t>& offsets,
+                                      std::vector<int32_t>& idx, std::string& err);
 
     PoolOptions opt_;
     bool half_ = true;
     int64_t cap_ = 0;
     int64_t npad_ = 0;
     int64_t max_chunks_ = 0;
+    int64_t max_clusters_ = 0, clpad_ = 0, ccap_ = 0, max_cchunks_ = 0;
+    int clm_ = 0;  // atoms per cluster of the cluster table (0: no table)
+    int num_sms_ = 1;
+    unsigned grid_cap(int64_t chunks, int per_sm) const;
     cudaStream_t stream_ = nullptr;
     std::vector<SysParams> hp_;
     std::vector<int> slot_tab_size_;
     std::vector<double> slot_rlist_;
     // free-space bookkeeping (first fit over atom and cell index ranges)
-    std::map<int64_t, int64_t> free_atoms_, free_cells_;
+    std::map<int64_t, int64_t> free_atoms_, free_cells_, free_clusters_;
     std::vector<int> free_tab_;
     // device allocations
     void* mem_ = nullptr;

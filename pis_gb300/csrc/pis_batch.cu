@@ -147,6 +147,10 @@ pis_status pis_batch_create(int64_t max_atoms, int32_t max_slots, int64_t max_ce
     b->opt.lpa = lanes ? lanes : 1;
     const int batch = (flags >> 16) & 0xff;
     b->opt.mix_batch = batch ? batch : 4;
+    b->opt.list_tma = (flags & PIS_OPT_LIST_TMA) != 0;
+    const int cl = (flags >> 24) & 0xf;
+    b->opt.cluster = cl > 1 ? cl : 0;
+    b->opt.build_cluster = (flags >> 28) & 0x7;
     b->opt.list_cap = 224;  // density up to 0.95 at rc + skin = 2.8 (expected ~88 full-list entries)
     b->opt.hist = 1024;
     std::string err;
@@ -270,6 +274,7 @@ pis_status pis_batch_result(pis_batch* b, int32_t slot, double* pos, double* vel
     if (steps_done) *steps_done = ss.steps_done;
     if (ss.flags & pis::FLAG_NAN) return bfail(b, PIS_ERR_NAN_DETECTED, "NaN detected in this slot");
     if (ss.flags & pis::FLAG_LIST_OVERFLOW) return bfail(b, PIS_ERR_LIST_OVERFLOW, "neighbour list overflow");
+    if (ss.flags & pis::FLAG_TIMEOUT) return bfail(b, PIS_ERR_TIMEOUT, "a device-side wait expired in this slot");
     return PIS_OK;
 }
 

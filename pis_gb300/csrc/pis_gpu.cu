@@ -22,6 +22,9 @@ struct pis_gpu_ctx {
     bool mixed_kahan = false;
     int lpa = 1;
     int mix_batch = 4;
+    bool list_tma = false;
+    int cluster = 0;
+    int build_cluster = 0;
     std::unique_ptr<pis::Engine> eng;
     int slot = -1;
     int64_t n = 0;
@@ -52,6 +55,8 @@ pis_status flags_to_status(pis_gpu_ctx* ctx, const pis::SysState& ss) {
     if (ss.flags & pis::FLAG_NAN) return fail(ctx, PIS_ERR_NAN_DETECTED, "NaN detected in positions or energies");
     if (ss.flags & pis::FLAG_LIST_OVERFLOW)
         return fail(ctx, PIS_ERR_LIST_OVERFLOW, "neighbour list capacity exceeded; results are invalid");
+    if (ss.flags & pis::FLAG_TIMEOUT)
+        return fail(ctx, PIS_ERR_TIMEOUT, "a device-side wait expired; results are invalid");
     return PIS_OK;
 }
 
@@ -96,7 +101,8 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
     if (!ctx) return PIS_ERR_INVALID_ARGUMENT;
     if (list_kind < PIS_LIST_DEFAULT || list_kind > PIS_LIST_FULL)
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown list kind");
-    if (flags & ~(PIS_OPT_FP64_FAST | PIS_OPT_MIXED_KAHAN | PIS_OPT_LANES(0xff) | PIS_OPT_BATCH(0xff)))
+    if (flags & ~(PIS_OPT_FP64_FAST | PIS_OPT_MIXED_KAHAN | PIS_OPT_LIST_TMA | PIS_OPT_LANES(0xff) | PIS_OPT_BATCH(0xff) |
+                  PIS_OPT_CLUSTER(0xf) | PIS_OPT_SCAN(0x7)))
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown option flag");
     const int batch = (flags >> 16) & 0xff;
     if (batch != 0 && batch != 4 && batch != 8 && batch != 16)
@@ -108,6 +114,18 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
     ctx->lpa = lanes ? lanes : 1;
     ctx->fp64_fast = (flags & PIS_OPT_FP64_FAST) != 0;
     ctx->mixed_kahan = (flags & PIS_OPT_MIXED_KAHAN) != 0;
+    ctx->list_tma = (flags & PIS_OPT_LIST_TMA) != 0;
+    const int cl = (flags >> 24) & 0xf;
+    if (cl > 1 && cl != 2 && cl != 4) return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "atoms per cluster must be 1, 2 or 4");
+    ctx->cluster = cl > 1 ? cl : 0;
+    const int scan = (flags >> 28) & 0x7;
+    if (scan != 0 && scan != 1 && scan != 2 && scan != 4)
+        return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "atoms per build cluster must be 1, 2 or 4");
+    ctx->build_cluster = scan;
+    if (ctx->cluster && (ctx->precision != PIS_PRECISION_MIXED || ctx->lpa != 1 || ctx->list_tma))
+        return fail(ctx, PIS_ERR_UNSUPPORTED, "the cluster list needs the mixed path, one thread per cluster");
+    if (ctx->list_tma && (ctx->precision != PIS_PRECISION_MIXED || ctx->lpa != 1))
+        return fail(ctx, PIS_ERR_UNSUPPORTED, "the bulk-copy list stream needs the mixed path, thread per atom");
     if (ctx->precision == PIS_PRECISION_MIXED && list_kind == PIS_LIST_HALF)
         return fail(ctx, PIS_ERR_UNSUPPORTED, "the mixed-precision path uses a full list");
     ctx->list_kind = list_kind;
@@ -147,6 +165,9 @@ pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_id
     opt.mixed_kahan = ctx->mixed_kahan;
     opt.lpa = ctx->lpa;
     opt.mix_batch = ctx->mix_batch;
+    opt.list_tma = ctx->list_tma;
+    opt.cluster = ctx->cluster;
+    opt.build_cluster = ctx->build_cluster;
     opt.max_atoms = n;
     opt.max_slots = 1;
     int64_t ncell = 1;
