@@ -2,7 +2,9 @@
 
 The measured knobs are the ones the C ABI exposes as variants: lanes per atom in the list build
 and force kernels (PIS_OPT_LANES), list entries per gather batch in the mixed force kernel
-(PIS_OPT_BATCH), and FP64 batch sums versus compensated FP32 sums (PIS_OPT_MIXED_KAHAN). For a
+(PIS_OPT_BATCH), FP64 batch sums versus compensated FP32 sums (PIS_OPT_MIXED_KAHAN), the list
+streamed into shared memory by bulk copies (PIS_OPT_LIST_TMA), cluster lists (PIS_OPT_CLUSTER)
+and the cluster-scanned per-atom list build (PIS_OPT_SCAN). For a
 given workload the tuner times a short run of every candidate on the real system (CUDA events on
 the engine's stream) and keeps the fastest. Results are cached in a JSON file keyed by GPU name,
 precision and size class (atoms per system rounded to a power of two), so a workload is tuned
@@ -22,10 +24,11 @@ CACHE = os.path.join(OUT_DIR, "autotune.json")
 MIXED_CANDIDATES = [
     {"lanes": 1, "batch": 4, "mixed_kahan": False},
     {"lanes": 1, "batch": 8, "mixed_kahan": False},
-    {"lanes": 1, "batch": 16, "mixed_kahan": False},
-    {"lanes": 1, "batch": 8, "mixed_kahan": True},
     {"lanes": 1, "batch": 4, "mixed_kahan": True},
-    {"lanes": 4, "batch": 0, "mixed_kahan": True},
+    {"lanes": 1, "batch": 8, "mixed_kahan": True},
+    {"lanes": 1, "batch": 4, "mixed_kahan": True, "scan": 4},
+    {"lanes": 1, "batch": 8, "mixed_kahan": True, "tma": True},
+    {"lanes": 1, "batch": 4, "mixed_kahan": True, "cluster": 4},
 ]
 FP64_CANDIDATES = [
     {"lanes": 1, "fp64_fast": False},

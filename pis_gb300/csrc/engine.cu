@@ -144,6 +144,14 @@ __device__ __forceinline__ bool lj_fp64(const LJ64& P, double r2, double& u, dou
     return true;
 }
 
+// A neighbour-list word: read once per evaluation, so it is not kept in L1, which is left to the
+// neighbour-position gathers (1 % faster force kernel on the 2.048M-atom liquid).
+__device__ __forceinline__ uint32_t load_list_word(const uint32_t* p) {
+    uint32_t v;
+    asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
 // Single hardware reciprocal approximation (rcp.approx.ftz.f32); ~1 ulp, flushes denormals.
 __device__ __forceinline__ float rcp_approx(float x) {
     float y;
@@ -242,11 +250,19 @@ __device__ __forceinline__ bool group_atom_of(const DP& P, int& s, int& i) {
     return group_atom_of_blk<LPA>(P, blockIdx.x, s, i);
 }
 
-// The neighbour-list rebuild kernels run on a grid capped at a whole number of waves and stride
-// over their chunks. Their first test is the device-wide "some slot rebuilds this step" word, so
-// on the ~9 steps in 10 without a rebuild each costs one short wave rather than a full grid.
-__device__ __forceinline__ bool rebuild_pending(const DP& P) { return *(volatile const int32_t*)P.ctl != 0; }
-#define PIS_FOR_CHUNKS(n) for (int blk = blockIdx.x; blk < (n); blk += gridDim.x)
+// The neighbour-list rebuild kernels' first test is the device-wide "some slot rebuilds this
+// step" word, so on the ~9 steps in 10 without a rebuild every block exits after one cached load.
+// They run one block per chunk (one warp per cell for the gather): the hardware balances the
+// rebuilding chunks dynamically (a grid capped at a fixed number of blocks per SM, striding over
+// chunks, left multi-wave tails and was measured slower).
+__device__ __forceinline__ bool rebuild_pending(const DP& P) { return P.ctl[0] != 0; }
+// The request word and the block's first table entry (its slot, or a cell's slot) are loaded
+// together, so both the early exit and a rebuilding block pay one memory latency for them.
+__device__ __forceinline__ bool rebuild_block(const DP& P, const int32_t* slot_table, int64_t idx) {
+    const int pending = P.ctl[0];
+    const int s = slot_table[idx];
+    return pending != 0 && s >= 0;
+}
 
 // Neighbour-list layout: entry k of atom i lives at (k / LPA) * (npad * LPA) + i * LPA + k % LPA.
 // The LPA lanes of one atom read or write one contiguous run of LPA words, and consecutive atoms'
@@ -366,9 +382,9 @@ __device__ __forceinline__ void bin_chunk(const DP& P, int blk, int respect_step
     P.lcell[i] = lc;
     P.slotin[i] = atomicAdd(&P.cell_count[sp.c0 + lc], 1);
 }
-__global__ void k_bin(const DP P, int respect_steps, int nblk) {
-    if (!rebuild_pending(P)) return;
-    PIS_FOR_CHUNKS(nblk) bin_chunk(P, blk, respect_steps);
+__global__ void k_bin(const DP P, int respect_steps) {
+    if (!rebuild_block(P, P.blk_sys, blockIdx.x)) return;
+    bin_chunk(P, blockIdx.x, respect_steps);
 }
 
 // One exclusive scan over a slot's cells: of the atom counts (CL = 0, the last pass, which also
@@ -474,9 +490,9 @@ __device__ __forceinline__ void scatter_chunk(const DP& P, int blk, int respect_
     int dst = P.cell_start[sp.c0 + P.lcell[i]] + P.slotin[i];
     P.perm[dst] = i;
 }
-__global__ void k_scatter(const DP P, int respect_steps, int nblk) {
-    if (!rebuild_pending(P)) return;
-    PIS_FOR_CHUNKS(nblk) scatter_chunk(P, blk, respect_steps);
+__global__ void k_scatter(const DP P, int respect_steps) {
+    if (!rebuild_block(P, P.blk_sys, blockIdx.x)) return;
+    scatter_chunk(P, blockIdx.x, respect_steps);
 }
 
 // Order key of an atom inside its cell: the Morton index of its sub-cell on a 4 x 4 x 4 grid over
@@ -487,10 +503,10 @@ __global__ void k_scatter(const DP P, int respect_steps, int nblk) {
 // on the physical state, never on atomics.
 __device__ __forceinline__ uint32_t cell_order_key(const SysParams& sp, const float4& q, uint32_t id) {
     uint32_t b[3];
-    const float r[3] = {q.x / sp.fcs[0], q.y / sp.fcs[1], q.z / sp.fcs[2]};
+    const float r[3] = {q.x, q.y, q.z};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const int v = __float2int_rd((r[d] + 0.5f) * 4.0f);
+        const int v = __float2int_rd(fmaf(r[d], sp.fsub[d], 2.0f));
         b[d] = (uint32_t)(v < 0 ? 0 : (v > 3 ? 3 : v));
     }
     const uint32_t m = (b[0] & 1u) | ((b[1] & 1u) << 1) | ((b[2] & 1u) << 2) | ((b[0] >> 1) << 3) |
@@ -500,7 +516,9 @@ __device__ __forceinline__ uint32_t cell_order_key(const SysParams& sp, const fl
 
 // One warp per cell: order the cell's atoms by cell_order_key, then move every per-atom array into
 // the new buffer set and record the build snapshot and cell-relative coordinates.
-__device__ __forceinline__ void gather_cell(const DP& P, int64_t g, int respect_steps) {
+constexpr int GATHER_SMEM_KEYS = 256;  // per warp: order keys of cells of 65..256 atoms
+
+__device__ __forceinline__ void gather_cell(const DP& P, int64_t g, int respect_steps, uint32_t* kb) {
     int lane = threadIdx.x & 31;
     int s = P.cell_sys[g];
     if (s < 0) return;
@@ -514,14 +532,15 @@ __device__ __forceinline__ void gather_cell(const DP& P, int64_t g, int respect_
     const int beg = P.cell_start[g], end = P.cell_start[g + 1];
     const int cnt = end - beg;
     // rank of every member by its order key: keys held in lane registers for cells of up to 64
-    // atoms (one or two per lane), compared through warp shuffles; larger cells recompute keys
+    // atoms (one or two per lane), compared through warp shuffles; cells of up to 256 atoms (small
+    // boxes have few, large cells) keep their keys in the warp's shared-memory buffer; larger
+    // cells recompute keys
     auto key_of = [&](int src) {
         const double4_32a p = P.pos[src_set][src];
         return cell_order_key(sp, cell_relative(sp, p, lc, 0), (uint32_t)P.id[src_set][src]);
     };
     int rk[2] = {0, 0}, srcs[2] = {-1, -1};
     uint32_t keys[2] = {0xffffffffu, 0xffffffffu};
-    double4_32a ps[2];
     float4 qs[2];
     if (cnt <= 64) {
 #pragma unroll
@@ -529,8 +548,8 @@ __device__ __forceinline__ void gather_cell(const DP& P, int64_t g, int respect_
             const int k = lane + 32 * h;
             if (k < cnt) {
                 srcs[h] = P.perm[beg + k];
-                ps[h] = P.pos[src_set][srcs[h]];
-                qs[h] = cell_relative(sp, ps[h], lc, type_of(ps[h].w));
+                const double4_32a p = P.pos[src_set][srcs[h]];
+                qs[h] = cell_relative(sp, p, lc, type_of(p.w));
                 keys[h] = cell_order_key(sp, qs[h], (uint32_t)P.id[src_set][srcs[h]]);
             }
         }
@@ -545,6 +564,9 @@ __device__ __forceinline__ void gather_cell(const DP& P, int64_t g, int respect_
             rk[0] += v < keys[0];
             rk[1] += v < keys[1];
         }
+    } else if (cnt <= GATHER_SMEM_KEYS) {
+        for (int k = lane; k < cnt; k += 32) kb[k] = key_of(P.perm[beg + k]);
+        __syncwarp();
     }
     for (int k = lane; k < cnt; k += 32) {
         int src, rank = 0;
@@ -554,8 +576,14 @@ __device__ __forceinline__ void gather_cell(const DP& P, int64_t g, int respect_
             const bool hi = k >= 32;
             src = hi ? srcs[1] : srcs[0];
             rank = hi ? rk[1] : rk[0];
-            p = hi ? ps[1] : ps[0];
+            p = P.pos[src_set][src];
             q = hi ? qs[1] : qs[0];
+        } else if (cnt <= GATHER_SMEM_KEYS) {
+            src = P.perm[beg + k];
+            const uint32_t mine = kb[k];
+            for (int r = 0; r < cnt; ++r) rank += kb[r] < mine;
+            p = P.pos[src_set][src];
+            q = cell_relative(sp, p, lc, type_of(p.w));
         } else {
             src = P.perm[beg + k];
             const uint32_t mine = key_of(src);
@@ -585,10 +613,9 @@ __device__ __forceinline__ void gather_cell(const DP& P, int64_t g, int respect_
     }
 }
 __global__ void k_gather(const DP P, int64_t max_cells, int respect_steps) {
-    if (!rebuild_pending(P)) return;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < max_cells; g += nw)
-        gather_cell(P, g, respect_steps);
+    __shared__ uint32_t keybuf[256 / 32][GATHER_SMEM_KEYS];
+    const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (g < max_cells && rebuild_block(P, P.cell_sys, g)) gather_cell(P, g, respect_steps, keybuf[threadIdx.x >> 5]);
 }
 
 // Neighbour-list build at rcut + skin. LPA lanes share one home atom (atoms in cell order, so
@@ -711,15 +738,14 @@ __device__ __forceinline__ void k_build_body(const DP& P, int blk, int step_mode
 }
 
 template <bool HALF, int LPA>
-__global__ void __launch_bounds__(256) k_build(const DP P, int step_mode, int nblk) {
-    if (!rebuild_pending(P)) return;
-    PIS_FOR_CHUNKS(nblk) k_build_body<HALF, LPA>(P, blk, step_mode);
+__global__ void __launch_bounds__(256) k_build(const DP P, int step_mode) {
+    if (!rebuild_block(P, P.blk_sys, blockIdx.x / LPA)) return;
+    k_build_body<HALF, LPA>(P, blockIdx.x, step_mode);
 }
 
 // Thread-per-atom list build (the default shape). Same contents and order as k_build<HALF, 1>;
-// the inner loop is kept minimal: the home cell (the only one holding i) is walked separately,
-// the capacity test is hoisted to once per neighbour cell when the cell cannot overflow the row,
-// and cells whose nearest face is beyond the list radius for this atom are skipped.
+// cells whose nearest face is beyond the list radius for this atom are skipped.
+//
 template <bool HALF>
 __device__ __forceinline__ void scan_cell(const float4* __restrict__ pp, int j, int jend, float sx, float sy,
                                           float sz, float rl2, uint32_t codebits, int i, bool home,
@@ -740,7 +766,6 @@ __device__ __forceinline__ void scan_cell(const float4* __restrict__ pp, int j, 
         }
     }
 }
-
 template <bool HALF>
 __device__ __forceinline__ void build1_chunk(const DP& P, int blk, int step_mode) {
     int s, i;
@@ -791,22 +816,19 @@ __device__ __forceinline__ void build1_chunk(const DP& P, int blk, int step_mode
     P.nn[i] = cnt > cap ? cap : cnt;
 }
 template <bool HALF>
-__global__ void __launch_bounds__(256) k_build1(const DP P, int step_mode, int nblk) {
-    if (!rebuild_pending(P)) return;
-    PIS_FOR_CHUNKS(nblk) build1_chunk<HALF>(P, blk, step_mode);
+__global__ void __launch_bounds__(256) k_build1(const DP P, int step_mode) {
+    if (!rebuild_block(P, P.blk_sys, blockIdx.x)) return;
+    build1_chunk<HALF>(P, blockIdx.x, step_mode);
 }
 
 // Slots with a two-cell axis: the group kernel's generic path, one lane per atom.
 template <bool HALF>
-__global__ void __launch_bounds__(256) k_build1_generic(const DP P, int step_mode, int nblk) {
-    if (!rebuild_pending(P)) return;
-    PIS_FOR_CHUNKS(nblk) {
-        const int s = P.blk_sys[blk];
-        if (s < 0) continue;
-        const SysParams& sp = P.sp[s];
-        if (sp.nc[0] >= 3 && sp.nc[1] >= 3 && sp.nc[2] >= 3) continue;
-        k_build_body<HALF, 1>(P, blk, step_mode);
-    }
+__global__ void __launch_bounds__(256) k_build1_generic(const DP P, int step_mode) {
+    if (!rebuild_block(P, P.blk_sys, blockIdx.x)) return;
+    const int s = P.blk_sys[blockIdx.x];
+    const SysParams& sp = P.sp[s];
+    if (sp.nc[0] >= 3 && sp.nc[1] >= 3 && sp.nc[2] >= 3) return;
+    k_build_body<HALF, 1>(P, blockIdx.x, step_mode);
 }
 
 // FP64 forces: the pair evaluation of LJVOffsetManager (src/potentials/lennard_jones.rs:214-235),
@@ -1085,11 +1107,11 @@ __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) 
             uint32_t ent[MIX_BATCH];
             if (k0 + LPA * MIX_BATCH <= nn) {
 #pragma unroll
-                for (int b = 0; b < MIX_BATCH; ++b) ent[b] = __ldg(nbp + qoff + (uint32_t)b * row32);
+                for (int b = 0; b < MIX_BATCH; ++b) ent[b] = load_list_word(nbp + qoff + (uint32_t)b * row32);
             } else {
 #pragma unroll
                 for (int b = 0; b < MIX_BATCH; ++b)
-                    ent[b] = (k0 + b * LPA + gl < nn) ? __ldg(nbp + qoff + (uint32_t)b * row32) : pad;
+                    ent[b] = (k0 + b * LPA + gl < nn) ? load_list_word(nbp + qoff + (uint32_t)b * row32) : pad;
             }
             qoff += (uint32_t)MIX_BATCH * row32;
             mixed_pairs<ONE, MIX_BATCH, ACC>(ent, prel, pi, shift, tab, P0, acc);
@@ -1338,9 +1360,9 @@ __device__ __forceinline__ void build_cl_chunk(const DP& P, int blk, int step_mo
     P.cl_nn[c] = cnt > cap ? cap : cnt;
 }
 template <int M>
-__global__ void __launch_bounds__(CL_THREADS) k_build_cl(const DP P, int step_mode, int nblk) {
-    if (!rebuild_pending(P)) return;
-    PIS_FOR_CHUNKS(nblk) build_cl_chunk<M>(P, blk, step_mode);
+__global__ void __launch_bounds__(CL_THREADS) k_build_cl(const DP P, int step_mode) {
+    if (!rebuild_block(P, P.cblk_sys, blockIdx.x)) return;
+    build_cl_chunk<M>(P, blockIdx.x, step_mode);
 }
 
 // Per-atom lists built per cluster (the default build of the thread-per-atom layout): one thread
@@ -1441,9 +1463,9 @@ __device__ __forceinline__ void build1_cl_chunk(const DP& P, int blk, int step_m
     }
 }
 template <bool HALF, int M>
-__global__ void __launch_bounds__(CL_THREADS) k_build1_cl(const DP P, int step_mode, int nblk) {
-    if (!rebuild_pending(P)) return;
-    PIS_FOR_CHUNKS(nblk) build1_cl_chunk<HALF, M>(P, blk, step_mode);
+__global__ void __launch_bounds__(CL_THREADS) k_build1_cl(const DP P, int step_mode) {
+    if (!rebuild_block(P, P.cblk_sys, blockIdx.x)) return;
+    build1_cl_chunk<HALF, M>(P, blockIdx.x, step_mode);
 }
 
 // Forces: thread per cluster. For each batch of NB list entries the words are loaded, then the
@@ -1819,12 +1841,7 @@ pis_status Engine::check(cudaError_t e, const char* what, std::string& err) {
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-// Grid of a strided rebuild kernel: its chunk count, capped at `per_sm` blocks per SM (one wave
-// of full occupancy for the block size used).
-unsigned Engine::grid_cap(int64_t chunks, int per_sm) const {
-    const int64_t cap = (int64_t)per_sm * num_sms_;
-    return (unsigned)(chunks < cap ? chunks : cap);
-}
+
 static cudaError_t allow_all_mixed_tma_smem();
 
 pis_status Engine::init(const PoolOptions& opt, std::string& err) {
@@ -2215,6 +2232,7 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     for (int a = 0; a < 3; ++a) {
         p.cs[a] = p.h[a] / nc[a];
         p.fcs[a] = (float)p.cs[a];
+        p.fsub[a] = (float)(4.0 / p.cs[a]);
     }
     p.half_skin2 = 0.25 * d.skin * d.skin;
     p.dt = d.dt;
@@ -2392,37 +2410,37 @@ pis_status Engine::set_steps(int slot, int64_t steps, std::string& err) {
 void Engine::enqueue_rebuild(bool respect) {
     const DP& P = *d_;
     int r = respect ? 1 : 0;
-    const unsigned ga = grid_cap(max_chunks_, 8);
-    LAUNCH(k_bin, ga, opt_.blk, P, r, (int)max_chunks_);
+    const unsigned ga = (unsigned)max_chunks_;
+    LAUNCH(k_bin, ga, opt_.blk, P, r);
     LAUNCH(k_scan, (unsigned)opt_.max_slots, SCAN_THREADS, P, r);
-    LAUNCH(k_scatter, ga, opt_.blk, P, r, (int)max_chunks_);
+    LAUNCH(k_scatter, ga, opt_.blk, P, r);
     unsigned gcells = (unsigned)((opt_.max_cells * 32 + 255) / 256);
-    LAUNCH(k_gather, grid_cap(gcells, 8), 256, P, (int64_t)opt_.max_cells, r);
+    LAUNCH(k_gather, gcells, 256, P, (int64_t)opt_.max_cells, r);
     launch_build(r);
 }
 
 // Lanes-per-atom kernels are templates; these dispatch on the pool's runtime choice. Their grid
 // has lpa blocks per chunk.
-// Rebuild kernels stride over `chunks` (times L for lanes-per-atom blocks) on at most `cap` blocks.
+// List build over `chunks` (L blocks per chunk for lanes-per-atom layouts).
 template <int L>
-static void launch_build_t(const DP& P, bool half, unsigned chunks, unsigned cap, cudaStream_t st, int r) {
-    const unsigned n = chunks * L, g = n < cap ? n : cap;
+static void launch_build_t(const DP& P, bool half, unsigned chunks, cudaStream_t st, int r) {
+    const unsigned g = chunks * L;
     if (L == 1) {
         // lean kernel for slots with >= 3 cells per axis, generic kernel for the rest
         if (half) {
-            k_build1<true><<<g, 256, 0, st>>>(P, r, (int)n);
-            k_build1_generic<true><<<g, 256, 0, st>>>(P, r, (int)n);
+            k_build1<true><<<g, 256, 0, st>>>(P, r);
+            k_build1_generic<true><<<g, 256, 0, st>>>(P, r);
         } else {
-            k_build1<false><<<g, 256, 0, st>>>(P, r, (int)n);
-            k_build1_generic<false><<<g, 256, 0, st>>>(P, r, (int)n);
+            k_build1<false><<<g, 256, 0, st>>>(P, r);
+            k_build1_generic<false><<<g, 256, 0, st>>>(P, r);
         }
         g_launches.fetch_add(2);
         return;
     }
     if (half)
-        k_build<true, L><<<g, 256, 0, st>>>(P, r, (int)n);
+        k_build<true, L><<<g, 256, 0, st>>>(P, r);
     else
-        k_build<false, L><<<g, 256, 0, st>>>(P, r, (int)n);
+        k_build<false, L><<<g, 256, 0, st>>>(P, r);
     g_launches.fetch_add(1);
 }
 
@@ -2505,13 +2523,12 @@ void Engine::launch_force_cluster(int r) {
 
 void Engine::launch_build(int r) {
     const unsigned ch = (unsigned)max_chunks_;
-    const int ncc = (int)max_cchunks_;
-    const unsigned gc = grid_cap(max_cchunks_, 16), ga = grid_cap(max_chunks_, 8);
+    const unsigned gc = (unsigned)max_cchunks_, ga = (unsigned)max_chunks_;
     if (opt_.cluster) {
         if (opt_.cluster == 2)
-            k_build_cl<2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, ncc);
+            k_build_cl<2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r);
         else
-            k_build_cl<4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, ncc);
+            k_build_cl<4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r);
         g_launches.fetch_add(1);
         return;
     }
@@ -2519,23 +2536,21 @@ void Engine::launch_build(int r) {
         // per-atom lists scanned per cluster; slots with a two-cell axis use the generic kernel
         if (half_) {
             if (clm_ == 2)
-                k_build1_cl<true, 2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, ncc);
+                k_build1_cl<true, 2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r);
             else
-                k_build1_cl<true, 4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, ncc);
-            k_build1_generic<true><<<ga, 256, 0, stream_>>>(*d_, r, (int)ch);
+                k_build1_cl<true, 4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r);
+            k_build1_generic<true><<<ga, 256, 0, stream_>>>(*d_, r);
         } else {
             if (clm_ == 2)
-                k_build1_cl<false, 2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, ncc);
+                k_build1_cl<false, 2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r);
             else
-                k_build1_cl<false, 4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, ncc);
-            k_build1_generic<false><<<ga, 256, 0, stream_>>>(*d_, r, (int)ch);
+                k_build1_cl<false, 4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r);
+            k_build1_generic<false><<<ga, 256, 0, stream_>>>(*d_, r);
         }
         g_launches.fetch_add(2);
         return;
     }
-    const unsigned capb = (unsigned)(8 * num_sms_);
-
-#define PIS_CALL(L) launch_build_t<L>(*d_, half_, ch, capb, stream_, r)
+#define PIS_CALL(L) launch_build_t<L>(*d_, half_, ch, stream_, r)
     PIS_LPA_DISPATCH(opt_.lpa, PIS_CALL)
 #undef PIS_CALL
 }
@@ -2978,6 +2993,7 @@ pis_status Engine::scale_box(int slot, const double* m, std::string& err) {
         (void)ncnew;
         p.cs[a] = nh[a] / p.nc[a];
         p.fcs[a] = (float)p.cs[a];
+        p.fsub[a] = (float)(4.0 / p.cs[a]);
     }
     p.hinv[0] = (p.h[1] * p.h[2]) / (p.h[0] * (p.h[1] * p.h[2]));
     p.hinv[1] = (p.h[0] * p.h[2]) / (p.h[0] * (p.h[1] * p.h[2]));

@@ -57,6 +57,8 @@ struct SysParams {
     double dt, dt2;    // dt, dt*dt
     float fcs[3];
     float frlist2;     // FP32 list radius squared, padded so the FP32 test is a superset
+    float fsub[3];     // 4 / cell edge: sub-cell index scale of the in-cell atom order
+    float pad_f;
 };
 
 // Device-side pair parameters: FP64 quantities computed exactly as the reference does per pair,
@@ -184,7 +186,6 @@ class Engine {
     int64_t max_clusters_ = 0, clpad_ = 0, ccap_ = 0, max_cchunks_ = 0;
     int clm_ = 0;  // atoms per cluster of the cluster table (0: no table)
     int num_sms_ = 1;
-    unsigned grid_cap(int64_t chunks, int per_sm) const;
     cudaStream_t stream_ = nullptr;
     std::vector<SysParams> hp_;
     std::vector<int> slot_tab_size_;
