@@ -94,7 +94,9 @@ pis_status pis_gpu_create(const pis_lj_pair* table, int32_t n_pairs, int32_t n_t
                               * cutoff is still decided with the reference's exact arithmetic */
 #define PIS_OPT_MIXED_KAHAN 2 /* mixed path: compensated FP32 sums instead of FP64 batch sums */
 #define PIS_OPT_LANES(n) ((n) << 8) /* lanes per atom in the list build and force kernels:
-                                     * 1 (thread per atom, default), 4, 8, 16 or 32 (warp per atom) */
+                                     * 1 (thread per atom, default), 4, 8, 16 or 32 (warp per atom);
+                                     * with PIS_OPT_CLUSTER(m), 1 = a thread per cluster and m = a
+                                     * lane per cluster member */
 #define PIS_OPT_BATCH(n) ((n) << 16) /* mixed path, thread per atom: list entries loaded per gather
                                       * batch, 4 (default), 8 or 16 */
 #define PIS_OPT_LIST_TMA 4 /* mixed path, thread per atom: the neighbour list is streamed into shared

@@ -86,6 +86,7 @@ struct Engine::DevPtrs {
     int32_t ccap;
     int32_t clm;          // atoms per cluster of the cluster table (0: no table)
     int32_t cl_force;     // forces run over cluster lists (else per-atom lists)
+    int32_t cl_lanes;     // cluster force blocks per cluster chunk (1, or M with a lane per member)
     int32_t* ctl;         // ctl[0]: some slot rebuilds its list in the current step or evaluation
 };
 using DP = Engine::DevPtrs;
@@ -1028,7 +1029,8 @@ struct MixLJ {
 // The FP32 LJ terms of one batch of list entries against atom i (cell-relative coordinates pi):
 // gathers of every neighbour's prel first (all in flight together), then the pair math, summed
 // into the accumulator's batch sums.
-template <bool ONE, int NB, int ACC>
+// SELF: the list may hold atom i itself (cluster lists), masked by r^2 > 0.
+template <bool ONE, int NB, int ACC, bool SELF = false>
 __device__ __forceinline__ void mixed_pairs(const uint32_t (&ent)[NB], const float4* __restrict__ prel,
                                             const float4& pi, const float4* shift, const LJDev* tab,
                                             const MixLJ& P0, MixAcc<ACC>& a) {
@@ -1053,7 +1055,7 @@ __device__ __forceinline__ void mixed_pairs(const uint32_t (&ent)[NB], const flo
         }
         // evaluated for every entry and masked, so the warp never splits on the cutoff
         // (padding entries have r2 ~ 1e36: 1/r2 -> 0, masked anyway)
-        const bool in = r2 <= frc2;
+        const bool in = SELF ? (r2 <= frc2 && r2 > 0.f) : r2 <= frc2;
         const float inv = rcp_approx(r2);
         const float s2 = fs2 * inv;
         const float s6 = s2 * s2 * s2;
@@ -1271,13 +1273,14 @@ constexpr int CL_THREADS = 128;
 // both are scanned and an atom may be listed once per image; for any one member at most one image
 // lies within the radius (the box is longer than twice the radius), so no pair counts twice.
 template <int M>
-__device__ __forceinline__ void build_cl_chunk(const DP& P, int blk, int step_mode) {
+__device__ __forceinline__ void build_cl_chunk(const DP& P, int blk, int step_mode, bool only_big) {
     const int s = P.cblk_sys[blk];
     if (s < 0) return;
     if (!slot_runs(P, s, step_mode)) return;
     const SysParams& sp = P.sp[s];
     SysState& st = P.st[s];
     if (!st.rebuild) return;
+    if (only_big && (sp.nc[0] < 3 || sp.nc[1] < 3 || sp.nc[2] < 3)) return;
     const int c = P.cblk_first[blk] + (int)threadIdx.x;
     if (c >= sp.cl0 + st.ncl) return;
     const uint32_t pk = (uint32_t)P.cl_atom[c];
@@ -1359,113 +1362,81 @@ __device__ __forceinline__ void build_cl_chunk(const DP& P, int blk, int step_mo
     if (cnt > cap) atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
     P.cl_nn[c] = cnt > cap ? cap : cnt;
 }
+// only_big: skip slots with a two-cell axis (the two-stage per-atom build leaves them to
+// k_build1_generic)
 template <int M>
-__global__ void __launch_bounds__(CL_THREADS) k_build_cl(const DP P, int step_mode) {
+__global__ void __launch_bounds__(CL_THREADS) k_build_cl(const DP P, int step_mode, int only_big) {
     if (!rebuild_block(P, P.cblk_sys, blockIdx.x)) return;
-    build_cl_chunk<M>(P, blockIdx.x, step_mode);
+    build_cl_chunk<M>(P, blockIdx.x, step_mode, only_big != 0);
 }
 
-// Per-atom lists built per cluster (the default build of the thread-per-atom layout): one thread
-// scans the candidates of a cluster's M members and writes each member's own list. Every member
-// gets exactly the list k_build1 gives it - the same neighbour cells in the same order, skipped by
-// the same per-atom face-distance test, the same FP32 distance arithmetic, self / half exclusion
-// and capacity handling - but each candidate position is loaded once for M members, and the lanes
-// of one home cell walk the same cells together. Slots with a two-cell axis are left to
-// k_build1_generic.
+// Per-atom lists from cluster union lists (two-stage build, PIS_OPT_SCAN): after k_build_cl has
+// listed, per cluster, every atom within the list radius of any member, one lane per member
+// filters its cluster's union list into the member's own list. The filter applies k_build1's
+// tests with k_build1's arithmetic - the per-atom face-distance skip of the entry's neighbour cell,
+// the FP32 distance test on the same expressions, self / half exclusion - and the union list
+// holds its candidates in k_build1's cell and atom order, so every member gets exactly the list
+// k_build1 gives it. Cheaper than k_build1 because the candidate scan runs once per cluster, and
+// the M lanes of a cluster share each union entry and each neighbour load. Slots with a two-cell
+// axis are left to k_build1_generic.
 template <bool HALF, int M>
-__device__ __forceinline__ void build1_cl_chunk(const DP& P, int blk, int step_mode) {
-    const int s = P.cblk_sys[blk];
-    if (s < 0) return;
+__global__ void __launch_bounds__(CL_THREADS) k_filter_cl(const DP P, int step_mode) {
+    const int chunk = blockIdx.x / M, sub = blockIdx.x % M;
+    if (!rebuild_block(P, P.cblk_sys, chunk)) return;
+    const int s = P.cblk_sys[chunk];
     if (!slot_runs(P, s, step_mode)) return;
     const SysParams& sp = P.sp[s];
     SysState& st = P.st[s];
     if (!st.rebuild) return;
-    const int nx = sp.nc[0], ny = sp.nc[1], nz = sp.nc[2];
-    if (nx < 3 || ny < 3 || nz < 3) return;
-    const int c = P.cblk_first[blk] + (int)threadIdx.x;
+    if (sp.nc[0] < 3 || sp.nc[1] < 3 || sp.nc[2] < 3) return;
+    const int c = P.cblk_first[chunk] + sub * (CL_THREADS / M) + (int)threadIdx.x / M;
     if (c >= sp.cl0 + st.ncl) return;
     const uint32_t pk = (uint32_t)P.cl_atom[c];
     const int first = (int)(pk & JMASK), n = (int)(pk >> JBITS) + 1;
-    const int lc = P.cellof[first];
-    const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
+    const int m = (int)threadIdx.x % M;
+    if (m >= n) return;
+    const int i = first + m;
     const float4* __restrict__ prel = P.prel;
+    const float4 pi = prel[i];
     const float csx = sp.fcs[0], csy = sp.fcs[1], csz = sp.fcs[2];
     const float rl2 = sp.frlist2;
+    const float gxm = fmaxf(pi.x + 0.5f * csx, 0.f), gxp = fmaxf(0.5f * csx - pi.x, 0.f);
+    const float gym = fmaxf(pi.y + 0.5f * csy, 0.f), gyp = fmaxf(0.5f * csy - pi.y, 0.f);
+    const float gzm = fmaxf(pi.z + 0.5f * csz, 0.f), gzp = fmaxf(0.5f * csz - pi.z, 0.f);
     const int64_t npad = P.npad;
     const int cap = P.cap;
-    const int32_t* __restrict__ cstart = P.cell_start + sp.c0;
-    float px[M], py[M], pz[M];
-    uint32_t* out[M];
-    int cnt[M];
-#pragma unroll
-    for (int m = 0; m < M; ++m) {
-        const float4 q = prel[first + (m < n ? m : 0)];
-        px[m] = q.x;
-        py[m] = q.y;
-        pz[m] = q.z;
-        out[m] = P.nbr + first + m;
-        cnt[m] = 0;
-    }
-    for (int oz = -1; oz <= 1; ++oz) {
-        const int z2 = wrapc(cz + oz, nz);
-        for (int oy = -1; oy <= 1; ++oy) {
-            const int y2 = wrapc(cy + oy, ny);
-            for (int ox = -1; ox <= 1; ++ox) {
-                // per member: k_build1's face-distance skip and its shift to the neighbour image
-                bool use[M];
-                float sx[M], sy[M], sz[M];
-                bool any = false;
-#pragma unroll
-                for (int m = 0; m < M; ++m) {
-                    const float ex = ox < 0 ? fmaxf(px[m] + 0.5f * csx, 0.f) : (ox > 0 ? fmaxf(0.5f * csx - px[m], 0.f) : 0.f);
-                    const float ey = oy < 0 ? fmaxf(py[m] + 0.5f * csy, 0.f) : (oy > 0 ? fmaxf(0.5f * csy - py[m], 0.f) : 0.f);
-                    const float ez = oz < 0 ? fmaxf(pz[m] + 0.5f * csz, 0.f) : (oz > 0 ? fmaxf(0.5f * csz - pz[m], 0.f) : 0.f);
-                    const float eyz = fmaf(ey, ey, ez * ez);
-                    use[m] = m < n && !(fmaf(ex, ex, eyz) > rl2);
-                    any |= use[m];
-                    sx[m] = ox * csx - px[m];
-                    sy[m] = oy * csy - py[m];
-                    sz[m] = oz * csz - pz[m];
-                }
-                if (!any) continue;
-                const int x2 = wrapc(cx + ox, nx);
-                const int nb = (z2 * ny + y2) * nx + x2;
-                const int b0 = cstart[nb], b1 = cstart[nb + 1];
-                const uint32_t codebits = (((uint32_t)(ox < 0 ? 2 : ox)) | ((uint32_t)(oy < 0 ? 2 : oy) << 2) |
-                                           ((uint32_t)(oz < 0 ? 2 : oz) << 4))
-                                          << JBITS;
-                const bool home = ox == 0 && oy == 0 && oz == 0;
-                for (int j = b0; j < b1; ++j) {
-                    const float4 pj = prel[j];
-#pragma unroll
-                    for (int m = 0; m < M; ++m) {
-                        const float dx = pj.x + sx[m], dy = pj.y + sy[m], dz = pj.z + sz[m];
-                        bool take = use[m] && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= rl2;
-                        if (HALF)
-                            take = take && j > first + m;
-                        else if (home)
-                            take = take && j != first + m;
-                        if (take) {
-                            if (cnt[m] < cap) *out[m] = (uint32_t)j | codebits;
-                            out[m] += npad;
-                            ++cnt[m];
-                        }
-                    }
-                }
-            }
+    const int nu = P.cl_nn[c];
+    const uint32_t* __restrict__ un = P.cl_nbr + c;
+    const uint32_t row = (uint32_t)P.clpad;
+    uint32_t* out = P.nbr + i;
+    int cnt = 0;
+    for (int k = 0; k < nu; ++k) {
+        const uint32_t e = load_list_word(un + (uint32_t)k * row);
+        const int j = (int)(e & JMASK);
+        const uint32_t code = e >> JBITS;
+        const int ox = (code & 3u) == 2u ? -1 : (int)(code & 3u);
+        const int oy = ((code >> 2) & 3u) == 2u ? -1 : (int)((code >> 2) & 3u);
+        const int oz = ((code >> 4) & 3u) == 2u ? -1 : (int)((code >> 4) & 3u);
+        const float ex = ox < 0 ? gxm : (ox > 0 ? gxp : 0.f);
+        const float ey = oy < 0 ? gym : (oy > 0 ? gyp : 0.f);
+        const float ez = oz < 0 ? gzm : (oz > 0 ? gzp : 0.f);
+        const float eyz = fmaf(ey, ey, ez * ez);
+        if (fmaf(ex, ex, eyz) > rl2) continue;  // k_build1 never scans this cell for atom i
+        const float4 pj = prel[j];
+        const float dx = pj.x + (ox * csx - pi.x), dy = pj.y + (oy * csy - pi.y), dz = pj.z + (oz * csz - pi.z);
+        bool take = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= rl2;
+        if (HALF)
+            take = take && j > i;
+        else if (ox == 0 && oy == 0 && oz == 0)
+            take = take && j != i;
+        if (take) {
+            if (cnt < cap) *out = e;
+            out += npad;
+            ++cnt;
         }
     }
-#pragma unroll
-    for (int m = 0; m < M; ++m) {
-        if (m >= n) continue;
-        if (cnt[m] > cap) atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
-        P.nn[first + m] = cnt[m] > cap ? cap : cnt[m];
-    }
-}
-template <bool HALF, int M>
-__global__ void __launch_bounds__(CL_THREADS) k_build1_cl(const DP P, int step_mode) {
-    if (!rebuild_block(P, P.cblk_sys, blockIdx.x)) return;
-    build1_cl_chunk<HALF, M>(P, blockIdx.x, step_mode);
+    if (cnt > cap) atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
+    P.nn[i] = cnt > cap ? cap : cnt;
 }
 
 // Forces: thread per cluster. For each batch of NB list entries the words are loaded, then the
@@ -1585,6 +1556,62 @@ __global__ void __launch_bounds__(CL_THREADS) k_force_cl(const DP P, int step_mo
     if (threadIdx.x == 0) P.pe_part[blockIdx.x] = tot;
 }
 
+// Forces over cluster lists, one lane per member: the M lanes of a cluster load the same list word
+// and the same neighbour position (a broadcast), and each evaluates its own member with the
+// per-atom kernel's arithmetic. A warp's gather then touches 32 / M addresses instead of 32, with
+// the registers and per-lane work of the per-atom kernel; a member meets itself in the list
+// (masked by r^2 > 0) and a padding lane of a short cluster idles. M blocks per cluster chunk.
+template <int ACC, bool ONE, int M, int NB>
+__global__ void __launch_bounds__(CL_THREADS) k_force_cl_lane(const DP P, int step_mode) {
+    __shared__ double sh[32];
+    __shared__ float4 shift[64];
+    const int chunk = blockIdx.x / M, sub = blockIdx.x % M;
+    const int s = P.cblk_sys[chunk];
+    if (s < 0) return;
+    if (!slot_runs(P, s, step_mode)) return;
+    const SysParams& sp = P.sp[s];
+    fill_shift_table(shift, sp);
+    __syncthreads();
+    const int c = P.cblk_first[chunk] + sub * (CL_THREADS / M) + (int)threadIdx.x / M;
+    const int m = (int)threadIdx.x % M;
+    MixAcc<ACC> acc;
+    if (c < sp.cl0 + P.st[s].ncl) {
+        const uint32_t pk = (uint32_t)P.cl_atom[c];
+        const int first = (int)(pk & JMASK), n = (int)(pk >> JBITS) + 1;
+        const bool live = m < n;
+        const float4* __restrict__ prel = P.prel;
+        const float4 pi = live ? prel[first + m] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
+        const LJDev* tab = P.tab + sp.tab0 + (live ? __float_as_int(pi.w) : 0) * sp.nt;
+        const MixLJ P0 = mix_lj_load(tab[0]);
+        const int nn = P.cl_nn[c];
+        const uint32_t* __restrict__ nbp = P.cl_nbr + c;
+        const uint32_t row = (uint32_t)P.clpad;
+        const uint32_t pad = (uint32_t)first | (63u << JBITS);
+        int since = 0;
+        for (int k0 = 0; k0 < nn; k0 += NB) {
+            uint32_t ent[NB];
+            const uint32_t q = (uint32_t)k0 * row;
+            if (k0 + NB <= nn) {
+#pragma unroll
+                for (int b = 0; b < NB; ++b) ent[b] = load_list_word(nbp + q + (uint32_t)b * row);
+            } else {
+#pragma unroll
+                for (int b = 0; b < NB; ++b) ent[b] = (k0 + b < nn) ? load_list_word(nbp + q + (uint32_t)b * row) : pad;
+            }
+            mixed_pairs<ONE, NB, ACC, true>(ent, prel, pi, shift, tab, P0, acc);
+            since += NB;
+            if (since >= MIX_FLUSH) {
+                acc.fold();
+                since = 0;
+            }
+        }
+        acc.finish();
+        if (live) P.frc[first + m] = make_double4_32a(acc.fx, acc.fy, acc.fz, 0.0);
+    }
+    double tot = block_sum<CL_THREADS>(acc.e, sh);
+    if (threadIdx.x == 0) P.pe_part[blockIdx.x] = tot;
+}
+
 // Exact cutoff test of every (member, entry) pair of one slot's cluster lists with the reference
 // arithmetic (min-image, Vector3::norm, `> rcut`), for neighbour-set export: bit m of keep marks
 // member m.
@@ -1697,8 +1724,10 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
     double pe = 0.0, ke = 0.0;
     const int F = P.pe_stride;
     if (mode != 2) {
-        if (P.cl_force)  // cluster kernels: one partial per cluster chunk
-            for (int c = threadIdx.x; c < sp.ncch; c += END_THREADS) pe += P.pe_part[(int64_t)sp.cch0 + c];
+        if (P.cl_force) {  // cluster kernels: cl_lanes partials per cluster chunk
+            const int L = P.cl_lanes;
+            for (int c = threadIdx.x; c < sp.ncch * L; c += END_THREADS) pe += P.pe_part[(int64_t)sp.cch0 * L + c];
+        }
         else
             for (int c = threadIdx.x; c < sp.nch * F; c += END_THREADS) pe += P.pe_part[(int64_t)sp.ch0 * F + c];
     }
@@ -1810,6 +1839,65 @@ __global__ void k_scale_pos(const DP P, int slot, double oh0, double oh1, double
     P.pos[cur][i] = p;
 }
 
+// Upload of one slot's state. The caller's arrays (x,y,z per atom, 1-based types) are copied as
+// they are into the slot's range of the idle buffer set (pos[1], vel[1], acc[1], id[1]: nothing
+// lives there before the first rebuild) and converted here: type bits in pos.w, the type's mass in
+// vel.w, a = 0 + F/m and 1/m in acc (the host arithmetic of Atoms::current_acceleration,
+// src/atoms/properties.rs:32-39, with IEEE division), the build snapshot, original indices.
+struct MassArg {
+    double m[16];
+};
+__global__ void k_load_slot(const DP P, int64_t a0, int n, const MassArg masses, int has_vel, int has_force) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double* xs = reinterpret_cast<const double*>(P.pos[1] + a0);
+    const double* vs = reinterpret_cast<const double*>(P.vel[1] + a0);
+    const double* fs = reinterpret_cast<const double*>(P.acc[1] + a0);
+    const int t0 = P.id[1][a0 + k] - 1;
+    const double m = masses.m[t0];
+    const double4_32a p = make_double4_32a(xs[3 * k], xs[3 * k + 1], xs[3 * k + 2], pack_type(t0));
+    const double vx = has_vel ? vs[3 * k] : 0.0, vy = has_vel ? vs[3 * k + 1] : 0.0, vz = has_vel ? vs[3 * k + 2] : 0.0;
+    const double fx = has_force ? fs[3 * k] : 0.0, fy = has_force ? fs[3 * k + 1] : 0.0,
+                 fz = has_force ? fs[3 * k + 2] : 0.0;
+    P.pos[0][a0 + k] = p;
+    P.posb[a0 + k] = p;
+    P.vel[0][a0 + k] = make_double4_32a(vx, vy, vz, m);
+    P.frc[a0 + k] = make_double4_32a(fx, fy, fz, 0.0);
+    P.acc[0][a0 + k] = make_double4_32a(__dadd_rn(0.0, __ddiv_rn(fx, m)), __dadd_rn(0.0, __ddiv_rn(fy, m)),
+                                        __dadd_rn(0.0, __ddiv_rn(fz, m)), __ddiv_rn(1.0, m));
+    P.id[0][a0 + k] = k;
+}
+
+// Download of one slot's state in the caller's atom order: the current arrays are un-permuted
+// (device order -> original index) into x,y,z-per-atom staging in the idle buffer set, which the
+// host then copies out in one transfer per array.
+__global__ void k_store_slot(const DP P, int64_t a0, int n, int cur, int want_pos, int want_vel, int want_force) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int o = P.id[cur][a0 + k];
+    if (want_pos) {
+        const double4_32a v = P.pos[cur][a0 + k];
+        double* out = reinterpret_cast<double*>(P.pos[cur ^ 1] + a0) + 3 * (int64_t)o;
+        out[0] = v.x;
+        out[1] = v.y;
+        out[2] = v.z;
+    }
+    if (want_vel) {
+        const double4_32a v = P.vel[cur][a0 + k];
+        double* out = reinterpret_cast<double*>(P.vel[cur ^ 1] + a0) + 3 * (int64_t)o;
+        out[0] = v.x;
+        out[1] = v.y;
+        out[2] = v.z;
+    }
+    if (want_force) {
+        const double4_32a v = P.frc[a0 + k];
+        double* out = reinterpret_cast<double*>(P.acc[cur ^ 1] + a0) + 3 * (int64_t)o;
+        out[0] = v.x;
+        out[1] = v.y;
+        out[2] = v.z;
+    }
+}
+
 // ---------------------------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------------------------
@@ -1854,8 +1942,9 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         err = "chunk size must be 256";
         return PIS_ERR_INVALID_ARGUMENT;
     }
-    if (opt.lpa != 1 && opt.lpa != 4 && opt.lpa != 8 && opt.lpa != 16 && opt.lpa != 32) {
-        err = "lanes per atom must be 1, 4, 8, 16 or 32";
+    if (opt.lpa != 1 && opt.lpa != 4 && opt.lpa != 8 && opt.lpa != 16 && opt.lpa != 32 &&
+        !(opt.lpa == 2 && opt.cluster == 2)) {
+        err = "lanes per atom must be 1, 4, 8, 16 or 32 (2 only with clusters of 2)";
         return PIS_ERR_INVALID_ARGUMENT;
     }
     half_ = opt.list_kind == PIS_LIST_HALF ||
@@ -1876,8 +1965,9 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         err = "atoms per cluster must be 2 or 4";
         return PIS_ERR_INVALID_ARGUMENT;
     }
-    if (opt.cluster && (opt.precision != PIS_PRECISION_MIXED || opt.lpa != 1 || opt.list_tma)) {
-        err = "the cluster list is a variant of the mixed path with one thread per cluster";
+    if (opt.cluster && (opt.precision != PIS_PRECISION_MIXED || (opt.lpa != 1 && opt.lpa != opt.cluster) ||
+                        opt.list_tma)) {
+        err = "the cluster list is a variant of the mixed path with one thread per cluster or one lane per member";
         return PIS_ERR_UNSUPPORTED;
     }
     if (opt.build_cluster != 0 && opt.build_cluster != 1 && opt.build_cluster != 2 && opt.build_cluster != 4) {
@@ -1907,7 +1997,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         max_clusters_ = (opt.max_atoms + M - 1) / M + max_cells + opt.max_slots;
         clpad_ = (int64_t)align_up((size_t)max_clusters_, 32);
         // union of M members' lists: ~1.4x (M = 2) / ~1.9x (M = 4) one atom's list
-        ccap_ = opt.cluster ? (int64_t)std::ceil((double)cap_ * (M == 2 ? 1.5 : 2.0)) : 0;
+        ccap_ = (int64_t)std::ceil((double)cap_ * (M == 2 ? 1.5 : 2.0));
         ccap_ = (ccap_ + 31) / 32 * 32;
         max_cchunks_ = (max_clusters_ + CL_THREADS - 1) / CL_THREADS + opt.max_slots;
         if ((double)clpad_ * (double)ccap_ >= 4294967296.0) {
@@ -1947,7 +2037,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         {(void**)&d_->cell_sys, 4 * NC}, {(void**)&d_->blk_sys, 4 * NCH},
         {(void**)&d_->blk_first, 4 * NCH}, {(void**)&d_->sp, sizeof(SysParams) * NS},
         {(void**)&d_->st, sizeof(SysState) * NS}, {(void**)&d_->tab, sizeof(LJDev) * (size_t)opt.max_types_total},
-        {(void**)&d_->pe_part, 8 * std::max(NCH * 32, NCC)}, {(void**)&d_->ke_part, 8 * NCH},
+        {(void**)&d_->pe_part, 8 * std::max(NCH * 32, NCC * 4)}, {(void**)&d_->ke_part, 8 * NCH},
         {(void**)&d_->vir_part, 72 * NCH}, {(void**)&d_->pe_hist, 8 * NS * (size_t)opt.hist},
         {(void**)&d_->ctl, 256},
     };
@@ -1957,7 +2047,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         items.push_back({(void**)&d_->cblk_sys, 4 * NCC});
         items.push_back({(void**)&d_->cblk_first, 4 * NCC});
     }
-    if (opt.cluster) {
+    if (clm_) {
         items.push_back({(void**)&d_->cl_nn, 4 * NCL});
         items.push_back({(void**)&d_->cl_nbr, 4 * (size_t)clpad_ * (size_t)ccap_});
     }
@@ -1983,6 +2073,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     d_->ccap = (int32_t)ccap_;
     d_->clm = clm_;
     d_->cl_force = opt.cluster ? 1 : 0;
+    d_->cl_lanes = (opt.cluster && opt.lpa == opt.cluster) ? opt.cluster : 1;
     st = check(cudaMemsetAsync(mem_, 0, total, stream_), "memset", err);
     if (st) return st;
     st = check(cudaMemsetAsync(d_->cell_sys, 0xff, 4 * NC, stream_), "memset", err);
@@ -2249,23 +2340,15 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     hp_[slot] = p;
     slot_rlist_[slot] = rlist;
 
-    // atom state: AoS (x,y,z per atom) -> double4_32a with the type (pos.w) and mass (vel.w)
-    std::vector<double4_32a> hpos(d.n), hvel(d.n), hfrc(d.n), hacc(d.n);
-    std::vector<int32_t> hid(d.n);
-    for (int64_t k = 0; k < d.n; ++k) {
-        int t0 = type_ids[k] - 1;
-        double w;
-        int32_t hi = t0, lo = 0;
-        uint64_t bits = ((uint64_t)(uint32_t)hi << 32) | (uint32_t)lo;
-        std::memcpy(&w, &bits, 8);
-        hpos[k] = make_double4_32a(pos[3 * k], pos[3 * k + 1], pos[3 * k + 2], w);
-        double m = d.masses[t0];
-        hvel[k] = vel ? make_double4_32a(vel[3 * k], vel[3 * k + 1], vel[3 * k + 2], m) : make_double4_32a(0, 0, 0, m);
-        hfrc[k] = force ? make_double4_32a(force[3 * k], force[3 * k + 1], force[3 * k + 2], 0.0) : make_double4_32a(0, 0, 0, 0);
-        // acc = 0 + F/m (Atoms::current_acceleration) and 1/m for the mixed path
-        hacc[k] = make_double4_32a(0.0 + hfrc[k].x / m, 0.0 + hfrc[k].y / m, 0.0 + hfrc[k].z / m, 1.0 / m);
-        hid[k] = (int32_t)k;
+    // atom state: the caller's x,y,z-per-atom arrays and types go to the device as they are, and
+    // k_load_slot builds the device layout
+    if (nt > 16) {
+        err = "at most 16 atom types per system";
+        return -PIS_ERR_UNSUPPORTED;
     }
+    MassArg ma;
+    std::memset(&ma, 0, sizeof(ma));
+    for (int t = 0; t < nt; ++t) ma.m[t] = d.masses[t];
     SysState ss;
     std::memset(&ss, 0, sizeof(ss));
     ss.cur = 0;
@@ -2276,12 +2359,13 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
         st = check(cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyHostToDevice, stream_), "upload", err); \
         if (st) return -st;                                                                             \
     } while (0)
-    CP(d_->pos[0] + a0, hpos.data(), 32 * d.n);
-    CP(d_->vel[0] + a0, hvel.data(), 32 * d.n);
-    CP(d_->frc + a0, hfrc.data(), 32 * d.n);
-    CP(d_->posb + a0, hpos.data(), 32 * d.n);
-    CP(d_->id[0] + a0, hid.data(), 4 * d.n);
-    CP(d_->acc[0] + a0, hacc.data(), 32 * d.n);
+    CP(d_->pos[1] + a0, pos, 24 * d.n);
+    if (vel) CP(d_->vel[1] + a0, vel, 24 * d.n);
+    if (force) CP(d_->acc[1] + a0, force, 24 * d.n);
+    CP(d_->id[1] + a0, type_ids, 4 * d.n);
+    LAUNCH(k_load_slot, (unsigned)((d.n + 255) / 256), 256, *d_, a0, (int)d.n, ma, vel ? 1 : 0, force ? 1 : 0);
+    st = check(cudaGetLastError(), "upload", err);
+    if (st) return -st;
     st = check(cudaMemsetAsync(d_->cellof + a0, 0, 4 * d.n, stream_), "upload", err);
     if (st) return -st;
     st = check(cudaMemsetAsync(d_->nn + a0, 0, 4 * d.n, stream_), "upload", err);
@@ -2496,7 +2580,14 @@ static void launch_fp64_t(const DP& P, bool half, bool fast, unsigned chunks, cu
     }
 
 template <int ACC, bool ONE, int M>
-static void launch_cluster_t(const DP& P, int batch, unsigned chunks, cudaStream_t st, int r) {
+static void launch_cluster_t(const DP& P, int batch, bool lanes, unsigned chunks, cudaStream_t st, int r) {
+    if (lanes) {
+        if (batch >= 8)
+            k_force_cl_lane<ACC, ONE, M, 8><<<chunks * M, CL_THREADS, 0, st>>>(P, r);
+        else
+            k_force_cl_lane<ACC, ONE, M, 4><<<chunks * M, CL_THREADS, 0, st>>>(P, r);
+        return;
+    }
     if (batch >= 8)
         k_force_cl<ACC, ONE, M, 8><<<chunks, CL_THREADS, 0, st>>>(P, r);
     else
@@ -2504,20 +2595,25 @@ static void launch_cluster_t(const DP& P, int batch, unsigned chunks, cudaStream
 }
 
 template <int M>
-static void launch_cluster_m(const DP& P, bool kahan, bool one, int batch, unsigned chunks, cudaStream_t st, int r) {
+static void launch_cluster_m(const DP& P, bool kahan, bool one, int batch, bool lanes, unsigned chunks, cudaStream_t st,
+                             int r) {
     if (kahan)
-        one ? launch_cluster_t<1, true, M>(P, batch, chunks, st, r) : launch_cluster_t<1, false, M>(P, batch, chunks, st, r);
+        one ? launch_cluster_t<1, true, M>(P, batch, lanes, chunks, st, r)
+            : launch_cluster_t<1, false, M>(P, batch, lanes, chunks, st, r);
     else
-        one ? launch_cluster_t<0, true, M>(P, batch, chunks, st, r) : launch_cluster_t<0, false, M>(P, batch, chunks, st, r);
+        one ? launch_cluster_t<0, true, M>(P, batch, lanes, chunks, st, r)
+            : launch_cluster_t<0, false, M>(P, batch, lanes, chunks, st, r);
 }
 
-// Cluster-list forces: entries per batch = the batch knob (4 or 8).
+// Cluster-list forces: entries per batch = the batch knob (4 or 8); lanes per atom = M selects the
+// lane-per-member kernel.
 void Engine::launch_force_cluster(int r) {
     const unsigned ch = (unsigned)max_cchunks_;
+    const bool lanes = opt_.lpa == opt_.cluster;
     if (opt_.cluster == 2)
-        launch_cluster_m<2>(*d_, opt_.mixed_kahan, single_type_, opt_.mix_batch, ch, stream_, r);
+        launch_cluster_m<2>(*d_, opt_.mixed_kahan, single_type_, opt_.mix_batch, lanes, ch, stream_, r);
     else
-        launch_cluster_m<4>(*d_, opt_.mixed_kahan, single_type_, opt_.mix_batch, ch, stream_, r);
+        launch_cluster_m<4>(*d_, opt_.mixed_kahan, single_type_, opt_.mix_batch, lanes, ch, stream_, r);
     g_launches.fetch_add(1);
 }
 
@@ -2526,28 +2622,33 @@ void Engine::launch_build(int r) {
     const unsigned gc = (unsigned)max_cchunks_, ga = (unsigned)max_chunks_;
     if (opt_.cluster) {
         if (opt_.cluster == 2)
-            k_build_cl<2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r);
+            k_build_cl<2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, 0);
         else
-            k_build_cl<4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r);
+            k_build_cl<4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, 0);
         g_launches.fetch_add(1);
         return;
     }
     if (clm_ && opt_.lpa == 1) {
-        // per-atom lists scanned per cluster; slots with a two-cell axis use the generic kernel
-        if (half_) {
-            if (clm_ == 2)
-                k_build1_cl<true, 2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r);
+        // two-stage per-atom build: cluster union lists, filtered per member; slots with a
+        // two-cell axis use the generic kernel
+        if (clm_ == 2) {
+            k_build_cl<2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, 1);
+            if (half_)
+                k_filter_cl<true, 2><<<gc * 2, CL_THREADS, 0, stream_>>>(*d_, r);
             else
-                k_build1_cl<true, 4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r);
-            k_build1_generic<true><<<ga, 256, 0, stream_>>>(*d_, r);
+                k_filter_cl<false, 2><<<gc * 2, CL_THREADS, 0, stream_>>>(*d_, r);
         } else {
-            if (clm_ == 2)
-                k_build1_cl<false, 2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r);
+            k_build_cl<4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, 1);
+            if (half_)
+                k_filter_cl<true, 4><<<gc * 4, CL_THREADS, 0, stream_>>>(*d_, r);
             else
-                k_build1_cl<false, 4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r);
-            k_build1_generic<false><<<ga, 256, 0, stream_>>>(*d_, r);
+                k_filter_cl<false, 4><<<gc * 4, CL_THREADS, 0, stream_>>>(*d_, r);
         }
-        g_launches.fetch_add(2);
+        if (half_)
+            k_build1_generic<true><<<ga, 256, 0, stream_>>>(*d_, r);
+        else
+            k_build1_generic<false><<<ga, 256, 0, stream_>>>(*d_, r);
+        g_launches.fetch_add(3);
         return;
     }
 #define PIS_CALL(L) launch_build_t<L>(*d_, half_, ch, stream_, r)
@@ -2750,44 +2851,26 @@ pis_status Engine::download(int slot, double* pos, double* vel, double* force, s
     SysState ss;
     pis_status st = read_state(slot, ss, err);
     if (st) return st;
+    if (!pos && !vel && !force) return PIS_OK;
     const int cur = ss.cur;
-    std::vector<double4_32a> hp(p.n), hv(p.n), hf(p.n);
-    std::vector<int32_t> hid(p.n);
-    st = check(cudaMemcpyAsync(hid.data(), d_->id[cur] + p.a0, 4 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "download", err);
+    LAUNCH(k_store_slot, (unsigned)((p.n + 255) / 256), 256, *d_, p.a0, p.n, cur, pos ? 1 : 0, vel ? 1 : 0,
+           force ? 1 : 0);
+    st = check(cudaGetLastError(), "download", err);
     if (st) return st;
+    const size_t bytes = 24 * (size_t)p.n;
     if (pos) {
-        st = check(cudaMemcpyAsync(hp.data(), d_->pos[cur] + p.a0, 32 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "download", err);
+        st = check(cudaMemcpyAsync(pos, d_->pos[cur ^ 1] + p.a0, bytes, cudaMemcpyDeviceToHost, stream_), "download", err);
         if (st) return st;
     }
     if (vel) {
-        st = check(cudaMemcpyAsync(hv.data(), d_->vel[cur] + p.a0, 32 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "download", err);
+        st = check(cudaMemcpyAsync(vel, d_->vel[cur ^ 1] + p.a0, bytes, cudaMemcpyDeviceToHost, stream_), "download", err);
         if (st) return st;
     }
     if (force) {
-        st = check(cudaMemcpyAsync(hf.data(), d_->frc + p.a0, 32 * (size_t)p.n, cudaMemcpyDeviceToHost, stream_), "download", err);
+        st = check(cudaMemcpyAsync(force, d_->acc[cur ^ 1] + p.a0, bytes, cudaMemcpyDeviceToHost, stream_), "download", err);
         if (st) return st;
     }
-    st = sync(err);
-    if (st) return st;
-    for (int k = 0; k < p.n; ++k) {
-        int o = hid[k];
-        if (pos) {
-            pos[3 * o] = hp[k].x;
-            pos[3 * o + 1] = hp[k].y;
-            pos[3 * o + 2] = hp[k].z;
-        }
-        if (vel) {
-            vel[3 * o] = hv[k].x;
-            vel[3 * o + 1] = hv[k].y;
-            vel[3 * o + 2] = hv[k].z;
-        }
-        if (force) {
-            force[3 * o] = hf[k].x;
-            force[3 * o + 1] = hf[k].y;
-            force[3 * o + 2] = hf[k].z;
-        }
-    }
-    return PIS_OK;
+    return sync(err);
 }
 
 pis_status Engine::read_state(int slot, SysState& ss, std::string& err) {

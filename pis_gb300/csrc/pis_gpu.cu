@@ -26,6 +26,7 @@ struct pis_gpu_ctx {
     int cluster = 0;
     int build_cluster = 0;
     std::unique_ptr<pis::Engine> eng;
+    pis::PoolOptions pool;  // options the current engine was created with
     int slot = -1;
     int64_t n = 0;
     double dt = 0.0;
@@ -49,6 +50,16 @@ int list_capacity(int64_t n, const double* h_rowmajor, double rlist) {
     double cap = 1.6 * full + 32.0;
     if (cap > 4096) cap = 4096;
     return ((int)std::ceil(cap) + 7) / 8 * 8;
+}
+
+// Two states with equal pool options (atom count, cell grid, list capacity, variants) share one
+// engine: its memory and captured step graphs are reused.
+bool same_pool(const pis::PoolOptions& a, const pis::PoolOptions& b) {
+    return a.precision == b.precision && a.list_kind == b.list_kind && a.blk == b.blk && a.list_cap == b.list_cap &&
+           a.max_atoms == b.max_atoms && a.max_slots == b.max_slots && a.max_cells == b.max_cells &&
+           a.max_types_total == b.max_types_total && a.hist == b.hist && a.fp64_fast == b.fp64_fast &&
+           a.mixed_kahan == b.mixed_kahan && a.lpa == b.lpa && a.mix_batch == b.mix_batch &&
+           a.list_tma == b.list_tma && a.cluster == b.cluster && a.build_cluster == b.build_cluster;
 }
 
 pis_status flags_to_status(pis_gpu_ctx* ctx, const pis::SysState& ss) {
@@ -109,8 +120,10 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "batch must be 4, 8 or 16");
     ctx->mix_batch = batch ? batch : 4;
     const int lanes = (flags >> 8) & 0xff;
-    if (lanes != 0 && lanes != 1 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
-        return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "lanes per atom must be 1, 4, 8, 16 or 32");
+    const int cl_req = (flags >> 24) & 0xf;
+    if (lanes != 0 && lanes != 1 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32 &&
+        !(lanes == 2 && cl_req == 2))
+        return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "lanes per atom must be 1, 4, 8, 16 or 32 (2 only with clusters of 2)");
     ctx->lpa = lanes ? lanes : 1;
     ctx->fp64_fast = (flags & PIS_OPT_FP64_FAST) != 0;
     ctx->mixed_kahan = (flags & PIS_OPT_MIXED_KAHAN) != 0;
@@ -122,8 +135,10 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
     if (scan != 0 && scan != 1 && scan != 2 && scan != 4)
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "atoms per build cluster must be 1, 2 or 4");
     ctx->build_cluster = scan;
-    if (ctx->cluster && (ctx->precision != PIS_PRECISION_MIXED || ctx->lpa != 1 || ctx->list_tma))
-        return fail(ctx, PIS_ERR_UNSUPPORTED, "the cluster list needs the mixed path, one thread per cluster");
+    if (ctx->cluster && (ctx->precision != PIS_PRECISION_MIXED || (ctx->lpa != 1 && ctx->lpa != ctx->cluster) ||
+                         ctx->list_tma))
+        return fail(ctx, PIS_ERR_UNSUPPORTED,
+                    "the cluster list needs the mixed path, one thread per cluster or one lane per member");
     if (ctx->list_tma && (ctx->precision != PIS_PRECISION_MIXED || ctx->lpa != 1))
         return fail(ctx, PIS_ERR_UNSUPPORTED, "the bulk-copy list stream needs the mixed path, thread per atom");
     if (ctx->precision == PIS_PRECISION_MIXED && list_kind == PIS_LIST_HALF)
@@ -154,10 +169,6 @@ pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_id
         if (e.present && e.rcut > rc) rc = e.rcut;
     double rlist = rc + ctx->skin;
 
-    ctx->eng.reset();
-    ctx->slot = -1;
-    ctx->n = 0;
-    auto eng = std::make_unique<pis::Engine>();
     pis::PoolOptions opt;
     opt.precision = ctx->precision;
     opt.list_kind = ctx->list_kind;
@@ -179,11 +190,27 @@ pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_id
     opt.max_types_total = ctx->n_types * ctx->n_types;
     opt.list_cap = list_capacity(n, d.h, rlist);
     std::string err;
+    if (ctx->eng && ctx->slot >= 0 && same_pool(ctx->pool, opt)) {
+        // same pool shape: replace the system in place
+        ctx->eng->remove_slot(ctx->slot);
+        ctx->slot = -1;
+        ctx->n = 0;
+        int slot = ctx->eng->add_slot(d, type_ids, pos, vel, force, err);
+        if (slot < 0) return fail(ctx, (pis_status)(-slot), err);
+        ctx->slot = slot;
+        ctx->n = n;
+        return PIS_OK;
+    }
+    ctx->eng.reset();
+    ctx->slot = -1;
+    ctx->n = 0;
+    auto eng = std::make_unique<pis::Engine>();
     pis_status st = eng->init(opt, err);
     if (st) return fail(ctx, st, err);
     int slot = eng->add_slot(d, type_ids, pos, vel, force, err);
     if (slot < 0) return fail(ctx, (pis_status)(-slot), err);
     ctx->eng = std::move(eng);
+    ctx->pool = opt;
     ctx->slot = slot;
     ctx->n = n;
     return PIS_OK;

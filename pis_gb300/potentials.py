@@ -81,8 +81,15 @@ class GpuContext:
         self._check(self._lib.pis_gpu_run_timed(self._h, float(dt), int(n_steps), C.byref(ms), _dp(st)))
         return ms.value, st
 
-    def get_state(self):
-        pos, vel, frc = np.zeros((self.n, 3)), np.zeros((self.n, 3)), np.zeros((self.n, 3))
+    def get_state(self, out=None):
+        """(positions, velocities, forces) as (n, 3) arrays; ``out`` may supply three C-contiguous
+        float64 (n, 3) arrays to fill (e.g. in pinned host memory)."""
+        if out is None:
+            out = (np.zeros((self.n, 3)), np.zeros((self.n, 3)), np.zeros((self.n, 3)))
+        for a in out:
+            if a.dtype != np.float64 or a.shape != (self.n, 3) or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError("output arrays must be C-contiguous float64 of shape (n, 3)")
+        pos, vel, frc = out
         self._check(self._lib.pis_gpu_get_state(self._h, _dp(pos), _dp(vel), _dp(frc)))
         return pos, vel, frc
 

@@ -1,7 +1,8 @@
 """Mixed precision through the cluster-list kernels (PIS_OPT_CLUSTER(2 or 4)), against the oracle.
 
 A cluster is a run of up to m spatially adjacent atoms of one cell; its list holds every atom
-within the list radius of any member, and one thread evaluates every (member, entry) pair. The
+within the list radius of any member; one thread evaluates every (member, entry) pair
+(PIS_OPT_LANES(1)) or one lane per member evaluates its own pairs (PIS_OPT_LANES(m)). The
 bars are the mixed-precision ones: force RMS <= 1e-5 relative to the FP64 oracle, energies within
 1e-5, neighbour sets within the cutoff identical to the reference's build_neighbour_list, and a
 replica bit-identical alone and in a mix.
@@ -35,13 +36,14 @@ def liquid_melt(oracle_lib, cuda_lib):
     return melted(liquid(nc=6), steps=300, dt=0.005)
 
 
+@pytest.mark.parametrize("lane", [False, True])
 @pytest.mark.parametrize("batch", [4, 8])
 @pytest.mark.parametrize("kahan", [False, True])
 @pytest.mark.parametrize("cluster", [2, 4])
-def test_cluster_force_error(liquid_melt, cluster, kahan, batch):
+def test_cluster_force_error(liquid_melt, cluster, kahan, batch, lane):
     o = to_oracle(liquid_melt)
     pe_ref = o.compute_potential()
-    g = to_gpu(liquid_melt, "mixed", mixed_kahan=kahan, batch=batch, cluster=cluster)
+    g = to_gpu(liquid_melt, "mixed", mixed_kahan=kahan, batch=batch, cluster=cluster, lanes=cluster if lane else 1)
     pe, f = g.compute_potential()
     rms = np.sqrt(np.sum((f - o.force) ** 2) / np.sum(o.force ** 2))
     assert rms <= 1e-5, rms
@@ -59,19 +61,21 @@ def test_cluster_neighbour_sets_exact(liquid_melt, cluster):
     assert _sets(off, idx) == [tuple(sorted(x)) for x in _sets(off_r, idx_r)]
 
 
+@pytest.mark.parametrize("lane", [False, True])
 @pytest.mark.parametrize("cluster", [2, 4])
-def test_cluster_trajectory_close(liquid_melt, cluster):
+def test_cluster_trajectory_close(liquid_melt, cluster, lane):
     o = to_oracle(liquid_melt)
     pe_ref, _ = o.run_nve(0.005, 50)
-    g = to_gpu(liquid_melt, "mixed", cluster=cluster)
+    g = to_gpu(liquid_melt, "mixed", cluster=cluster, lanes=cluster if lane else 1)
     g.compute_potential()
     pe = g.verlet_step_nve(0.005, 50)
     assert np.max(np.abs(pe - pe_ref[1:]) / np.abs(pe_ref[1:])) <= 1e-4
     assert g.stats()["rebuilds"] >= 2
 
 
+@pytest.mark.parametrize("lane", [False, True])
 @pytest.mark.parametrize("cluster", [2, 4])
-def test_cluster_two_type_mixture(oracle_lib, cuda_lib, cluster):
+def test_cluster_two_type_mixture(oracle_lib, cuda_lib, cluster, lane):
     rng = np.random.default_rng(4)
     s = liquid(nc=6, rho=0.8)
     n = len(s["pos"])
@@ -81,7 +85,7 @@ def test_cluster_two_type_mixture(oracle_lib, cuda_lib, cluster):
     s = displaced(s, 0.02, 2)
     o = to_oracle(s)
     pe_ref = o.compute_potential()
-    g = to_gpu(s, "mixed", cluster=cluster)
+    g = to_gpu(s, "mixed", cluster=cluster, lanes=cluster if lane else 1)
     pe, f = g.compute_potential()
     assert abs(pe - pe_ref) <= 1e-5 * abs(pe_ref)
     assert rel_norm(f, o.force) <= 1e-5
@@ -90,14 +94,15 @@ def test_cluster_two_type_mixture(oracle_lib, cuda_lib, cluster):
     assert _sets(off, idx) == [tuple(sorted(x)) for x in _sets(off_r, idx_r)]
 
 
+@pytest.mark.parametrize("lane", [False, True])
 @pytest.mark.parametrize("cluster", [2, 4])
-def test_cluster_small_box_two_cells(oracle_lib, cuda_lib, cluster):
+def test_cluster_small_box_two_cells(oracle_lib, cuda_lib, cluster, lane):
     # 2 cells per axis at rc + skin: both images of the other cell are scanned
     import oracle
     s = displaced(liquid(nc=5, rho=0.95), 0.02, 3)
     o = to_oracle(s)
     pe_ref = o.compute_potential(manager=oracle.ALLPAIRS)
-    g = to_gpu(s, "mixed", cluster=cluster)
+    g = to_gpu(s, "mixed", cluster=cluster, lanes=cluster if lane else 1)
     assert g.stats()["cells"] == (2, 2, 2)
     pe, f = g.compute_potential()
     assert abs(pe - pe_ref) <= 1e-5 * abs(pe_ref)
@@ -107,7 +112,8 @@ def test_cluster_small_box_two_cells(oracle_lib, cuda_lib, cluster):
     assert _sets(off, idx) == [tuple(sorted(x)) for x in _sets(off_r, idx_r)]
 
 
-def test_cluster_batch_alone_equals_mix(cuda_lib):
+@pytest.mark.parametrize("lane", [False, True])
+def test_cluster_batch_alone_equals_mix(cuda_lib, lane):
     """An odd-sized replica and a liquid give bit-identical results alone and together."""
     from pis_gb300.batch import Batch
     a = liquid(nc=5, seed=21)
@@ -115,7 +121,7 @@ def test_cluster_batch_alone_equals_mix(cuda_lib):
     b = liquid(nc=6, rho=0.8, seed=22)
 
     def run(systems):
-        bt = Batch(4096, 4, 0, precision="mixed", cluster=4)
+        bt = Batch(4096, 4, 0, precision="mixed", cluster=4, lanes=4 if lane else 1)
         slots = [bt.admit(x["pos"], x["types"], x["masses"], x["h"], x["table"], 80, velocities=x["vel"])
                  for x in systems]
         bt.advance(80)
@@ -141,6 +147,9 @@ def test_cluster_option_checks(cuda_lib):
     with pytest.raises(PisError) as e:
         to_gpu(s, "mixed", cluster=3)
     assert e.value.name == "PIS_ERR_INVALID_ARGUMENT"
+    with pytest.raises(PisError) as e:
+        to_gpu(s, "mixed", cluster=4, lanes=2)
+    assert e.value.name in ("PIS_ERR_UNSUPPORTED", "PIS_ERR_INVALID_ARGUMENT")
 
 
 # ---- per-atom lists built per cluster (PIS_OPT_SCAN) -----------------------------------------

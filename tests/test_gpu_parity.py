@@ -229,3 +229,26 @@ def test_kernel_launch_counter_moves(liquid_melt):
     g.compute_potential()
     g.verlet_step_nve(0.005, 10)
     assert kernel_launches() - before >= 10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_set_state_reuses_pool_and_matches_fresh_context(liquid_melt, precision):
+    # a second state of the same shape is placed in the same device pool (memory and captured
+    # step graphs reused); its results must equal those of a fresh context bit for bit
+    g = to_gpu(liquid_melt, precision, list_kind="full")
+    g.compute_potential()
+    g.verlet_step_nve(0.005, 20)
+    s2 = displaced(liquid_melt, 0.01, 9)
+    g.set_state(s2["pos"], s2["types"], s2["masses"], s2["h"], velocities=s2["vel"])
+    pe, f = g.compute_potential()
+    e = g.verlet_step_nve(0.005, 30)
+    out = (np.empty((len(s2["pos"]), 3)), np.empty((len(s2["pos"]), 3)), np.empty((len(s2["pos"]), 3)))
+    p, v, fo = g.get_state(out=out)
+    assert p is out[0] and v is out[1] and fo is out[2]
+    fresh = to_gpu(s2, precision, list_kind="full")
+    pe_f, f_f = fresh.compute_potential()
+    e_f = fresh.verlet_step_nve(0.005, 30)
+    p_f, v_f, fo_f = fresh.get_state()
+    assert pe == pe_f and np.array_equal(f, f_f) and np.array_equal(e, e_f)
+    assert np.array_equal(p, p_f) and np.array_equal(v, v_f) and np.array_equal(fo, fo_f)
+    assert g.stats()["steps"] == 30
