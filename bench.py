@@ -52,6 +52,9 @@ def parse():
     p.add_argument("--serve-jobs", type=int, default=32)
     p.add_argument("--no-drift", action="store_true", help="skip the 10^4-step energy-drift runs")
     p.add_argument("--drift-steps", type=int, default=10000)
+    p.add_argument("--mixed-options", default=None,
+                   help='kernel variant of the mixed path as JSON (GpuContext keywords, e.g. '
+                        '\'{"batch": 8, "tma": true}\'); default: the autotuner\'s choice')
     return p.parse_args()
 
 
@@ -230,7 +233,10 @@ def main():
     mix.close()
     # kernel shape from the project's autotuner (cached per GPU / precision / size class)
     from pis_gb300.autotune import tune_system
-    tuned = tune_system(TABLE, 1, melt_pos, types, [1.0], h, melt_vel, precision="mixed", skin=SKIN, dt=DT)
+    if args.mixed_options:
+        tuned = json.loads(args.mixed_options)
+    else:
+        tuned = tune_system(TABLE, 1, melt_pos, types, [1.0], h, melt_vel, precision="mixed", skin=SKIN, dt=DT)
     mix = GpuContext(TABLE, 1, skin=SKIN, precision="mixed", **tuned)
     mix.set_state(melt_pos, types, [1.0], h, velocities=melt_vel)
     mix.compute_potential(want_forces=False)
