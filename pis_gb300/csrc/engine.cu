@@ -322,10 +322,10 @@ __global__ void k_integrate1(const DP P) {
         y = wrap_axis(y, sp.h[1], sp.hinv[1]);
         z = wrap_axis(z, sp.h[2], sp.hinv[2]);
     } else {
-        const double hdt2 = 0.5 * sp.dt2;
-        x = p.x + fma(v.x, sp.dt, a.x * hdt2);
-        y = p.y + fma(v.y, sp.dt, a.y * hdt2);
-        z = p.z + fma(v.z, sp.dt, a.z * hdt2);
+        // x + v dt + a dt^2/2 as two fused multiply-adds per axis
+        x = fma(a.x, sp.hdt2, fma(v.x, sp.dt, p.x));
+        y = fma(a.y, sp.hdt2, fma(v.y, sp.dt, p.y));
+        z = fma(a.z, sp.hdt2, fma(v.z, sp.dt, p.z));
         x = wrap_if_out(x, sp.h[0]);
         y = wrap_if_out(y, sp.h[1]);
         z = wrap_if_out(z, sp.h[2]);
@@ -1683,19 +1683,20 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
                 v.y = __dadd_rn(v.y, __dmul_rn(__dmul_rn(__dadd_rn(a.y, by), 0.5), sp.dt));
                 v.z = __dadd_rn(v.z, __dmul_rn(__dmul_rn(__dadd_rn(a.z, bz), 0.5), sp.dt));
             } else {
-                const double hdt = 0.5 * sp.dt;
-                v.x = fma(a.x + bx, hdt, v.x);
-                v.y = fma(a.y + by, hdt, v.y);
-                v.z = fma(a.z + bz, hdt, v.z);
+                v.x = fma(a.x + bx, sp.hdt, v.x);
+                v.y = fma(a.y + by, sp.hdt, v.y);
+                v.z = fma(a.z + bz, sp.hdt, v.z);
             }
             P.vel[cur][i] = v;
         }
         P.acc[cur][i] = make_double4_32a(bx, by, bz, a.w);
-        ke = __dmul_rn(__dmul_rn(0.5, m), norm2_ref(v.x, v.y, v.z));
+        // m |v|^2 here and the factor 1/2 on the block sum: halving is exact, so this equals the
+        // sum of (0.5 m) |v|^2 (properties.rs:17-24) bit for bit
+        ke = EXACT ? __dmul_rn(m, norm2_ref(v.x, v.y, v.z)) : m * fma(v.x, v.x, fma(v.y, v.y, v.z * v.z));
         if (st.want_virial) p = P.pos[cur][i];
     }
     double tot = block_sum<256>(ke, sh);
-    if (threadIdx.x == 0) P.ke_part[blockIdx.x] = tot;
+    if (threadIdx.x == 0) P.ke_part[blockIdx.x] = 0.5 * tot;
     if (st.want_virial) {
         double r[3] = {p.x, p.y, p.z}, g[3] = {f.x, f.y, f.z};
 #pragma unroll
@@ -2328,6 +2329,8 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     p.half_skin2 = 0.25 * d.skin * d.skin;
     p.dt = d.dt;
     p.dt2 = d.dt * d.dt;
+    p.hdt = 0.5 * p.dt;
+    p.hdt2 = 0.5 * p.dt2;
     double rl = rlist * (1.0 + 1e-5);
     p.frlist2 = (float)(rl * rl);
     // chunks
@@ -2478,6 +2481,8 @@ pis_status Engine::set_dt(int slot, double dt, std::string& err) {
     if (p.dt == dt) return PIS_OK;
     p.dt = dt;
     p.dt2 = dt * dt;
+    p.hdt = 0.5 * p.dt;
+    p.hdt2 = 0.5 * p.dt2;
     pis_status st = check(cudaMemcpyAsync(d_->sp + slot, &p, sizeof(SysParams), cudaMemcpyHostToDevice, stream_),
                           "params", err);
     if (st) return st;

@@ -55,6 +55,7 @@ struct SysParams {
     double cs[3];      // cell edge
     double half_skin2; // (skin / 2)^2
     double dt, dt2;    // dt, dt*dt
+    double hdt, hdt2;  // dt/2, dt*dt/2 (mixed-path integrators)
     float fcs[3];
     float frlist2;     // FP32 list radius squared, padded so the FP32 test is a superset
     float fsub[3];     // 4 / cell edge: sub-cell index scale of the in-cell atom order
