@@ -2008,14 +2008,6 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     }
     pis_status st = check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream", err);
     if (st) return st;
-    {
-        int dev = 0, sms = 0;
-        st = check(cudaGetDevice(&dev), "device", err);
-        if (st) return st;
-        st = check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device", err);
-        if (st) return st;
-        num_sms_ = sms > 0 ? sms : 1;
-    }
 
     const size_t NA = (size_t)opt.max_atoms, NC = (size_t)max_cells, NCH = (size_t)max_chunks_,
                  NS = (size_t)opt.max_slots, NCL = (size_t)max_clusters_, NCC = (size_t)max_cchunks_;

@@ -186,7 +186,6 @@ class Engine {
     int64_t max_chunks_ = 0;
     int64_t max_clusters_ = 0, clpad_ = 0, ccap_ = 0, max_cchunks_ = 0;
     int clm_ = 0;  // atoms per cluster of the cluster table (0: no table)
-    int num_sms_ = 1;
     cudaStream_t stream_ = nullptr;
     std::vector<SysParams> hp_;
     std::vector<int> slot_tab_size_;

@@ -64,3 +64,46 @@ def test_product_never_imports_oracle():
                 text = open(os.path.join(dirpath, f)).read()
                 assert "import oracle" not in text and "from oracle" not in text, f
                 assert "liboracle" not in text, f
+
+
+def _ctx(lib, precision):
+    from pis_gb300 import _ffi
+    h = ctypes.c_void_p()
+    pair = (_ffi.LJPair * 1)(_ffi.LJPair(1, 1, 1.0, 1.0, 2.5, 1))
+    assert lib.pis_gpu_create(pair, 1, 1, 0.3, precision, ctypes.byref(h)) == 0
+    return h
+
+
+@pytest.mark.parametrize("precision,flags,status", [
+    (1, 0, 0),                                      # defaults
+    (1, 4 | (8 << 16), 0),                          # bulk-copy list stream, 8 rows per stage
+    (1, (4 << 24) | (4 << 8), 0),                   # clusters of 4, a lane per member
+    (1, (2 << 24) | (2 << 8), 0),                   # clusters of 2, a lane per member
+    (1, 4 << 28, 0),                                # two-stage build
+    (0, 4 << 28, 0),                                # two-stage build, FP64 path
+    (0, 4, 26),                                     # bulk-copy stream needs the mixed path
+    (1, 4 | (4 << 8), 26),                          # ... and one thread per atom
+    (0, 4 << 24, 26),                               # cluster lists need the mixed path
+    (1, (4 << 24) | (2 << 8), 1),                   # 2 lanes only with clusters of 2
+    (1, 3 << 24, 1),                                # clusters of 3
+    (1, 3 << 28, 1),                                # build clusters of 3
+    (1, 5 << 16, 1),                                # batch of 5
+    (1, 1 << 7, 1),                                 # unknown flag bit
+])
+def test_set_options_validates_without_gpu(precision, flags, status):
+    from pis_gb300 import _ffi
+    lib = _ffi.lib()
+    h = _ctx(lib, precision)
+    assert lib.pis_gpu_set_options(h, 0, flags) == status
+    lib.pis_gpu_destroy(h)
+
+
+def test_option_flags_match_header():
+    from pis_gb300 import _ffi
+    text = open(os.path.join(ROOT, "include", "pis_gpu.h")).read()
+    assert "#define PIS_OPT_LIST_TMA 4" in text and "PIS_OPT_CLUSTER(m) ((m) << 24)" in text
+    assert "PIS_OPT_SCAN(m) ((m) << 28)" in text and "PIS_ERR_TIMEOUT = 27" in text
+    assert _ffi.option_flags(tma=True, batch=8) == 4 | (8 << 16)
+    assert _ffi.option_flags(cluster=4, lanes=4, scan=0) == (4 << 24) | (4 << 8)
+    assert _ffi.option_flags(scan=4, mixed_kahan=True) == (4 << 28) | 2
+    assert _ffi.STATUS_NAMES[27] == "PIS_ERR_TIMEOUT"
