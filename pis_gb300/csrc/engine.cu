@@ -1840,6 +1840,14 @@ __global__ void k_scale_pos(const DP P, int slot, double oh0, double oh1, double
     P.pos[cur][i] = p;
 }
 
+// Condition of a step's rebuild node: some slot rebuilds in this step (the device-wide word).
+// Also counts executed rebuild bodies (ctl[2..3], 64 bits) for the launch counter.
+__global__ void k_set_rebuild_cond(const DP P, cudaGraphConditionalHandle h) {
+    const bool go = P.ctl[0] != 0;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+    if (go) ++*reinterpret_cast<unsigned long long*>(P.ctl + 2);
+}
+
 // Upload of one slot's state. The caller's arrays (x,y,z per atom, 1-based types) are copied as
 // they are into the slot's range of the idle buffer set (pos[1], vel[1], acc[1], id[1]: nothing
 // lives there before the first rebuild) and converted here: type bits in pos.w, the type's mass in
@@ -1904,7 +1912,7 @@ __global__ void k_store_slot(const DP P, int64_t a0, int n, int cur, int want_po
 // ---------------------------------------------------------------------------------------------
 #define LAUNCH(kern, grid, block, ...)                                \
     do {                                                               \
-        kern<<<(grid), (block), 0, stream_>>>(__VA_ARGS__);           \
+        kern<<<(grid), (block), 0, ls_>>>(__VA_ARGS__);               \
         g_launches.fetch_add(1);                                       \
     } while (0)
 
@@ -1918,6 +1926,7 @@ Engine::~Engine() {
     if (d_ && d_->keep) cudaFree(d_->keep);
     if (mem_) cudaFree(mem_);
     if (stream_) cudaStreamDestroy(stream_);
+    if (side_) cudaStreamDestroy(side_);
     delete d_;
 }
 
@@ -2008,6 +2017,9 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     }
     pis_status st = check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream", err);
     if (st) return st;
+    st = check(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking), "stream", err);
+    if (st) return st;
+    ls_ = stream_;
 
     const size_t NA = (size_t)opt.max_atoms, NC = (size_t)max_cells, NCH = (size_t)max_chunks_,
                  NS = (size_t)opt.max_slots, NCL = (size_t)max_clusters_, NCC = (size_t)max_cchunks_;
@@ -2466,7 +2478,11 @@ pis_status Engine::rebuild_block_map(std::string& err) {
     return st;
 }
 
-pis_status Engine::sync(std::string& err) { return check(cudaStreamSynchronize(stream_), "stream sync", err); }
+pis_status Engine::sync(std::string& err) {
+    pis_status st = check(cudaStreamSynchronize(stream_), "stream sync", err);
+    if (!st) account_body_launches();
+    return st;
+}
 
 pis_status Engine::set_dt(int slot, double dt, std::string& err) {
     SysParams& p = hp_[slot];
@@ -2619,9 +2635,9 @@ void Engine::launch_build(int r) {
     const unsigned gc = (unsigned)max_cchunks_, ga = (unsigned)max_chunks_;
     if (opt_.cluster) {
         if (opt_.cluster == 2)
-            k_build_cl<2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, 0);
+            k_build_cl<2><<<gc, CL_THREADS, 0, ls_>>>(*d_, r, 0);
         else
-            k_build_cl<4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, 0);
+            k_build_cl<4><<<gc, CL_THREADS, 0, ls_>>>(*d_, r, 0);
         g_launches.fetch_add(1);
         return;
     }
@@ -2629,26 +2645,26 @@ void Engine::launch_build(int r) {
         // two-stage per-atom build: cluster union lists, filtered per member; slots with a
         // two-cell axis use the generic kernel
         if (clm_ == 2) {
-            k_build_cl<2><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, 1);
+            k_build_cl<2><<<gc, CL_THREADS, 0, ls_>>>(*d_, r, 1);
             if (half_)
-                k_filter_cl<true, 2><<<gc * 2, CL_THREADS, 0, stream_>>>(*d_, r);
+                k_filter_cl<true, 2><<<gc * 2, CL_THREADS, 0, ls_>>>(*d_, r);
             else
-                k_filter_cl<false, 2><<<gc * 2, CL_THREADS, 0, stream_>>>(*d_, r);
+                k_filter_cl<false, 2><<<gc * 2, CL_THREADS, 0, ls_>>>(*d_, r);
         } else {
-            k_build_cl<4><<<gc, CL_THREADS, 0, stream_>>>(*d_, r, 1);
+            k_build_cl<4><<<gc, CL_THREADS, 0, ls_>>>(*d_, r, 1);
             if (half_)
-                k_filter_cl<true, 4><<<gc * 4, CL_THREADS, 0, stream_>>>(*d_, r);
+                k_filter_cl<true, 4><<<gc * 4, CL_THREADS, 0, ls_>>>(*d_, r);
             else
-                k_filter_cl<false, 4><<<gc * 4, CL_THREADS, 0, stream_>>>(*d_, r);
+                k_filter_cl<false, 4><<<gc * 4, CL_THREADS, 0, ls_>>>(*d_, r);
         }
         if (half_)
-            k_build1_generic<true><<<ga, 256, 0, stream_>>>(*d_, r);
+            k_build1_generic<true><<<ga, 256, 0, ls_>>>(*d_, r);
         else
-            k_build1_generic<false><<<ga, 256, 0, stream_>>>(*d_, r);
+            k_build1_generic<false><<<ga, 256, 0, ls_>>>(*d_, r);
         g_launches.fetch_add(3);
         return;
     }
-#define PIS_CALL(L) launch_build_t<L>(*d_, half_, ch, stream_, r)
+#define PIS_CALL(L) launch_build_t<L>(*d_, half_, ch, ls_, r)
     PIS_LPA_DISPATCH(opt_.lpa, PIS_CALL)
 #undef PIS_CALL
 }
@@ -2727,7 +2743,10 @@ void Engine::enqueue_step(bool respect, cudaEvent_t* ev) {
     else
         LAUNCH(k_integrate1<false>, (unsigned)max_chunks_, opt_.blk, P);
     if (ev) cudaEventRecordWithFlags(ev[1], stream_, cudaEventRecordExternal);
-    enqueue_rebuild(respect);
+    if (cond_step_)
+        cond_error_ = cond_error_ ? cond_error_ : enqueue_rebuild_conditional(respect);
+    else
+        enqueue_rebuild(respect);
     if (ev) cudaEventRecordWithFlags(ev[2], stream_, cudaEventRecordExternal);
     if (mixed)
         launch_force_mixed(r);
@@ -2754,6 +2773,58 @@ void Engine::enqueue_potential(int only) {
     else
         launch_force_fp64(0);
     LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 1);
+}
+
+// Inside a stream capture of stream_: a 1-thread kernel sets the condition from the rebuild word,
+// then a conditional IF node whose body (the rebuild kernels, captured on side_) runs only when
+// some slot rebuilds. On the ~8 steps in 9 without a rebuild the step then launches no rebuild
+// kernel at all.
+pis_status Engine::enqueue_rebuild_conditional(bool respect) {
+    cudaStreamCaptureStatus cs;
+    unsigned long long id = 0;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* edges = nullptr;
+    size_t nd = 0;
+    if (cudaStreamGetCaptureInfo(stream_, &cs, &id, &g, &deps, &edges, &nd) != cudaSuccess ||
+        cs != cudaStreamCaptureStatusActive)
+        return PIS_ERR_CUDA;
+    cudaGraphConditionalHandle h;
+    if (cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) return PIS_ERR_CUDA;
+    k_set_rebuild_cond<<<1, 1, 0, stream_>>>(*d_, h);
+    g_launches.fetch_add(1);
+    if (cudaStreamGetCaptureInfo(stream_, &cs, &id, &g, &deps, &edges, &nd) != cudaSuccess) return PIS_ERR_CUDA;
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, g, deps, edges, nd, &cp) != cudaSuccess) return PIS_ERR_CUDA;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if (cudaStreamUpdateCaptureDependencies(stream_, &node, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess)
+        return PIS_ERR_CUDA;
+    if (cudaStreamBeginCaptureToGraph(side_, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return PIS_ERR_CUDA;
+    const int64_t before = g_launches.load();
+    ls_ = side_;
+    enqueue_rebuild(respect);
+    ls_ = stream_;
+    const int64_t n_body = g_launches.load() - before;
+    g_launches.fetch_sub(n_body);  // counted when a body actually runs (account_body_launches)
+    body_kernels_ = n_body;
+    cudaGraph_t out = nullptr;
+    if (cudaStreamEndCapture(side_, &out) != cudaSuccess) return PIS_ERR_CUDA;
+    return PIS_OK;
+}
+
+void Engine::account_body_launches() {
+    if (!body_kernels_ || !d_) return;
+    unsigned long long n = 0;
+    if (cudaMemcpy(&n, d_->ctl + 2, sizeof(n), cudaMemcpyDeviceToHost) != cudaSuccess) return;
+    if (n > body_seen_) {
+        g_launches.fetch_add((int64_t)(n - body_seen_) * body_kernels_);
+        body_seen_ = n;
+    }
 }
 
 pis_status Engine::compute_potential(std::string& err) { return compute_potential_slot(-1, err); }
@@ -2807,19 +2878,33 @@ pis_status Engine::run(int64_t k, std::string& err) {
                     if (st) return st;
                 }
             }
-            cudaGraph_t graph;
-            st = check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture", err);
-            if (st) return st;
-            int64_t before = g_launches.load();
-            for (int64_t q = 0; q < g; ++q) enqueue_step(true, instrument_ ? rec.ev.data() + 6 * q : nullptr);
-            int64_t captured = g_launches.load() - before;
-            g_launches.fetch_sub(captured);
-            kernels_per_step_ = captured / g;
-            st = check(cudaStreamEndCapture(stream_, &graph), "capture", err);
-            if (st) return st;
-            st = check(cudaGraphInstantiate(&rec.exec, graph, 0), "instantiate", err);
-            cudaGraphDestroy(graph);
-            if (st) return st;
+            cudaGraph_t graph = nullptr;
+            for (int attempt = 0; attempt < 2; ++attempt) {
+                st = check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture", err);
+                if (st) return st;
+                int64_t before = g_launches.load();
+                cond_step_ = cond_rebuild_;
+                cond_error_ = PIS_OK;
+                for (int64_t q = 0; q < g; ++q) enqueue_step(true, instrument_ ? rec.ev.data() + 6 * q : nullptr);
+                cond_step_ = false;
+                int64_t captured = g_launches.load() - before;
+                g_launches.fetch_sub(captured);
+                kernels_per_step_ = captured / g;
+                cudaError_t ce = cudaStreamEndCapture(stream_, &graph);
+                if (ce == cudaSuccess && cond_error_ == PIS_OK) {
+                    ce = cudaGraphInstantiate(&rec.exec, graph, 0);
+                    cudaGraphDestroy(graph);
+                    if (ce == cudaSuccess) break;
+                } else if (graph) {
+                    cudaGraphDestroy(graph);
+                }
+                graph = nullptr;
+                cudaGetLastError();
+                if (!cond_rebuild_) return check(ce == cudaSuccess ? cudaErrorUnknown : ce, "capture", err);
+                // conditional nodes unavailable: capture the plain step sequence instead
+                cond_rebuild_ = false;
+                body_kernels_ = 0;
+            }
             it = graphs_.emplace(key, rec).first;
         }
         st = check(cudaGraphLaunch(it->second.exec, stream_), "graph launch", err);

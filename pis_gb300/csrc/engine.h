@@ -170,6 +170,11 @@ class Engine {
     pis_status rebuild_block_map(std::string& err);
     void enqueue_step(bool respect_steps, cudaEvent_t* ev);
     void enqueue_rebuild(bool respect_steps);
+    // The rebuild kernels of a captured step inside a conditional graph node that runs only when
+    // some slot rebuilds in that step (the condition is set on the device).
+    pis_status enqueue_rebuild_conditional(bool respect_steps);
+    // Conditional rebuild bodies executed since the last call, counted on the device.
+    void account_body_launches();
     void enqueue_potential(int only);
     void launch_force_fp64(int respect_steps);
     void launch_force_mixed(int respect_steps);
@@ -186,6 +191,14 @@ class Engine {
     int64_t max_chunks_ = 0;
     int64_t max_clusters_ = 0, clpad_ = 0, ccap_ = 0, max_cchunks_ = 0;
     int clm_ = 0;  // atoms per cluster of the cluster table (0: no table)
+    cudaStream_t ls_ = nullptr;    // stream the rebuild kernels are launched on (stream_, or side_ while a
+                                   // conditional body is captured)
+    cudaStream_t side_ = nullptr;  // capture stream of conditional bodies
+    bool cond_rebuild_ = true;     // step graphs skip the rebuild kernels through a conditional node
+    int64_t body_kernels_ = 0;     // kernels in one conditional rebuild body
+    uint64_t body_seen_ = 0;       // bodies already counted into the launch counter
+    bool cond_step_ = false;       // a capture with conditional rebuild nodes is in progress
+    pis_status cond_error_ = PIS_OK;
     cudaStream_t stream_ = nullptr;
     std::vector<SysParams> hp_;
     std::vector<int> slot_tab_size_;
