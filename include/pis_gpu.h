@@ -102,6 +102,12 @@ pis_status pis_gpu_create(const pis_lj_pair* table, int32_t n_pairs, int32_t n_t
 #define PIS_OPT_LIST_TMA 4 /* mixed path, thread per atom: the neighbour list is streamed into shared
                             * memory by bulk (TMA) copies several batches ahead of the pair loop;
                             * PIS_OPT_BATCH(8 or 16) sets the rows per copy stage (4 counts as 8) */
+#define PIS_OPT_TILE 8 /* mixed path, thread per atom: the neighbour cells of each 256-atom chunk are
+                        * staged in shared memory by bulk (TMA) copies and the pair loop gathers
+                        * neighbour positions from there */
+#define PIS_OPT_PLAIN_GRAPHS 16 /* step graphs launch the list-rebuild kernels on every step (they exit at
+                                 * once when nothing rebuilds) instead of behind a conditional graph node:
+                                 * for profilers that cannot look inside graphs holding conditional nodes */
 #define PIS_OPT_CLUSTER(m) ((m) << 24) /* mixed path, neighbour-list shape: 1 = one list per atom,
                                         * 2 or 4 = one list per cluster of m spatially adjacent atoms
                                         * of a cell (each neighbour read serves m pairs);

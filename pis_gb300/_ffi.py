@@ -22,10 +22,12 @@ PRECISION = {"fp64": 0, "mixed": 1}
 LIST_KIND = {"default": 0, "half": 1, "full": 2}
 
 
-def option_flags(fp64_fast=False, mixed_kahan=False, lanes=0, batch=0, tma=False, cluster=0, scan=0) -> int:
+def option_flags(fp64_fast=False, mixed_kahan=False, lanes=0, batch=0, tma=False, cluster=0, scan=0,
+                 tiles=False, plain_graphs=False) -> int:
     """PIS_OPT_* bits of include/pis_gpu.h for the variant knobs."""
-    return ((1 if fp64_fast else 0) | (2 if mixed_kahan else 0) | (4 if tma else 0) | (int(lanes) << 8)
-            | (int(batch) << 16) | (int(cluster) << 24) | (int(scan) << 28))
+    return ((1 if fp64_fast else 0) | (2 if mixed_kahan else 0) | (4 if tma else 0) | (8 if tiles else 0)
+            | (16 if plain_graphs else 0) | (int(lanes) << 8) | (int(batch) << 16) | (int(cluster) << 24)
+            | (int(scan) << 28))
 
 
 class PisError(RuntimeError):

@@ -1029,14 +1029,12 @@ struct MixLJ {
 // The FP32 LJ terms of one batch of list entries against atom i (cell-relative coordinates pi):
 // gathers of every neighbour's prel first (all in flight together), then the pair math, summed
 // into the accumulator's batch sums.
-// SELF: the list may hold atom i itself (cluster lists), masked by r^2 > 0.
+// SELF: the list may hold atom i itself (cluster lists), masked by r^2 > 0. pj: the entries'
+// neighbour positions, already gathered.
 template <bool ONE, int NB, int ACC, bool SELF = false>
-__device__ __forceinline__ void mixed_pairs(const uint32_t (&ent)[NB], const float4* __restrict__ prel,
-                                            const float4& pi, const float4* shift, const LJDev* tab,
-                                            const MixLJ& P0, MixAcc<ACC>& a) {
-    float4 pj[NB];
-#pragma unroll
-    for (int b = 0; b < NB; ++b) pj[b] = __ldg(prel + (ent[b] & JMASK));
+__device__ __forceinline__ void mixed_pairs_math(const uint32_t (&ent)[NB], const float4 (&pj)[NB], const float4& pi,
+                                                 const float4* shift, const LJDev* tab, const MixLJ& P0,
+                                                 MixAcc<ACC>& a) {
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
         const float4 sv = shift[ent[b] >> JBITS];
@@ -1067,6 +1065,16 @@ __device__ __forceinline__ void mixed_pairs(const uint32_t (&ent)[NB], const flo
         a.pz = fmaf(-c, dz, a.pz);
         a.pe += u;
     }
+}
+
+template <bool ONE, int NB, int ACC, bool SELF = false>
+__device__ __forceinline__ void mixed_pairs(const uint32_t (&ent)[NB], const float4* __restrict__ prel,
+                                            const float4& pi, const float4* shift, const LJDev* tab,
+                                            const MixLJ& P0, MixAcc<ACC>& a) {
+    float4 pj[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) pj[b] = __ldg(prel + (ent[b] & JMASK));
+    mixed_pairs_math<ONE, NB, ACC, SELF>(ent, pj, pi, shift, tab, P0, a);
 }
 
 __device__ __forceinline__ MixLJ mix_lj_load(const LJDev& L) {
@@ -1252,6 +1260,166 @@ __global__ void __launch_bounds__(256, KB <= 8 ? 4 : 2) k_force_mixed_tma(const 
     if (live) P.frc[i] = make_double4_32a(acc.fx, acc.fy, acc.fz, 0.0);
     double tot = block_sum<256>(acc.e, sh);
     if (threadIdx.x == 0) P.pe_part[blockIdx.x] = tot;
+}
+
+// Mixed precision forces with the neighbour-cell tiles staged in shared memory by bulk copies
+// (cp.async.bulk, the TMA engine's untiled mode). Atoms are sorted by cell with x fastest, so when
+// a 256-atom chunk lies in one cell row its neighbours lie in 9 rows (y, z = home +- 1), each a
+// contiguous run of cells [xa - 1, xb + 1] - one contiguous atom range - plus, where the chunk
+// touches x = 0 or x = nx - 1, the single wrapped cell at the other end of each row. Thread 0
+// copies these <= 27 pieces of cell-relative positions into shared memory with one mbarrier
+// counting the bytes. A list entry j | code then lives in shared memory at j + delta, delta
+// depending only on the entry's piece - given by its image code and by whether the owning atom sits
+// at a row end (x = 0 or nx - 1, where the -1 or +1 neighbour is the wrapped cell) - so delta is
+// carried in the w field of the image-shift table (3 x 64 entries), and the gather becomes one
+// shared-memory load with no extra instruction. The pair arithmetic is k_force_mixed's. Chunks
+// that span two rows, or whose tiles exceed the buffer, gather from global memory as usual; the
+// mbarrier wait is bounded (on expiry: FLAG_TIMEOUT, and the chunk gathers from global memory).
+constexpr int TILE_ATOMS = 3328;  // 52 KB of float4 per block: four blocks per SM
+
+template <int ACC, bool ONE>
+__global__ void __launch_bounds__(256) k_force_mixed_tile(const DP P, int step_mode) {
+    extern __shared__ __align__(16) float4 tile[];  // TILE_ATOMS
+    __shared__ float4 shd[3 * 64];                 // (wrap state, code) -> image shift, delta bits in w
+    __shared__ int psrc[27], plen[27], poff[27];   // pieces: first atom, atoms, shared-memory offset
+    __shared__ int use_tile;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ double sh[32];
+    int s, i;
+    const bool live = atom_of(P, s, i);
+    if (s < 0) return;  // uniform per block (one slot per chunk)
+    if (!slot_runs(P, s, step_mode)) return;
+    const SysParams& sp = P.sp[s];
+    SysState& st = P.st[s];
+    const int t = threadIdx.x;
+    const int nx = sp.nc[0], ny = sp.nc[1], nz = sp.nc[2];
+    const int first = P.blk_first[blockIdx.x];
+    const int cnt = min(256, (int)(sp.a0 + sp.n) - first);
+    if (t == 0) {
+        int ok = 0;
+        if (nx >= 3 && ny >= 3 && nz >= 3) {
+            const int la = P.cellof[first], lb = P.cellof[first + cnt - 1];
+            const int xa = la % nx, ya = (la / nx) % ny, za = la / (nx * ny);
+            const int xb = lb % nx, yb = (lb / nx) % ny, zb = lb / (nx * ny);
+            if (ya == yb && za == zb && !(xa == 0 && xb == nx - 1)) {
+                const int32_t* cs = P.cell_start + sp.c0;
+                const int xl = max(xa - 1, 0), xh = min(xb + 1, nx - 1);
+                int off = 0;
+                for (int oz = -1; oz <= 1; ++oz)
+                    for (int oy = -1; oy <= 1; ++oy) {
+                        const int row = (oz + 1) * 3 + (oy + 1);
+                        const int rb = (wrapc(za + oz, nz) * ny + wrapc(ya + oy, ny)) * nx;
+                        psrc[row] = cs[rb + xl];
+                        plen[row] = cs[rb + xh + 1] - cs[rb + xl];
+                        poff[row] = off;
+                        off += plen[row];
+                        psrc[9 + row] = cs[rb + nx - 1];  // wrapped -1 neighbour of x = 0
+                        plen[9 + row] = xa == 0 ? cs[rb + nx] - cs[rb + nx - 1] : 0;
+                        poff[9 + row] = off;
+                        off += plen[9 + row];
+                        psrc[18 + row] = cs[rb];  // wrapped +1 neighbour of x = nx - 1
+                        plen[18 + row] = xb == nx - 1 ? cs[rb + 1] - cs[rb] : 0;
+                        poff[18 + row] = off;
+                        off += plen[18 + row];
+                    }
+                ok = off <= TILE_ATOMS;
+            }
+        }
+        use_tile = ok;
+        if (ok) {
+            mbar_init(&bar, 1);
+            mbar_fence_init();
+        }
+    }
+    __syncthreads();
+    const bool tiled = use_tile != 0;
+    if (tiled && t == 0) {
+        uint32_t bytes = 0;
+        for (int p = 0; p < 27; ++p) bytes += (uint32_t)plen[p] * 16u;
+        mbar_arrive_tx(&bar, bytes);
+        for (int p = 0; p < 27; ++p)
+            if (plen[p] > 0) bulk_g2s(tile + poff[p], P.prel + psrc[p], (uint32_t)plen[p] * 16u, &bar);
+    }
+    if (t < 3 * 64) {
+        const int c = t & 63, w = t >> 6;
+        const int bx = c & 3, by = (c >> 2) & 3, bz = (c >> 4) & 3;
+        const bool pad = bx == 3 || by == 3 || bz == 3;
+        const int ox = bx == 1 ? 1 : (bx == 2 ? -1 : 0);
+        const int oy = by == 1 ? 1 : (by == 2 ? -1 : 0);
+        const int oz = bz == 1 ? 1 : (bz == 2 ? -1 : 0);
+        int delta = 0;
+        if (tiled) {
+            // padding entries point at the owning atom, which is in the home row's main piece
+            const int row = pad ? 4 : (oz + 1) * 3 + (oy + 1);
+            int p = row;
+            if (!pad && w == 1 && ox == -1) p = 9 + row;
+            if (!pad && w == 2 && ox == 1) p = 18 + row;
+            delta = poff[p] - psrc[p];
+        }
+        shd[t] = pad ? make_float4(1e18f, 1e18f, 1e18f, __int_as_float(delta))
+                     : make_float4(ox * sp.fcs[0], oy * sp.fcs[1], oz * sp.fcs[2], __int_as_float(delta));
+    }
+    __syncthreads();
+    bool got = tiled && mbar_wait(&bar, 0u);
+    if (tiled && !got) atomicOr(&st.flags, FLAG_TIMEOUT);
+    // every thread uses the tile only if the whole block saw it arrive
+    got = __syncthreads_and(got ? 1 : 0) != 0;
+    MixAcc<ACC> acc;
+    if (live) {
+        const float4* __restrict__ prel = P.prel;
+        const float4 pi = prel[i];
+        const int ti = __float_as_int(pi.w);
+        const LJDev* tab = P.tab + sp.tab0 + ti * sp.nt;
+        const MixLJ P0 = mix_lj_load(tab[0]);
+        const int cx = P.cellof[i] % nx;
+        const float4* shift = shd + (got ? 64 * (cx == 0 ? 1 : (cx == nx - 1 ? 2 : 0)) : 0);
+        const int nn = P.nn[i];
+        const uint32_t row32 = (uint32_t)P.npad;
+        const uint32_t* __restrict__ nbp = P.nbr + i;
+        const uint32_t pad = (uint32_t)i | (63u << JBITS);
+        constexpr int NB = 4;
+        int since = 0;
+        uint32_t qoff = 0;
+        for (int k0 = 0; k0 < nn; k0 += NB) {
+            uint32_t ent[NB];
+            if (k0 + NB <= nn) {
+#pragma unroll
+                for (int b = 0; b < NB; ++b) ent[b] = load_list_word(nbp + qoff + (uint32_t)b * row32);
+            } else {
+#pragma unroll
+                for (int b = 0; b < NB; ++b)
+                    ent[b] = (k0 + b < nn) ? load_list_word(nbp + qoff + (uint32_t)b * row32) : pad;
+            }
+            qoff += (uint32_t)NB * row32;
+            float4 pj[NB];
+            if (got) {
+#pragma unroll
+                for (int b = 0; b < NB; ++b)
+                    pj[b] = tile[(int)(ent[b] & JMASK) + __float_as_int(shift[ent[b] >> JBITS].w)];
+            } else {
+#pragma unroll
+                for (int b = 0; b < NB; ++b) pj[b] = __ldg(prel + (ent[b] & JMASK));
+            }
+            mixed_pairs_math<ONE, NB, ACC>(ent, pj, pi, shift, tab, P0, acc);
+            since += NB;
+            if (since >= MIX_FLUSH) {
+                acc.fold();
+                since = 0;
+            }
+        }
+        acc.finish();
+        P.frc[i] = make_double4_32a(acc.fx, acc.fy, acc.fz, 0.0);
+    }
+    // no copy may still be writing into shared memory when the block exits
+    if (tiled && !got && t == 0) mbar_wait(&bar, 0u);
+    double tot = block_sum<256>(acc.e, sh);
+    if (threadIdx.x == 0) P.pe_part[blockIdx.x] = tot;
+}
+
+template <int ACC, bool ONE>
+static cudaError_t allow_tile_smem() {
+    return cudaFuncSetAttribute(k_force_mixed_tile<ACC, ONE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(TILE_ATOMS * sizeof(float4)));
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1971,6 +2139,18 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         pis_status st0 = check(allow_all_mixed_tma_smem(), "shared-memory attribute", err);
         if (st0) return st0;
     }
+    if (opt.cell_tiles && (opt.precision != PIS_PRECISION_MIXED || opt.lpa != 1 || opt.list_tma || opt.cluster)) {
+        err = "neighbour-cell tiles are a variant of the mixed, thread-per-atom force kernel";
+        return PIS_ERR_UNSUPPORTED;
+    }
+    if (opt.cell_tiles) {
+        cudaError_t e = allow_tile_smem<0, true>();
+        if (e == cudaSuccess) e = allow_tile_smem<0, false>();
+        if (e == cudaSuccess) e = allow_tile_smem<1, true>();
+        if (e == cudaSuccess) e = allow_tile_smem<1, false>();
+        pis_status st0 = check(e, "shared-memory attribute", err);
+        if (st0) return st0;
+    }
     if (opt.cluster != 0 && opt.cluster != 2 && opt.cluster != 4) {
         err = "atoms per cluster must be 2 or 4";
         return PIS_ERR_INVALID_ARGUMENT;
@@ -2020,6 +2200,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     st = check(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking), "stream", err);
     if (st) return st;
     ls_ = stream_;
+    cond_rebuild_ = !opt.plain_graphs;
 
     const size_t NA = (size_t)opt.max_atoms, NC = (size_t)max_cells, NCH = (size_t)max_chunks_,
                  NS = (size_t)opt.max_slots, NCL = (size_t)max_clusters_, NCC = (size_t)max_cchunks_;
@@ -2715,6 +2896,17 @@ void Engine::launch_force_mixed(int r) {
     const unsigned ch = (unsigned)max_chunks_;
     if (opt_.cluster) {
         launch_force_cluster(r);
+        return;
+    }
+    if (opt_.cell_tiles) {
+        const size_t smem = TILE_ATOMS * sizeof(float4);
+        if (opt_.mixed_kahan)
+            single_type_ ? k_force_mixed_tile<1, true><<<ch, 256, smem, stream_>>>(*d_, r)
+                         : k_force_mixed_tile<1, false><<<ch, 256, smem, stream_>>>(*d_, r);
+        else
+            single_type_ ? k_force_mixed_tile<0, true><<<ch, 256, smem, stream_>>>(*d_, r)
+                         : k_force_mixed_tile<0, false><<<ch, 256, smem, stream_>>>(*d_, r);
+        g_launches.fetch_add(1);
         return;
     }
     if (opt_.list_tma && opt_.lpa == 1) {

@@ -102,6 +102,9 @@ struct PoolOptions {
     int lpa = 1;               // lanes per atom in the list build and force kernels (1,4,8,16,32)
     int mix_batch = 4;         // list entries per gather batch in the mixed force kernel (4, 8, 16)
     bool list_tma = false;     // mixed, thread per atom: list rows streamed to shared memory by bulk copies
+    bool cell_tiles = false;   // mixed, thread per atom: neighbour-cell tiles staged in shared memory
+    bool plain_graphs = false; // step graphs without the conditional rebuild node (profilers cannot
+                               // look inside graphs holding conditional nodes)
     int cluster = 0;           // mixed: atoms per cluster of the cluster-list kernels (2 or 4); 0 = per-atom list
     int build_cluster = 0;     // per-atom list, thread per atom: build scans candidates per cluster of this
                                // many atoms (2 or 4; 0 or 1 = per atom)

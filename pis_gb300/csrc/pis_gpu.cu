@@ -25,6 +25,8 @@ struct pis_gpu_ctx {
     bool list_tma = false;
     int cluster = 0;
     int build_cluster = 0;
+    bool cell_tiles = false;
+    bool plain_graphs = false;
     std::unique_ptr<pis::Engine> eng;
     pis::PoolOptions pool;  // options the current engine was created with
     int slot = -1;
@@ -59,7 +61,8 @@ bool same_pool(const pis::PoolOptions& a, const pis::PoolOptions& b) {
            a.max_atoms == b.max_atoms && a.max_slots == b.max_slots && a.max_cells == b.max_cells &&
            a.max_types_total == b.max_types_total && a.hist == b.hist && a.fp64_fast == b.fp64_fast &&
            a.mixed_kahan == b.mixed_kahan && a.lpa == b.lpa && a.mix_batch == b.mix_batch &&
-           a.list_tma == b.list_tma && a.cluster == b.cluster && a.build_cluster == b.build_cluster;
+           a.list_tma == b.list_tma && a.cluster == b.cluster && a.build_cluster == b.build_cluster &&
+           a.cell_tiles == b.cell_tiles && a.plain_graphs == b.plain_graphs;
 }
 
 pis_status flags_to_status(pis_gpu_ctx* ctx, const pis::SysState& ss) {
@@ -112,8 +115,8 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
     if (!ctx) return PIS_ERR_INVALID_ARGUMENT;
     if (list_kind < PIS_LIST_DEFAULT || list_kind > PIS_LIST_FULL)
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown list kind");
-    if (flags & ~(PIS_OPT_FP64_FAST | PIS_OPT_MIXED_KAHAN | PIS_OPT_LIST_TMA | PIS_OPT_LANES(0xff) | PIS_OPT_BATCH(0xff) |
-                  PIS_OPT_CLUSTER(0xf) | PIS_OPT_SCAN(0x7)))
+    if (flags & ~(PIS_OPT_FP64_FAST | PIS_OPT_MIXED_KAHAN | PIS_OPT_LIST_TMA | PIS_OPT_TILE | PIS_OPT_PLAIN_GRAPHS |
+                  PIS_OPT_LANES(0xff) | PIS_OPT_BATCH(0xff) | PIS_OPT_CLUSTER(0xf) | PIS_OPT_SCAN(0x7)))
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown option flag");
     const int batch = (flags >> 16) & 0xff;
     if (batch != 0 && batch != 4 && batch != 8 && batch != 16)
@@ -135,6 +138,10 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
     if (scan != 0 && scan != 1 && scan != 2 && scan != 4)
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "atoms per build cluster must be 1, 2 or 4");
     ctx->build_cluster = scan;
+    ctx->cell_tiles = (flags & PIS_OPT_TILE) != 0;
+    ctx->plain_graphs = (flags & PIS_OPT_PLAIN_GRAPHS) != 0;
+    if (ctx->cell_tiles && (ctx->precision != PIS_PRECISION_MIXED || ctx->lpa != 1 || ctx->list_tma || ctx->cluster))
+        return fail(ctx, PIS_ERR_UNSUPPORTED, "neighbour-cell tiles need the mixed path, thread per atom, per-atom lists");
     if (ctx->cluster && (ctx->precision != PIS_PRECISION_MIXED || (ctx->lpa != 1 && ctx->lpa != ctx->cluster) ||
                          ctx->list_tma))
         return fail(ctx, PIS_ERR_UNSUPPORTED,
@@ -179,6 +186,8 @@ pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_id
     opt.list_tma = ctx->list_tma;
     opt.cluster = ctx->cluster;
     opt.build_cluster = ctx->build_cluster;
+    opt.cell_tiles = ctx->cell_tiles;
+    opt.plain_graphs = ctx->plain_graphs;
     opt.max_atoms = n;
     opt.max_slots = 1;
     int64_t ncell = 1;

@@ -25,7 +25,8 @@ class GpuContext:
     """One device-resident LJ system (the C-ABI context)."""
 
     def __init__(self, table, n_types, skin=0.3, precision="fp64", list_kind="default", shift=True,
-                 fp64_fast=False, mixed_kahan=False, lanes=0, batch=0, tma=False, cluster=0, scan=0):
+                 fp64_fast=False, mixed_kahan=False, lanes=0, batch=0, tma=False, cluster=0, scan=0, tiles=False,
+                 plain_graphs=False):
         self._lib = _ffi.lib()
         self.n_types = int(n_types)
         pairs = (_ffi.LJPair * len(table))()
@@ -39,7 +40,8 @@ class GpuContext:
         self._h = h
         self.n = 0
         self.precision = precision
-        flags = _ffi.option_flags(fp64_fast, mixed_kahan, lanes, batch, tma, cluster, scan)
+        flags = _ffi.option_flags(fp64_fast, mixed_kahan, lanes, batch, tma, cluster, scan, tiles,
+                                  plain_graphs)
         if list_kind != "default" or flags:
             self._check(self._lib.pis_gpu_set_options(self._h, _ffi.LIST_KIND[list_kind], flags))
 

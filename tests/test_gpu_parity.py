@@ -252,3 +252,21 @@ def test_set_state_reuses_pool_and_matches_fresh_context(liquid_melt, precision)
     assert pe == pe_f and np.array_equal(f, f_f) and np.array_equal(e, e_f)
     assert np.array_equal(p, p_f) and np.array_equal(v, v_f) and np.array_equal(fo, fo_f)
     assert g.stats()["steps"] == 30
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_plain_step_graphs_equal_conditional(liquid_melt, precision):
+    # PIS_OPT_PLAIN_GRAPHS captures the step graphs with the rebuild kernels launched on every
+    # step (exiting at once when nothing rebuilds) instead of behind a conditional node; the
+    # trajectory, energies and rebuild count must be those of the default graphs bit for bit
+    from pis_gb300.potentials import kernel_launches
+    a = to_gpu(liquid_melt, precision)
+    b = to_gpu(liquid_melt, precision, plain_graphs=True)
+    e_a = a.verlet_step_nve(0.005, 120)
+    k0 = kernel_launches()
+    e_b = b.verlet_step_nve(0.005, 120)
+    assert kernel_launches() - k0 >= 120 * 4
+    assert np.array_equal(e_a, e_b)
+    for x, y in zip(a.get_state(), b.get_state()):
+        assert np.array_equal(x, y)
+    assert a.stats()["rebuilds"] == b.stats()["rebuilds"] >= 2
