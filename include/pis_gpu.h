@@ -107,7 +107,9 @@ pis_status pis_gpu_create(const pis_lj_pair* table, int32_t n_pairs, int32_t n_t
                         * neighbour positions from there */
 #define PIS_OPT_PLAIN_GRAPHS 16 /* step graphs launch the list-rebuild kernels on every step (they exit at
                                  * once when nothing rebuilds) instead of behind a conditional graph node:
-                                 * for profilers that cannot look inside graphs holding conditional nodes */
+                                 * for profilers that cannot look inside graphs holding conditional nodes;
+                                 * PIS_GPU_PLAIN_GRAPHS=1 in the environment does the same for every
+                                 * context and batch of the process */
 #define PIS_OPT_CLUSTER(m) ((m) << 24) /* mixed path, neighbour-list shape: 1 = one list per atom,
                                         * 2 or 4 = one list per cluster of m spatially adjacent atoms
                                         * of a cell (each neighbour read serves m pairs);

@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 namespace cg = cooperative_groups;
@@ -2200,7 +2201,10 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     st = check(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking), "stream", err);
     if (st) return st;
     ls_ = stream_;
-    cond_rebuild_ = !opt.plain_graphs;
+    // PIS_GPU_PLAIN_GRAPHS=1 in the environment selects plain step graphs for every pool of the
+    // process (for profilers that cannot look inside graphs holding conditional nodes)
+    const char* plain_env = std::getenv("PIS_GPU_PLAIN_GRAPHS");
+    cond_rebuild_ = !opt.plain_graphs && !(plain_env && plain_env[0] && std::strcmp(plain_env, "0") != 0);
 
     const size_t NA = (size_t)opt.max_atoms, NC = (size_t)max_cells, NCH = (size_t)max_chunks_,
                  NS = (size_t)opt.max_slots, NCL = (size_t)max_clusters_, NCC = (size_t)max_cchunks_;
