@@ -255,12 +255,20 @@ def main():
     ms_s, stages = mix.run_timed(DT, args.steps, stages=True)
     stages_per = stages / args.steps
     list_per_atom = st["list_entries"] / n
-    # force-kernel algorithmic bytes: list entries + own cell-relative position + nn + force write
-    force_bytes = n * (4 + 16 + 32) + st["list_entries"] * 4
+    fused = bool(st.get("fused_step"))
+    if fused:
+        # fused step kernel, per atom: nn 4 + own cell-relative position 16 + force write 32 +
+        # velocity and acceleration read/write 2 x 64 + position read/write 64 + build snapshot 32 +
+        # build-time cell-relative position 16 + new cell-relative position 16, plus the list words
+        step_kernel, per_atom_bytes = "k_step_mixed", 4 + 16 + 32 + 64 + 64 + 64 + 32 + 16 + 16
+    else:
+        # force kernel: nn + own cell-relative position + force write, plus the list words
+        step_kernel, per_atom_bytes = "k_force_mixed", 4 + 16 + 32
+    force_bytes = n * per_atom_bytes + st["list_entries"] * 4
     force_ms = stages_per[2]
     achieved = force_bytes / (force_ms * 1e-3) / 1e9
     pairs_per_step = 27.6 * n  # in-cutoff unordered pairs per step at rho* = 0.8442
-    traffic = read_traffic("force_mixed", n)
+    traffic = read_traffic("step_mixed" if fused else "force_mixed", n)
 
     # ---- plain FP64 on the same state --------------------------------------------------------
     f64 = GpuContext(TABLE, 1, skin=SKIN, precision="fp64")
@@ -350,7 +358,7 @@ def main():
             "tuned_options": tuned,
             "drift": drift,
             "list_entries_per_atom": list_per_atom,
-            "roofline": {"bound": "hbm", "kernel": "k_force_mixed", "achieved": achieved, "peak": hbm_peak,
+            "roofline": {"bound": "hbm", "kernel": step_kernel, "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_src,
                          "traffic": traffic, "algorithmic_bytes_per_launch": force_bytes},
             "cpu_baseline": cpu,

@@ -81,6 +81,8 @@ typedef struct {
     int32_t cells[3];         /* cell grid used by the list build */
     double pe, ke;            /* energies after the last force evaluation / step */
     double virial[9];         /* sum_i r_i F_i^T (row-major), as src/atoms/properties.rs:49-51 */
+    int32_t fused_step;       /* 1 when steps run the fused force + kick + drift kernel */
+    int32_t reserved_;
 } pis_gpu_stats;
 
 /* Create a context for a pair table (the PotentialManager built in System::contextualize,
@@ -110,6 +112,8 @@ pis_status pis_gpu_create(const pis_lj_pair* table, int32_t n_pairs, int32_t n_t
                                  * for profilers that cannot look inside graphs holding conditional nodes;
                                  * PIS_GPU_PLAIN_GRAPHS=1 in the environment does the same for every
                                  * context and batch of the process */
+#define PIS_OPT_UNFUSED 32 /* mixed precision, default kernel shape: separate force, kick and drift kernels
+                            * in each step instead of the fused step kernel (same results bit for bit) */
 #define PIS_OPT_CLUSTER(m) ((m) << 24) /* mixed path, neighbour-list shape: 1 = one list per atom,
                                         * 2 or 4 = one list per cluster of m spatially adjacent atoms
                                         * of a cell (each neighbour read serves m pairs);

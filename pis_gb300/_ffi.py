@@ -23,10 +23,10 @@ LIST_KIND = {"default": 0, "half": 1, "full": 2}
 
 
 def option_flags(fp64_fast=False, mixed_kahan=False, lanes=0, batch=0, tma=False, cluster=0, scan=0,
-                 tiles=False, plain_graphs=False) -> int:
+                 tiles=False, plain_graphs=False, unfused=False) -> int:
     """PIS_OPT_* bits of include/pis_gpu.h for the variant knobs."""
     return ((1 if fp64_fast else 0) | (2 if mixed_kahan else 0) | (4 if tma else 0) | (8 if tiles else 0)
-            | (16 if plain_graphs else 0) | (int(lanes) << 8) | (int(batch) << 16) | (int(cluster) << 24)
+            | (16 if plain_graphs else 0) | (32 if unfused else 0) | (int(lanes) << 8) | (int(batch) << 16) | (int(cluster) << 24)
             | (int(scan) << 28))
 
 
@@ -47,7 +47,8 @@ class LJPair(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("n_atoms", C.c_int64), ("steps", C.c_int64), ("rebuilds", C.c_int64),
                 ("list_entries", C.c_int64), ("list_capacity", C.c_int32), ("cells", C.c_int32 * 3),
-                ("pe", C.c_double), ("ke", C.c_double), ("virial", C.c_double * 9)]
+                ("pe", C.c_double), ("ke", C.c_double), ("virial", C.c_double * 9), ("fused_step", C.c_int32),
+                ("reserved_", C.c_int32)]
 
 
 class Job(C.Structure):

@@ -33,10 +33,10 @@ def lj_pool_cells(k, rho, rlist=2.8) -> int:
 class Batch:
     def __init__(self, max_atoms, max_slots, max_cells=0, precision="mixed", fp64_fast=False, mixed_kahan=False,
                  lanes=0, batch=0, tma=False, cluster=0, scan=0, tiles=False,
-                 plain_graphs=False):
+                 plain_graphs=False, unfused=False):
         self._lib = _ffi.lib()
         flags = _ffi.option_flags(fp64_fast, mixed_kahan, lanes, batch, tma, cluster, scan, tiles,
-                                  plain_graphs)
+                                  plain_graphs, unfused)
         h = C.c_void_p()
         st = self._lib.pis_batch_create(int(max_atoms), int(max_slots), int(max_cells), _ffi.PRECISION[precision],
                                         flags, C.byref(h))

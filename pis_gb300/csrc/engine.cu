@@ -89,6 +89,9 @@ struct Engine::DevPtrs {
     int32_t cl_force;     // forces run over cluster lists (else per-atom lists)
     int32_t cl_lanes;     // cluster force blocks per cluster chunk (1, or M with a lane per member)
     int32_t* ctl;         // ctl[0]: some slot rebuilds its list in the current step or evaluation
+    // fused step: cell-relative coordinates of the drifted atoms go to prel_out (the buffer the next
+    // step reads)
+    float4* prel_out;
 };
 using DP = Engine::DevPtrs;
 
@@ -301,6 +304,44 @@ __device__ __forceinline__ float4 cell_relative(const SysParams& sp, double4_32a
 // FP64 division fewer per component - the FP64 pipe is the scarce unit on GB300).
 // EXACT (FP64 path): the reference's rounding sequence and wrap of every atom every step.
 // Mixed path: FP64 with fused multiply-adds, and only atoms that left the box are wrapped.
+//
+// The mixed path's drift arithmetic (x + v dt + a dt^2/2 as two fused multiply-adds per axis, then
+// the wrap of atoms that left the box); shared by k_integrate1 and the fused step kernel.
+__device__ __forceinline__ void drift_mixed(const SysParams& sp, const double4_32a& p, const double4_32a& v,
+                                            double ax, double ay, double az, double& x, double& y, double& z) {
+    x = wrap_if_out(fma(ax, sp.hdt2, fma(v.x, sp.dt, p.x)), sp.h[0]);
+    y = wrap_if_out(fma(ay, sp.hdt2, fma(v.y, sp.dt, p.y)), sp.h[1]);
+    z = wrap_if_out(fma(az, sp.hdt2, fma(v.z, sp.dt, p.z)), sp.h[2]);
+}
+// Skin test: the slot rebuilds when any atom moved more than skin/2 since the last build. The
+// minimum image is only taken when the plain difference fails the test (moved far, or crossed
+// the periodic boundary). Returns the displacement since the build (for the cell-relative
+// coordinates).
+__device__ __forceinline__ void skin_test(const DP& P, const SysParams& sp, SysState& st, int i, double x,
+                                          double y, double z, double& dx, double& dy, double& dz) {
+    const double4_32a b = P.posb[i];
+    dx = x - b.x, dy = y - b.y, dz = z - b.z;
+    double d2 = fma(dx, dx, fma(dy, dy, dz * dz));
+    // d2 >= 0, so comparing bit patterns as integers orders it like the doubles (a NaN with
+    // either sign fails the test too: its magnitude bits exceed every finite value's)
+    if ((__double_as_longlong(d2) & 0x7fffffffffffffffll) > __double_as_longlong(sp.half_skin2)) {
+        dx = min_image_axis(dx, sp.h[0], sp.hinv[0]);
+        dy = min_image_axis(dy, sp.h[1], sp.hinv[1]);
+        dz = min_image_axis(dz, sp.h[2], sp.hinv[2]);
+        d2 = fma(dx, dx, fma(dy, dy, dz * dz));
+        if (!(d2 <= sp.half_skin2)) {  // NaN also requests a rebuild
+            st.rebuild = 1;
+            P.ctl[0] = 1;
+        }
+        if (x != x || y != y || z != z) atomicOr(&st.flags, FLAG_NAN);
+    }
+}
+// cell-relative FP32 coordinates = build-time ones + displacement since the build
+__device__ __forceinline__ float4 cell_relative_moved(const DP& P, int i, double dx, double dy, double dz) {
+    const float4 q = P.prelb[i];
+    return make_float4(q.x + (float)dx, q.y + (float)dy, q.z + (float)dz, q.w);
+}
+
 template <bool MIXED>
 __global__ void k_integrate1(const DP P) {
     int s, i;
@@ -323,40 +364,13 @@ __global__ void k_integrate1(const DP P) {
         y = wrap_axis(y, sp.h[1], sp.hinv[1]);
         z = wrap_axis(z, sp.h[2], sp.hinv[2]);
     } else {
-        // x + v dt + a dt^2/2 as two fused multiply-adds per axis
-        x = fma(a.x, sp.hdt2, fma(v.x, sp.dt, p.x));
-        y = fma(a.y, sp.hdt2, fma(v.y, sp.dt, p.y));
-        z = fma(a.z, sp.hdt2, fma(v.z, sp.dt, p.z));
-        x = wrap_if_out(x, sp.h[0]);
-        y = wrap_if_out(y, sp.h[1]);
-        z = wrap_if_out(z, sp.h[2]);
+        drift_mixed(sp, p, v, a.x, a.y, a.z, x, y, z);
     }
     P.pos[cur][i] = make_double4_32a(x, y, z, p.w);
     if (P.zero_forces) P.frc[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
-    // skin test: rebuild when any atom moved more than skin/2 since the last build. The
-    // minimum image is only taken when the plain difference fails the test (moved far, or
-    // crossed the periodic boundary).
-    const double4_32a b = P.posb[i];
-    double dx = x - b.x, dy = y - b.y, dz = z - b.z;
-    double d2 = fma(dx, dx, fma(dy, dy, dz * dz));
-    // d2 >= 0, so comparing bit patterns as integers orders it like the doubles (a NaN with
-    // either sign fails the test too: its magnitude bits exceed every finite value's)
-    if ((__double_as_longlong(d2) & 0x7fffffffffffffffll) > __double_as_longlong(sp.half_skin2)) {
-        dx = min_image_axis(dx, sp.h[0], sp.hinv[0]);
-        dy = min_image_axis(dy, sp.h[1], sp.hinv[1]);
-        dz = min_image_axis(dz, sp.h[2], sp.hinv[2]);
-        d2 = fma(dx, dx, fma(dy, dy, dz * dz));
-        if (!(d2 <= sp.half_skin2)) {  // NaN also requests a rebuild
-            st.rebuild = 1;
-            P.ctl[0] = 1;
-        }
-        if (x != x || y != y || z != z) atomicOr(&st.flags, FLAG_NAN);
-    }
-    if (MIXED) {
-        // cell-relative FP32 coordinates = build-time ones + displacement since the build
-        const float4 q = P.prelb[i];
-        P.prel[i] = make_float4(q.x + (float)dx, q.y + (float)dy, q.z + (float)dz, q.w);
-    }
+    double dx, dy, dz;
+    skin_test(P, sp, st, i, x, y, z, dx, dy, dz);
+    if (MIXED) P.prel[i] = cell_relative_moved(P, i, dx, dy, dz);
 }
 
 // Counting sort, pass 1: cell of every atom (reference binning of src/atoms/neighbour_list.rs:
@@ -1084,6 +1098,49 @@ __device__ __forceinline__ MixLJ mix_lj_load(const LJDev& L) {
 
 constexpr int MIX_FLUSH = 32;  // entries per lane between FP64 (or compensated) folds
 
+// The pair sum of one atom (or of lane gl of its LPA lanes) over its list: gathers in batches of
+// MIX_BATCH entries, FP32 pair terms, folds every MIX_FLUSH entries. Returns the atom's
+// cell-relative position. Shared by k_force_mixed and the fused step kernel.
+template <int ACC, int LPA, bool ONE, int MIX_BATCH>
+__device__ __forceinline__ float4 mixed_atom_forces(const DP& P, const SysParams& sp, int i, int gl,
+                                                    const float4* shift, MixAcc<ACC>& acc) {
+    const float4* __restrict__ prel = P.prel;
+    const float4 pi = prel[i];
+    const int ti = __float_as_int(pi.w);
+    const LJDev* tab = P.tab + sp.tab0 + ti * sp.nt;
+    const MixLJ P0 = mix_lj_load(tab[0]);
+    const int nn = P.nn[i];
+    const int64_t row = P.npad * LPA;
+    const uint32_t* __restrict__ nbp = P.nbr + (int64_t)i * LPA + gl;
+    const uint32_t pad = (uint32_t)i | (63u << JBITS);
+    int since = 0;
+    // list words are addressed with 32-bit offsets from the lane's first word (the pool's list
+    // is below 2^32 words, checked at init); full batches load unconditionally, the last
+    // partial batch pads with an out-of-range entry
+    const uint32_t row32 = (uint32_t)row;
+    uint32_t qoff = 0;
+    for (int k0 = 0; k0 < nn; k0 += LPA * MIX_BATCH) {
+        uint32_t ent[MIX_BATCH];
+        if (k0 + LPA * MIX_BATCH <= nn) {
+#pragma unroll
+            for (int b = 0; b < MIX_BATCH; ++b) ent[b] = load_list_word(nbp + qoff + (uint32_t)b * row32);
+        } else {
+#pragma unroll
+            for (int b = 0; b < MIX_BATCH; ++b)
+                ent[b] = (k0 + b * LPA + gl < nn) ? load_list_word(nbp + qoff + (uint32_t)b * row32) : pad;
+        }
+        qoff += (uint32_t)MIX_BATCH * row32;
+        mixed_pairs<ONE, MIX_BATCH, ACC>(ent, prel, pi, shift, tab, P0, acc);
+        since += MIX_BATCH;
+        if (since >= MIX_FLUSH) {
+            acc.fold();
+            since = 0;
+        }
+    }
+    acc.finish();
+    return pi;
+}
+
 template <int ACC, int LPA, bool ONE, int MIX_BATCH>
 __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) {
     __shared__ double sh[32];
@@ -1098,42 +1155,7 @@ __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) 
     __syncthreads();
     const int gl = (int)tile.thread_rank();
     MixAcc<ACC> acc;
-    if (live) {
-        const float4* __restrict__ prel = P.prel;
-        const float4 pi = prel[i];
-        const int ti = __float_as_int(pi.w);
-        const LJDev* tab = P.tab + sp.tab0 + ti * sp.nt;
-        const MixLJ P0 = mix_lj_load(tab[0]);
-        const int nn = P.nn[i];
-        const int64_t row = P.npad * LPA;
-        const uint32_t* __restrict__ nbp = P.nbr + (int64_t)i * LPA + gl;
-        const uint32_t pad = (uint32_t)i | (63u << JBITS);
-        int since = 0;
-        // list words are addressed with 32-bit offsets from the lane's first word (the pool's list
-        // is below 2^32 words, checked at init); full batches load unconditionally, the last
-        // partial batch pads with an out-of-range entry
-        const uint32_t row32 = (uint32_t)row;
-        uint32_t qoff = 0;
-        for (int k0 = 0; k0 < nn; k0 += LPA * MIX_BATCH) {
-            uint32_t ent[MIX_BATCH];
-            if (k0 + LPA * MIX_BATCH <= nn) {
-#pragma unroll
-                for (int b = 0; b < MIX_BATCH; ++b) ent[b] = load_list_word(nbp + qoff + (uint32_t)b * row32);
-            } else {
-#pragma unroll
-                for (int b = 0; b < MIX_BATCH; ++b)
-                    ent[b] = (k0 + b * LPA + gl < nn) ? load_list_word(nbp + qoff + (uint32_t)b * row32) : pad;
-            }
-            qoff += (uint32_t)MIX_BATCH * row32;
-            mixed_pairs<ONE, MIX_BATCH, ACC>(ent, prel, pi, shift, tab, P0, acc);
-            since += MIX_BATCH;
-            if (since >= MIX_FLUSH) {
-                acc.fold();
-                since = 0;
-            }
-        }
-        acc.finish();
-    }
+    if (live) mixed_atom_forces<ACC, LPA, ONE, MIX_BATCH>(P, sp, i, gl, shift, acc);
     double fx = acc.fx, fy = acc.fy, fz = acc.fz, e = acc.e;
 #pragma unroll
     for (int o = LPA / 2; o > 0; o >>= 1) {
@@ -1819,6 +1841,26 @@ __global__ void __launch_bounds__(CL_THREADS) k_keep_cl(const DP P, int slot) {
 // W = sum r_i F_i^T (:49-51). UPDATE = false only refreshes acc = F/m and reduces (after a
 // force evaluation). EXACT keeps the reference's division and rounding order; the mixed path
 // multiplies by the stored 1/m (acc.w) and fuses.
+//
+// The mixed path's arithmetic (a_tdt = F * (1/m) with 1/m stored in acc.w; v += (a_t + a_tdt) dt/2
+// as one fused multiply-add per axis; m |v|^2 with m in vel.w) is shared by k_integrate2 and the
+// fused step kernel, with explicit roundings so that both compile to the same operations.
+__device__ __forceinline__ void accel_mixed(const double4_32a& f, double inv_m, double& bx, double& by,
+                                            double& bz) {
+    bx = __dmul_rn(f.x, inv_m);
+    by = __dmul_rn(f.y, inv_m);
+    bz = __dmul_rn(f.z, inv_m);
+}
+__device__ __forceinline__ void kick_mixed(const SysParams& sp, double4_32a& v, const double4_32a& a, double bx,
+                                           double by, double bz) {
+    v.x = fma(__dadd_rn(a.x, bx), sp.hdt, v.x);
+    v.y = fma(__dadd_rn(a.y, by), sp.hdt, v.y);
+    v.z = fma(__dadd_rn(a.z, bz), sp.hdt, v.z);
+}
+__device__ __forceinline__ double twice_ke_mixed(const double4_32a& v) {
+    return __dmul_rn(v.w, fma(v.x, v.x, fma(v.y, v.y, __dmul_rn(v.z, v.z))));
+}
+
 template <bool UPDATE, bool EXACT>
 __global__ void k_integrate2(const DP P, int respect_steps) {
     __shared__ double sh[32];
@@ -1842,9 +1884,7 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
             by = __dadd_rn(0.0, __ddiv_rn(f.y, m));
             bz = __dadd_rn(0.0, __ddiv_rn(f.z, m));
         } else {
-            bx = f.x * a.w;
-            by = f.y * a.w;
-            bz = f.z * a.w;
+            accel_mixed(f, a.w, bx, by, bz);
         }
         if (UPDATE) {
             if (EXACT) {
@@ -1852,16 +1892,14 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
                 v.y = __dadd_rn(v.y, __dmul_rn(__dmul_rn(__dadd_rn(a.y, by), 0.5), sp.dt));
                 v.z = __dadd_rn(v.z, __dmul_rn(__dmul_rn(__dadd_rn(a.z, bz), 0.5), sp.dt));
             } else {
-                v.x = fma(a.x + bx, sp.hdt, v.x);
-                v.y = fma(a.y + by, sp.hdt, v.y);
-                v.z = fma(a.z + bz, sp.hdt, v.z);
+                kick_mixed(sp, v, a, bx, by, bz);
             }
             P.vel[cur][i] = v;
         }
         P.acc[cur][i] = make_double4_32a(bx, by, bz, a.w);
         // m |v|^2 here and the factor 1/2 on the block sum: halving is exact, so this equals the
         // sum of (0.5 m) |v|^2 (properties.rs:17-24) bit for bit
-        ke = EXACT ? __dmul_rn(m, norm2_ref(v.x, v.y, v.z)) : m * fma(v.x, v.x, fma(v.y, v.y, v.z * v.z));
+        ke = EXACT ? __dmul_rn(m, norm2_ref(v.x, v.y, v.z)) : twice_ke_mixed(v);
         if (st.want_virial) p = P.pos[cur][i];
     }
     double tot = block_sum<256>(ke, sh);
@@ -1878,13 +1916,79 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
     }
 }
 
+// One velocity-Verlet step of the mixed path in a single pass over the atoms (thread per atom):
+// the forces of step t (k_force_mixed's arithmetic), the kick that ends step t (k_integrate2's),
+// and, when DRIFT and the slot runs another step, the drift and skin test that start step t + 1
+// (k_integrate1's). The drift and the kick are FP64 work that now overlaps the gather-bound pair
+// loop of other warps (the FP64 pipe is otherwise nearly idle in the force kernel), and the
+// separate passes over velocities, accelerations and positions disappear.
+// Other threads are still gathering neighbour positions from P.prel when an atom drifts, so the
+// new cell-relative coordinates go to the other buffer (P.prel_out); the step graph alternates
+// the two buffers. A slot runs step t + 1 exactly when it drifted here, and the coordinates are a
+// function of the FP64 state (the list build writes them, every drift rewrites them from the build
+// snapshot), so nothing else ever reads a stale buffer. Results equal those of the three separate
+// kernels bit for bit (same arithmetic, same block partial sums).
+template <int ACC, bool ONE, int MIX_BATCH, bool DRIFT>
+__global__ void __launch_bounds__(256) k_step_mixed(const DP P) {
+    __shared__ double sh[32];
+    __shared__ float4 shift[64];
+    int s, i;
+    const bool live = atom_of(P, s, i);
+    if (s < 0) return;
+    if (!slot_runs(P, s, 1)) return;
+    const SysParams& sp = P.sp[s];
+    SysState& st = P.st[s];
+    fill_shift_table(shift, sp);
+    __syncthreads();
+    MixAcc<ACC> acc;
+    if (live) mixed_atom_forces<ACC, 1, ONE, MIX_BATCH>(P, sp, i, 0, shift, acc);
+    const bool drift = DRIFT && st.steps_left > 1;
+    const bool want_virial = st.want_virial != 0;
+    double ke = 0.0;
+    double4_32a p = make_double4_32a(0.0, 0.0, 0.0, 0.0), f = p;
+    if (live) {
+        f = make_double4_32a(acc.fx, acc.fy, acc.fz, 0.0);
+        P.frc[i] = f;
+        const int cur = st.cur;
+        double4_32a v = P.vel[cur][i];
+        const double4_32a a = P.acc[cur][i];
+        double bx, by, bz;
+        accel_mixed(f, a.w, bx, by, bz);
+        kick_mixed(sp, v, a, bx, by, bz);
+        P.vel[cur][i] = v;
+        P.acc[cur][i] = make_double4_32a(bx, by, bz, a.w);
+        ke = twice_ke_mixed(v);
+        if (want_virial || drift) p = P.pos[cur][i];
+        if (drift) {
+            double x, y, z;
+            drift_mixed(sp, p, v, bx, by, bz, x, y, z);
+            P.pos[cur][i] = make_double4_32a(x, y, z, p.w);
+            double dx, dy, dz;
+            skin_test(P, sp, st, i, x, y, z, dx, dy, dz);
+            P.prel_out[i] = cell_relative_moved(P, i, dx, dy, dz);
+        }
+    }
+    const double pe_tot = block_sum<256>(acc.e, sh);
+    if (threadIdx.x == 0) P.pe_part[blockIdx.x] = pe_tot;
+    const double ke_tot = block_sum<256>(ke, sh);
+    if (threadIdx.x == 0) P.ke_part[blockIdx.x] = 0.5 * ke_tot;
+    if (want_virial) {
+        double r[3] = {p.x, p.y, p.z}, g[3] = {f.x, f.y, f.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                double t = block_sum<256>(live ? r[a] * g[b] : 0.0, sh);
+                if (threadIdx.x == 0) P.vir_part[(int64_t)blockIdx.x * 9 + a * 3 + b] = t;
+            }
+    }
+}
+
 // Per-slot end of a step (or of a force evaluation): deterministic sums of the chunk partials,
 // energy history, NaN check (PisError::NaNEnergy, src/errors.rs:87-88), counters.
 // mode 0: step; mode 1: force evaluation only (PE); mode 2: KE/virial only.
 __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) {
     __shared__ double sh[32];
-    // every rebuild of this step or evaluation is done: lower the device-wide request word
-    if (mode != 2 && blockIdx.x == 0 && threadIdx.x == 0) P.ctl[0] = 0;
     int s = blockIdx.x;
     const SysParams& sp = P.sp[s];
     if (!sp.active) return;
@@ -1923,10 +2027,6 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
         if (vir)
             for (int q = 0; q < 9; ++q) st.virial[q] = w[q];
         if ((mode != 2 && pe != pe) || (mode != 1 && ke != ke)) st.flags |= FLAG_NAN;
-        if (mode != 2 && st.rebuild) {
-            st.rebuilds += 1;
-            st.rebuild = 0;
-        }
         if (mode == 2) {
             st.eval = 0;
             st.want_virial = 0;
@@ -1936,6 +2036,21 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
             st.steps_done += 1;
             st.steps_left -= 1;
         }
+    }
+}
+
+// End of a rebuild phase (its last kernel, so every rebuild kernel has read the request flags):
+// count and clear the rebuilt slots' flags and lower the device-wide request word. A drift that
+// runs later in the same step (the fused step kernel) may raise them again for the next step.
+__global__ void k_rebuild_done(const DP P, int step_mode) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0) P.ctl[0] = 0;
+    if (s >= P.max_slots || !P.sp[s].active) return;
+    if (!slot_runs(P, s, step_mode)) return;
+    SysState& st = P.st[s];
+    if (st.rebuild) {
+        st.rebuilds += 1;
+        st.rebuild = 0;
     }
 }
 
@@ -2210,6 +2325,11 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
                  NS = (size_t)opt.max_slots, NCL = (size_t)max_clusters_, NCC = (size_t)max_cchunks_;
     // the per-atom list is not used (and kept minimal) when the cluster list is
     const size_t nbr_bytes = opt.cluster ? 256 : 4 * (size_t)npad_ * cap_;
+    // the fused step kernel serves the mixed path's default shape (thread per atom, per-atom full
+    // list, gathers from global memory, 4- or 8-entry batches)
+    fused_ = opt.precision == PIS_PRECISION_MIXED && !opt.unfused && opt.lpa == 1 && !opt.list_tma &&
+             !opt.cell_tiles && !opt.cluster && !clm_ && !half_ && opt.blk == 256 &&
+             (opt.mix_batch == 4 || opt.mix_batch == 8);
     struct Item {
         void** p;
         size_t bytes;
@@ -2231,6 +2351,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         {(void**)&d_->vir_part, 72 * NCH}, {(void**)&d_->pe_hist, 8 * NS * (size_t)opt.hist},
         {(void**)&d_->ctl, 256},
     };
+    if (fused_) items.push_back({&prel_buf_[1], 16 * NA});
     if (clm_) {
         items.push_back({(void**)&d_->cl_atom, 4 * NCL});
         items.push_back({(void**)&d_->cl_start, 4 * NC});
@@ -2264,6 +2385,8 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     d_->clm = clm_;
     d_->cl_force = opt.cluster ? 1 : 0;
     d_->cl_lanes = (opt.cluster && opt.lpa == opt.cluster) ? opt.cluster : 1;
+    prel_buf_[0] = d_->prel;
+    d_->prel_out = nullptr;
     st = check(cudaMemsetAsync(mem_, 0, total, stream_), "memset", err);
     if (st) return st;
     st = check(cudaMemsetAsync(d_->cell_sys, 0xff, 4 * NC, stream_), "memset", err);
@@ -2699,6 +2822,7 @@ void Engine::enqueue_rebuild(bool respect) {
     unsigned gcells = (unsigned)((opt_.max_cells * 32 + 255) / 256);
     LAUNCH(k_gather, gcells, 256, P, (int64_t)opt_.max_cells, r);
     launch_build(r);
+    LAUNCH(k_rebuild_done, (unsigned)((opt_.max_slots + 127) / 128), 128, P, r);
 }
 
 // Lanes-per-atom kernels are templates; these dispatch on the pool's runtime choice. Their grid
@@ -2929,33 +3053,82 @@ void Engine::launch_force_fp64(int r) {
 #undef PIS_CALL
 }
 
-void Engine::enqueue_step(bool respect, cudaEvent_t* ev) {
+// Step q of a g-step graph. Unfused: drift, rebuild, forces, kick, step end. Fused (mixed path,
+// default kernel shape): the graph's first step drifts alone, every step then runs rebuild, the
+// fused forces + kick + next drift (no drift in the graph's last step), step end; step q reads
+// cell-relative coordinates from buffer q & 1 (its list rebuild writes them there) and the drift
+// writes the other.
+void Engine::enqueue_step(bool respect, cudaEvent_t* ev, int64_t q, int64_t g) {
     const DP& P = *d_;
     int r = respect ? 1 : 0;
     const bool mixed = opt_.precision == PIS_PRECISION_MIXED;
+    const bool fused = mixed && fused_;
     if (ev) cudaEventRecordWithFlags(ev[0], stream_, cudaEventRecordExternal);
-    if (mixed)
-        LAUNCH(k_integrate1<true>, (unsigned)max_chunks_, opt_.blk, P);
-    else
-        LAUNCH(k_integrate1<false>, (unsigned)max_chunks_, opt_.blk, P);
+    if (!fused || q == 0) {
+        if (mixed)
+            LAUNCH(k_integrate1<true>, (unsigned)max_chunks_, opt_.blk, P);
+        else
+            LAUNCH(k_integrate1<false>, (unsigned)max_chunks_, opt_.blk, P);
+    }
     if (ev) cudaEventRecordWithFlags(ev[1], stream_, cudaEventRecordExternal);
+    if (fused) {
+        d_->prel = (float4*)prel_buf_[q & 1];
+        d_->prel_out = (float4*)prel_buf_[(q + 1) & 1];
+    }
     if (cond_step_)
         cond_error_ = cond_error_ ? cond_error_ : enqueue_rebuild_conditional(respect);
     else
         enqueue_rebuild(respect);
     if (ev) cudaEventRecordWithFlags(ev[2], stream_, cudaEventRecordExternal);
-    if (mixed)
+    if (fused)
+        launch_step_mixed(q + 1 < g);
+    else if (mixed)
         launch_force_mixed(r);
     else
         launch_force_fp64(r);
     if (ev) cudaEventRecordWithFlags(ev[3], stream_, cudaEventRecordExternal);
-    if (mixed)
-        LAUNCH((k_integrate2<true, false>), (unsigned)max_chunks_, opt_.blk, P, r);
-    else
-        LAUNCH((k_integrate2<true, true>), (unsigned)max_chunks_, opt_.blk, P, r);
+    if (!fused) {
+        if (mixed)
+            LAUNCH((k_integrate2<true, false>), (unsigned)max_chunks_, opt_.blk, P, r);
+        else
+            LAUNCH((k_integrate2<true, true>), (unsigned)max_chunks_, opt_.blk, P, r);
+    }
     if (ev) cudaEventRecordWithFlags(ev[4], stream_, cudaEventRecordExternal);
     LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 0);
     if (ev) cudaEventRecordWithFlags(ev[5], stream_, cudaEventRecordExternal);
+    if (fused) {
+        d_->prel = (float4*)prel_buf_[0];
+        d_->prel_out = nullptr;
+    }
+}
+
+template <int ACC, bool ONE, int B>
+static void launch_step_mixed_t(const DP& P, bool drift, unsigned chunks, cudaStream_t st) {
+    if (drift)
+        k_step_mixed<ACC, ONE, B, true><<<chunks, 256, 0, st>>>(P);
+    else
+        k_step_mixed<ACC, ONE, B, false><<<chunks, 256, 0, st>>>(P);
+}
+
+void Engine::launch_step_mixed(bool drift) {
+    const unsigned ch = (unsigned)max_chunks_;
+    const bool b8 = opt_.mix_batch == 8;
+    if (opt_.mixed_kahan) {
+        if (single_type_)
+            b8 ? launch_step_mixed_t<1, true, 8>(*d_, drift, ch, stream_)
+               : launch_step_mixed_t<1, true, 4>(*d_, drift, ch, stream_);
+        else
+            b8 ? launch_step_mixed_t<1, false, 8>(*d_, drift, ch, stream_)
+               : launch_step_mixed_t<1, false, 4>(*d_, drift, ch, stream_);
+    } else {
+        if (single_type_)
+            b8 ? launch_step_mixed_t<0, true, 8>(*d_, drift, ch, stream_)
+               : launch_step_mixed_t<0, true, 4>(*d_, drift, ch, stream_);
+        else
+            b8 ? launch_step_mixed_t<0, false, 8>(*d_, drift, ch, stream_)
+               : launch_step_mixed_t<0, false, 4>(*d_, drift, ch, stream_);
+    }
+    g_launches.fetch_add(1);
 }
 
 void Engine::enqueue_potential(int only) {
@@ -3081,10 +3254,12 @@ pis_status Engine::run(int64_t k, std::string& err) {
                 int64_t before = g_launches.load();
                 cond_step_ = cond_rebuild_;
                 cond_error_ = PIS_OK;
-                for (int64_t q = 0; q < g; ++q) enqueue_step(true, instrument_ ? rec.ev.data() + 6 * q : nullptr);
+                for (int64_t q = 0; q < g; ++q)
+                    enqueue_step(true, instrument_ ? rec.ev.data() + 6 * q : nullptr, q, g);
                 cond_step_ = false;
                 int64_t captured = g_launches.load() - before;
                 g_launches.fetch_sub(captured);
+                rec.kernels = captured;
                 kernels_per_step_ = captured / g;
                 cudaError_t ce = cudaStreamEndCapture(stream_, &graph);
                 if (ce == cudaSuccess && cond_error_ == PIS_OK) {
@@ -3105,7 +3280,7 @@ pis_status Engine::run(int64_t k, std::string& err) {
         }
         st = check(cudaGraphLaunch(it->second.exec, stream_), "graph launch", err);
         if (st) return st;
-        g_launches.fetch_add(kernels_per_step_ * g);
+        g_launches.fetch_add(it->second.kernels);
         if (instrument_) {
             st = sync(err);
             if (st) return st;

@@ -108,6 +108,8 @@ struct PoolOptions {
     int cluster = 0;           // mixed: atoms per cluster of the cluster-list kernels (2 or 4); 0 = per-atom list
     int build_cluster = 0;     // per-atom list, thread per atom: build scans candidates per cluster of this
                                // many atoms (2 or 4; 0 or 1 = per atom)
+    bool unfused = false;      // mixed, default kernel shape: separate force, kick and drift kernels
+                               // (otherwise one fused step kernel does all three)
 };
 
 class Engine {
@@ -159,6 +161,7 @@ class Engine {
     static int64_t launches();
     // Kernels launched per captured step (for launch accounting).
     int64_t graph_kernels_per_step() const { return kernels_per_step_; }
+    bool fused_step() const { return fused_; }
     // Stage timing with CUDA events captured into the step graphs (integrate1, list rebuild,
     // force, integrate2, reductions); costs one host sync per graph launch while enabled.
     void set_instrument(bool on) { instrument_ = on; }
@@ -171,7 +174,8 @@ class Engine {
 
   private:
     pis_status rebuild_block_map(std::string& err);
-    void enqueue_step(bool respect_steps, cudaEvent_t* ev);
+    // Step q of a g-step graph.
+    void enqueue_step(bool respect_steps, cudaEvent_t* ev, int64_t q, int64_t g);
     void enqueue_rebuild(bool respect_steps);
     // The rebuild kernels of a captured step inside a conditional graph node that runs only when
     // some slot rebuilds in that step (the condition is set on the device).
@@ -181,6 +185,7 @@ class Engine {
     void enqueue_potential(int only);
     void launch_force_fp64(int respect_steps);
     void launch_force_mixed(int respect_steps);
+    void launch_step_mixed(bool drift);
     void launch_build(int respect_steps);
     void launch_force_cluster(int respect_steps);
     pis_status check(cudaError_t e, const char* what, std::string& err);
@@ -216,6 +221,7 @@ class Engine {
     struct GraphRec {
         cudaGraphExec_t exec = nullptr;
         std::vector<cudaEvent_t> ev;  // 6 per step when instrumented
+        int64_t kernels = 0;          // kernels launched by one replay (conditional bodies aside)
     };
     std::map<int64_t, GraphRec> graphs_;
     bool instrument_ = false;
@@ -225,6 +231,8 @@ class Engine {
     int64_t kernels_per_step_ = 0;
     bool dirty_map_ = true;
     bool single_type_ = true;  // every active slot has one atom type (selects the force kernel)
+    bool fused_ = false;       // mixed steps run the fused force + kick + drift kernel
+    void* prel_buf_[2] = {nullptr, nullptr};  // the two cell-relative coordinate buffers (fused steps)
 };
 
 }  // namespace pis

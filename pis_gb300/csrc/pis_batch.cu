@@ -153,6 +153,7 @@ pis_status pis_batch_create(int64_t max_atoms, int32_t max_slots, int64_t max_ce
     b->opt.build_cluster = (flags >> 28) & 0x7;
     b->opt.cell_tiles = (flags & PIS_OPT_TILE) != 0;
     b->opt.plain_graphs = (flags & PIS_OPT_PLAIN_GRAPHS) != 0;
+    b->opt.unfused = (flags & PIS_OPT_UNFUSED) != 0;
     b->opt.list_cap = 224;  // density up to 0.95 at rc + skin = 2.8 (expected ~88 full-list entries)
     b->opt.hist = 1024;
     std::string err;

@@ -27,6 +27,7 @@ struct pis_gpu_ctx {
     int build_cluster = 0;
     bool cell_tiles = false;
     bool plain_graphs = false;
+    bool unfused = false;
     std::unique_ptr<pis::Engine> eng;
     pis::PoolOptions pool;  // options the current engine was created with
     int slot = -1;
@@ -62,7 +63,8 @@ bool same_pool(const pis::PoolOptions& a, const pis::PoolOptions& b) {
            a.max_types_total == b.max_types_total && a.hist == b.hist && a.fp64_fast == b.fp64_fast &&
            a.mixed_kahan == b.mixed_kahan && a.lpa == b.lpa && a.mix_batch == b.mix_batch &&
            a.list_tma == b.list_tma && a.cluster == b.cluster && a.build_cluster == b.build_cluster &&
-           a.cell_tiles == b.cell_tiles && a.plain_graphs == b.plain_graphs;
+           a.cell_tiles == b.cell_tiles && a.plain_graphs == b.plain_graphs &&
+           a.unfused == b.unfused;
 }
 
 pis_status flags_to_status(pis_gpu_ctx* ctx, const pis::SysState& ss) {
@@ -115,7 +117,7 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
     if (!ctx) return PIS_ERR_INVALID_ARGUMENT;
     if (list_kind < PIS_LIST_DEFAULT || list_kind > PIS_LIST_FULL)
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown list kind");
-    if (flags & ~(PIS_OPT_FP64_FAST | PIS_OPT_MIXED_KAHAN | PIS_OPT_LIST_TMA | PIS_OPT_TILE | PIS_OPT_PLAIN_GRAPHS |
+    if (flags & ~(PIS_OPT_FP64_FAST | PIS_OPT_MIXED_KAHAN | PIS_OPT_LIST_TMA | PIS_OPT_TILE | PIS_OPT_PLAIN_GRAPHS | PIS_OPT_UNFUSED |
                   PIS_OPT_LANES(0xff) | PIS_OPT_BATCH(0xff) | PIS_OPT_CLUSTER(0xf) | PIS_OPT_SCAN(0x7)))
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown option flag");
     const int batch = (flags >> 16) & 0xff;
@@ -140,6 +142,7 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
     ctx->build_cluster = scan;
     ctx->cell_tiles = (flags & PIS_OPT_TILE) != 0;
     ctx->plain_graphs = (flags & PIS_OPT_PLAIN_GRAPHS) != 0;
+    ctx->unfused = (flags & PIS_OPT_UNFUSED) != 0;
     if (ctx->cell_tiles && (ctx->precision != PIS_PRECISION_MIXED || ctx->lpa != 1 || ctx->list_tma || ctx->cluster))
         return fail(ctx, PIS_ERR_UNSUPPORTED, "neighbour-cell tiles need the mixed path, thread per atom, per-atom lists");
     if (ctx->cluster && (ctx->precision != PIS_PRECISION_MIXED || (ctx->lpa != 1 && ctx->lpa != ctx->cluster) ||
@@ -188,6 +191,7 @@ pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_id
     opt.build_cluster = ctx->build_cluster;
     opt.cell_tiles = ctx->cell_tiles;
     opt.plain_graphs = ctx->plain_graphs;
+    opt.unfused = ctx->unfused;
     opt.max_atoms = n;
     opt.max_slots = 1;
     int64_t ncell = 1;
@@ -385,6 +389,7 @@ pis_status pis_gpu_get_stats(pis_gpu_ctx* ctx, pis_gpu_stats* out) {
     out->pe = ss.pe;
     out->ke = ss.ke;
     for (int q = 0; q < 9; ++q) out->virial[q] = ss.virial[q];
+    out->fused_step = ctx->eng->fused_step() ? 1 : 0;
     return PIS_OK;
 }
 

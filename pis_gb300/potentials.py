@@ -26,7 +26,7 @@ class GpuContext:
 
     def __init__(self, table, n_types, skin=0.3, precision="fp64", list_kind="default", shift=True,
                  fp64_fast=False, mixed_kahan=False, lanes=0, batch=0, tma=False, cluster=0, scan=0, tiles=False,
-                 plain_graphs=False):
+                 plain_graphs=False, unfused=False):
         self._lib = _ffi.lib()
         self.n_types = int(n_types)
         pairs = (_ffi.LJPair * len(table))()
@@ -41,7 +41,7 @@ class GpuContext:
         self.n = 0
         self.precision = precision
         flags = _ffi.option_flags(fp64_fast, mixed_kahan, lanes, batch, tma, cluster, scan, tiles,
-                                  plain_graphs)
+                                  plain_graphs, unfused)
         if list_kind != "default" or flags:
             self._check(self._lib.pis_gpu_set_options(self._h, _ffi.LIST_KIND[list_kind], flags))
 
@@ -125,7 +125,7 @@ class GpuContext:
         self._check(self._lib.pis_gpu_get_stats(self._h, C.byref(s)))
         return {"n_atoms": s.n_atoms, "steps": s.steps, "rebuilds": s.rebuilds, "list_entries": s.list_entries,
                 "list_capacity": s.list_capacity, "cells": tuple(s.cells), "pe": s.pe, "ke": s.ke,
-                "virial": np.array(s.virial).reshape(3, 3)}
+                "virial": np.array(s.virial).reshape(3, 3), "fused_step": bool(s.fused_step)}
 
     def close(self):
         if getattr(self, "_h", None):
