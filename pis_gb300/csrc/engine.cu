@@ -1928,8 +1928,16 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
 // function of the FP64 state (the list build writes them, every drift rewrites them from the build
 // snapshot), so nothing else ever reads a stale buffer. Results equal those of the three separate
 // kernels bit for bit (same arithmetic, same block partial sums).
+// Compiled for five resident blocks per SM with 4-entry batches (at most 51 registers; a few bytes
+// of the FP64 epilogue spill) and four with 8-entry batches: the pair loop is latency-bound and
+// needs the warps (measured on the 2.048M liquid: 4-entry batches 0.48 ms at five blocks, 0.56 ms at
+// four, 0.64 ms unconstrained at 64-72 registers; 8-entry batches 0.55 ms at four, 0.60 at five).
+template <int MIX_BATCH>
+constexpr int step_min_blocks() {
+    return MIX_BATCH == 4 ? 5 : 4;
+}
 template <int ACC, bool ONE, int MIX_BATCH, bool DRIFT>
-__global__ void __launch_bounds__(256) k_step_mixed(const DP P) {
+__global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixed(const DP P) {
     __shared__ double sh[32];
     __shared__ float4 shift[64];
     int s, i;
