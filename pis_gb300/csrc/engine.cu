@@ -996,6 +996,24 @@ __device__ __forceinline__ void fill_shift_table(float4* shift, const SysParams&
     }
 }
 
+// Per-axis image shifts: t[4a + c] = (0, +1, -1, pad) x cell edge along axis a for the axis's
+// 2-bit code c. Three 4-word tables: the lanes of a warp read at most 4 distinct words per axis, so
+// a lookup is one shared-memory wavefront, where the 64-entry float4 table's scattered 16-byte reads
+// conflict on banks (~7 wavefronts per warp-wide lookup).
+__device__ __forceinline__ void fill_shift_axes(float* t, const SysParams& sp) {
+    if (threadIdx.x < 12) {
+        const int a = threadIdx.x >> 2, c = threadIdx.x & 3;
+        t[threadIdx.x] = c == 3 ? 1e18f : (c == 1 ? sp.fcs[a] : (c == 2 ? -sp.fcs[a] : 0.f));
+    }
+}
+__device__ __forceinline__ float3 shift_of(const float4* t, uint32_t code) {
+    const float4 v = t[code];
+    return make_float3(v.x, v.y, v.z);
+}
+__device__ __forceinline__ float3 shift_of(const float* t, uint32_t code) {
+    return make_float3(t[code & 3u], t[4 + ((code >> 2) & 3u)], t[8 + (code >> 4)]);
+}
+
 // Per-atom accumulator of the mixed kernels: FP32 pair terms summed over a batch, batch sums
 // added in FP64 (ACC = 0) or kept as compensated FP32 sums (ACC = 1) and converted at the end.
 template <int ACC>
@@ -1047,13 +1065,13 @@ struct MixLJ {
 // into the accumulator's batch sums.
 // SELF: the list may hold atom i itself (cluster lists), masked by r^2 > 0. pj: the entries'
 // neighbour positions, already gathered.
-template <bool ONE, int NB, int ACC, bool SELF = false>
+template <bool ONE, int NB, int ACC, bool SELF = false, typename SH>
 __device__ __forceinline__ void mixed_pairs_math(const uint32_t (&ent)[NB], const float4 (&pj)[NB], const float4& pi,
-                                                 const float4* shift, const LJDev* tab, const MixLJ& P0,
+                                                 const SH* shift, const LJDev* tab, const MixLJ& P0,
                                                  MixAcc<ACC>& a) {
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
-        const float4 sv = shift[ent[b] >> JBITS];
+        const float3 sv = shift_of(shift, ent[b] >> JBITS);
         const float dx = (pj[b].x - pi.x) + sv.x;
         const float dy = (pj[b].y - pi.y) + sv.y;
         const float dz = (pj[b].z - pi.z) + sv.z;
@@ -1083,9 +1101,9 @@ __device__ __forceinline__ void mixed_pairs_math(const uint32_t (&ent)[NB], cons
     }
 }
 
-template <bool ONE, int NB, int ACC, bool SELF = false>
+template <bool ONE, int NB, int ACC, bool SELF = false, typename SH>
 __device__ __forceinline__ void mixed_pairs(const uint32_t (&ent)[NB], const float4* __restrict__ prel,
-                                            const float4& pi, const float4* shift, const LJDev* tab,
+                                            const float4& pi, const SH* shift, const LJDev* tab,
                                             const MixLJ& P0, MixAcc<ACC>& a) {
     float4 pj[NB];
 #pragma unroll
@@ -1104,9 +1122,9 @@ constexpr int MIX_FLUSH = 32;  // entries per lane between FP64 (or compensated)
 // cell-relative position. Shared by k_force_mixed and the fused step kernel.
 // PF > 0 (thread per atom): the list rows of the batch PF batches ahead are prefetched into L2, so
 // the list words (streamed from DRAM) arrive while the current batch's gathers are in flight.
-template <int ACC, int LPA, bool ONE, int MIX_BATCH, int PF = 0>
+template <int ACC, int LPA, bool ONE, int MIX_BATCH, int PF = 0, typename SH>
 __device__ __forceinline__ float4 mixed_atom_forces(const DP& P, const SysParams& sp, int i, int gl,
-                                                    const float4* shift, MixAcc<ACC>& acc) {
+                                                    const SH* shift, MixAcc<ACC>& acc) {
     const float4* __restrict__ prel = P.prel;
     const float4 pi = prel[i];
     const int ti = __float_as_int(pi.w);
@@ -1152,14 +1170,14 @@ __device__ __forceinline__ float4 mixed_atom_forces(const DP& P, const SysParams
 template <int ACC, int LPA, bool ONE, int MIX_BATCH>
 __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) {
     __shared__ double sh[32];
-    __shared__ float4 shift[64];
+    __shared__ float shift[12];
     auto tile = cg::tiled_partition<LPA>(cg::this_thread_block());
     int s, i;
     const bool live = group_atom_of<LPA>(P, s, i);
     if (s < 0) return;
     if (!slot_runs(P, s, step_mode)) return;
     const SysParams& sp = P.sp[s];
-    fill_shift_table(shift, sp);
+    fill_shift_axes(shift, sp);
     __syncthreads();
     const int gl = (int)tile.thread_rank();
     MixAcc<ACC> acc;
@@ -1954,14 +1972,14 @@ __host__ __device__ constexpr int step_list_prefetch() {
 template <int ACC, bool ONE, int MIX_BATCH, bool DRIFT>
 __global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixed(const DP P) {
     __shared__ double sh[32];
-    __shared__ float4 shift[64];
+    __shared__ float shift[12];
     int s, i;
     const bool live = atom_of(P, s, i);
     if (s < 0) return;
     if (!slot_runs(P, s, 1)) return;
     const SysParams& sp = P.sp[s];
     SysState& st = P.st[s];
-    fill_shift_table(shift, sp);
+    fill_shift_axes(shift, sp);
     __syncthreads();
     MixAcc<ACC> acc;
     if (live) mixed_atom_forces<ACC, 1, ONE, MIX_BATCH, step_list_prefetch<MIX_BATCH>()>(P, sp, i, 0, shift, acc);
