@@ -232,6 +232,7 @@ class Engine {
     bool dirty_map_ = true;
     bool single_type_ = true;  // every active slot has one atom type (selects the force kernel)
     bool fused_ = false;       // mixed steps run the fused force + kick + drift kernel
+    bool list_groups_ = false; // the per-atom list is stored in groups of consecutive entries
     void* prel_buf_[2] = {nullptr, nullptr};  // the two cell-relative coordinate buffers (fused steps)
 };
 
