@@ -815,7 +815,7 @@ __device__ __forceinline__ void build1_chunk(const DP& P, int blk, int step_mode
     SysState& st = P.st[s];
     if (!st.rebuild) return;
     const int nx = sp.nc[0], ny = sp.nc[1], nz = sp.nc[2];
-    if (nx < 3 || ny < 3 || nz < 3) return;  // two-cell axes: the generic kernel handles the slot
+    if (!sp.walk27) return;  // the generic kernel handles the slot
     const int lc = P.cellof[i];
     const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
     const float4 pi = P.prel[i];
@@ -857,19 +857,25 @@ __device__ __forceinline__ void build1_chunk(const DP& P, int blk, int step_mode
     if (cnt > cap) atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
     P.nn[i] = cnt > cap ? cap : cnt;
 }
+// only_two_cell: just the slots with a two-cell axis (the two-stage build covers the others).
 template <bool HALF>
-__global__ void __launch_bounds__(256) k_build1(const DP P, int step_mode) {
+__global__ void __launch_bounds__(256) k_build1(const DP P, int step_mode, int only_two_cell) {
     if (!rebuild_block(P, P.blk_sys, blockIdx.x)) return;
+    if (only_two_cell) {
+        const SysParams& sp = P.sp[P.blk_sys[blockIdx.x]];
+        if (sp.nc[0] >= 3 && sp.nc[1] >= 3 && sp.nc[2] >= 3) return;
+    }
     build1_chunk<HALF>(P, blockIdx.x, step_mode);
 }
 
-// Slots with a two-cell axis: the group kernel's generic path, one lane per atom.
+// Slots the 27-cell walk does not serve (flagged !walk27: a two-cell axis within 1e-5 of twice
+// the list radius): the group kernel's generic path, one lane per atom.
 template <bool HALF>
 __global__ void __launch_bounds__(256) k_build1_generic(const DP P, int step_mode) {
     if (!rebuild_block(P, P.blk_sys, blockIdx.x)) return;
     const int s = P.blk_sys[blockIdx.x];
     const SysParams& sp = P.sp[s];
-    if (sp.nc[0] >= 3 && sp.nc[1] >= 3 && sp.nc[2] >= 3) return;
+    if (sp.walk27) return;
     k_build_body<HALF, 1>(P, blockIdx.x, step_mode);
 }
 
@@ -2764,6 +2770,14 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     p.hdt2 = 0.5 * p.dt2;
     double rl = rlist * (1.0 + 1e-5);
     p.frlist2 = (float)(rl * rl);
+    // The 27-cell walk (k_build1) serves axes of two cells too: there the -1 and +1 neighbours are
+    // the same cell seen through two images, and the box edge (2 cells of at least the list radius)
+    // exceeds twice the padded list radius, so at most one image of a pair passes the distance
+    // test and no pair is listed twice. Only an edge within 1e-5 of that bound is left to the
+    // generic walk, which keeps the nearer image per pair.
+    p.walk27 = 1;
+    for (int a = 0; a < 3; ++a)
+        if (nc[a] < 2 || (nc[a] == 2 && !(p.h[a] > 2.0 * std::sqrt((double)p.frlist2) * (1.0 + 1e-5)))) p.walk27 = 0;
     // chunks
     p.nch = (int32_t)((d.n + opt_.blk - 1) / opt_.blk);
     p.ch0 = 0;  // assigned by the block map
@@ -2953,10 +2967,10 @@ static void launch_build_t(const DP& P, bool half, unsigned chunks, cudaStream_t
     if (L == 1) {
         // lean kernel for slots with >= 3 cells per axis, generic kernel for the rest
         if (half) {
-            k_build1<true><<<g, 256, 0, st>>>(P, r);
+            k_build1<true><<<g, 256, 0, st>>>(P, r, 0);
             k_build1_generic<true><<<g, 256, 0, st>>>(P, r);
         } else {
-            k_build1<false><<<g, 256, 0, st>>>(P, r);
+            k_build1<false><<<g, 256, 0, st>>>(P, r, 0);
             k_build1_generic<false><<<g, 256, 0, st>>>(P, r);
         }
         g_launches.fetch_add(2);
@@ -3083,7 +3097,7 @@ void Engine::launch_build(int r) {
     }
     if (clm_ && opt_.lpa == 1) {
         // two-stage per-atom build: cluster union lists, filtered per member; slots with a
-        // two-cell axis use the generic kernel
+        // two-cell axis use the 27-cell walk (or, at the two-cell edge bound, the generic kernel)
         if (clm_ == 2) {
             k_build_cl<2><<<gc, CL_THREADS, 0, ls_>>>(*d_, r, 1);
             if (half_)
@@ -3097,11 +3111,14 @@ void Engine::launch_build(int r) {
             else
                 k_filter_cl<false, 4><<<gc * 4, CL_THREADS, 0, ls_>>>(*d_, r);
         }
-        if (half_)
+        if (half_) {
+            k_build1<true><<<ga, 256, 0, ls_>>>(*d_, r, 1);
             k_build1_generic<true><<<ga, 256, 0, ls_>>>(*d_, r);
-        else
+        } else {
+            k_build1<false><<<ga, 256, 0, ls_>>>(*d_, r, 1);
             k_build1_generic<false><<<ga, 256, 0, ls_>>>(*d_, r);
-        g_launches.fetch_add(3);
+        }
+        g_launches.fetch_add(4);
         return;
     }
 #define PIS_CALL(L) launch_build_t<L>(*d_, half_, ch, ls_, r)
@@ -3670,6 +3687,10 @@ pis_status Engine::scale_box(int slot, const double* m, std::string& err) {
             err = "box shrank below the cell size; re-create the state to re-grid";
             return PIS_ERR_UNSUPPORTED;
         }
+    // the 27-cell walk's two-cell condition (add_slot) for the new edges
+    p.walk27 = 1;
+    for (int a = 0; a < 3; ++a)
+        if (p.nc[a] < 2 || (p.nc[a] == 2 && !(p.h[a] > 2.0 * std::sqrt((double)p.frlist2) * (1.0 + 1e-5)))) p.walk27 = 0;
     pis_status st = check(cudaMemcpyAsync(d_->sp + slot, &p, sizeof(SysParams), cudaMemcpyHostToDevice, stream_), "params", err);
     if (st) return st;
     int32_t one = 1;

@@ -59,7 +59,7 @@ struct SysParams {
     float fcs[3];
     float frlist2;     // FP32 list radius squared, padded so the FP32 test is a superset
     float fsub[3];     // 4 / cell edge: sub-cell index scale of the in-cell atom order
-    float pad_f;
+    int32_t walk27;    // the 27-cell walk of the thread-per-atom build is valid (see add_slot)
 };
 
 // Device-side pair parameters: FP64 quantities computed exactly as the reference does per pair,

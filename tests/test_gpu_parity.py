@@ -200,6 +200,29 @@ def test_small_box_two_cells(oracle_lib, cuda_lib):
         assert rel_norm(f, o.force) <= tol
 
 
+@pytest.mark.parametrize("edge_margin", [0.5, 2e-6])
+def test_two_cell_box_walks(oracle_lib, cuda_lib, edge_margin):
+    # two cells per axis: the 27-cell walk serves the box when its edge exceeds twice the padded
+    # list radius (margin 0.5: skin 0.3), the generic walk when the edge is within 1e-5 of it
+    # (skin chosen so that rcut + skin = L / 2 (1 - 2e-6)); both must give the all-pairs forces
+    # (a pair listed under two images would count twice)
+    import oracle
+    s = displaced(liquid(nc=5, rho=0.95), 0.02, 4)
+    L = s["h"][0, 0]
+    skin = 0.3 if edge_margin == 0.5 else L / 2 * (1 - edge_margin) - 2.5
+    o = to_oracle(s)
+    pe_ref = o.compute_potential(manager=oracle.ALLPAIRS)
+    for prec in ("fp64", "mixed"):
+        g = to_gpu(s, prec, skin=skin, list_kind="full")
+        assert g.stats()["cells"] == (2, 2, 2)
+        pe, f = g.compute_potential()
+        tol = FP64_TOL if prec == "fp64" else 1e-5
+        assert abs(pe - pe_ref) <= tol * abs(pe_ref)
+        assert rel_norm(f, o.force) <= tol
+        e = g.verlet_step_nve(0.005, 20)
+        assert np.all(np.isfinite(e))
+
+
 def test_errors_are_reported(oracle_lib, cuda_lib):
     from pis_gb300 import PisError
     s = liquid(nc=2)  # L = 3.36 < 2 (rc + skin)
