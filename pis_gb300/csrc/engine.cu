@@ -2859,10 +2859,21 @@ int Engine::n_active() const {
 pis_status Engine::rebuild_block_map(std::string& err) {
     if (!dirty_map_) return PIS_OK;
     std::vector<int32_t> bs(max_chunks_, -1), bf(max_chunks_, 0);
+    // Slots with the most atoms per cell first: their list-build blocks walk the most candidates
+    // per atom (small boxes have cells well above the list radius) and, scheduled last, were the
+    // tail of every rebuild in a mixed pool. A slot's chunks stay consecutive, so its sums and
+    // results do not depend on the order.
+    std::vector<int> order;
+    for (int s = 0; s < opt_.max_slots; ++s)
+        if (hp_[s].active) order.push_back(s);
+    auto per_cell = [&](int s) {
+        const SysParams& p = hp_[s];
+        return (double)p.n / ((double)p.nc[0] * p.nc[1] * p.nc[2]);
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return per_cell(a) > per_cell(b); });
     int64_t c = 0;
-    for (int s = 0; s < opt_.max_slots; ++s) {
+    for (int s : order) {
         SysParams& p = hp_[s];
-        if (!p.active) continue;
         p.ch0 = (int32_t)c;
         for (int k = 0; k < p.nch; ++k, ++c) {
             bs[c] = s;
