@@ -499,6 +499,20 @@ def run_served(args):
         ok = all(r["status"] == 0 for r in res)
         out[name] = {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                      "atom_steps_per_s": work / wall, "wall_s": wall, "all_ok": ok}
+    # arrival-rate sweep of the continuous-batching path (a longer stream per rate)
+    sweep = []
+    for rate in (100.0, 200.0, 400.0, 800.0):
+        rq = serve_requests(4 * args.serve_jobs, seed=78, rate=rate)
+        w = sum(4 * j.k ** 3 * j.steps for _, j in rq)
+        cells = max(lj_pool_cells(j.k, j.rho) for _, j in rq) * 16
+        b = Batch(max_atoms, 64, cells, precision="mixed")
+        res, wall = b.serve(rq, graph_steps=50)
+        b.close()
+        lat = np.array([r["finished_s"] - r["arrival_s"] for r in res])
+        sweep.append({"rate_per_s": rate, "jobs": len(rq), "offered_atom_steps_per_s": w / max(rq[-1][0], 1e-9),
+                      "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+                      "atom_steps_per_s": w / wall, "all_ok": all(r["status"] == 0 for r in res)})
+    out["mixed_rate_sweep"] = sweep
     return out
 
 

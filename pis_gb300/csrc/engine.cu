@@ -282,11 +282,13 @@ __device__ __forceinline__ bool group_atom_of(const DP& P, int& s, int& i) {
 // chunks, left multi-wave tails and was measured slower).
 __device__ __forceinline__ bool rebuild_pending(const DP& P) { return P.ctl[0] != 0; }
 // The request word and the block's first table entry (its slot, or a cell's slot) are loaded
-// together, so both the early exit and a rebuilding block pay one memory latency for them.
+// together, so both the early exit and a rebuilding block pay one memory latency for them; then the
+// slot's own flag, so that in a pool where some slot rebuilds every step (a replica mix) the blocks
+// of the other slots exit after a second load.
 __device__ __forceinline__ bool rebuild_block(const DP& P, const int32_t* slot_table, int64_t idx) {
     const int pending = P.ctl[0];
     const int s = slot_table[idx];
-    return pending != 0 && s >= 0;
+    return pending != 0 && s >= 0 && P.st[s].rebuild != 0;
 }
 
 // Neighbour-list layout: entry k of atom i lives at (k / LPA) * (npad * LPA) + i * LPA + k % LPA.
