@@ -13,6 +13,7 @@
 #include <memory>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "engine.h"
@@ -327,9 +328,37 @@ pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64
     int active = 0;
     const auto t0 = std::chrono::steady_clock::now();
     std::string err;
-    while (finished < n) {
+    // Initial states of queued jobs, generated on the host while the GPU runs the previous graph
+    // (the generation is deterministic per job, so results do not depend on when it happens).
+    struct Prepared {
+        std::vector<double> pos, vel;
+        double L = 0;
+    };
+    std::unordered_map<int32_t, Prepared> ready;
+    auto prepare = [&](int32_t q) {
+        if (ready.count(q)) return;
+        Prepared p;
+        make_lj_state(reqs[q].job, p.pos, p.vel, p.L);
+        ready.emplace(q, std::move(p));
+    };
+    auto admit_ready = [&](int32_t q, int32_t* slot) {
+        prepare(q);
+        Prepared& p = ready[q];
+        const pis_lj_job& job = reqs[q].job;
+        if (job.k < 1 || !(job.rho > 0) || !(job.t_star >= 0) || !(job.rcut > 0))
+            return bfail(b, PIS_ERR_INVALID_ARGUMENT, "bad LJ job parameters");
+        pis::SlotDesc d = lj_desc(job, p.L);
+        std::vector<int32_t> types((size_t)d.n, 1);
+        pis_status st = admit_desc(b, d, types.data(), p.pos.data(), p.vel.data(), job.steps, slot);
+        ready.erase(q);
+        return st;
+    };
+    auto arrivals = [&]() {
         const double now = seconds_since(t0);
         while (next < order.size() && reqs[order[next]].arrival_s <= now) queue.push_back(order[next++]);
+    };
+    while (finished < n) {
+        arrivals();
         // admit in arrival order while the head of the queue fits
         while (!queue.empty()) {
             const int32_t q = queue.front();
@@ -341,7 +370,7 @@ pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64
                 continue;
             }
             int32_t slot = -1;
-            pis_status st = pis_batch_admit_lj(b, &reqs[q].job, &slot);
+            pis_status st = admit_ready(q, &slot);
             queue.pop_front();
             out[q].admitted_s = seconds_since(t0);
             out[q].atoms = 4ll * reqs[q].job.k * reqs[q].job.k * reqs[q].job.k;
@@ -363,6 +392,15 @@ pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64
         }
         pis_status st = b->eng.run(graph_steps, err);
         if (st) return bfail(b, st, err);
+        // while the graph runs: the initial states of the next queued jobs
+        arrivals();
+        {
+            int k = 0;
+            for (int32_t q : queue) {
+                if (k++ >= 8) break;
+                prepare(q);
+            }
+        }
         std::vector<pis::SysState> ss;
         st = b->eng.read_states(ss, err);  // synchronises with the graph
         if (st) return bfail(b, st, err);
