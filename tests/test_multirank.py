@@ -1,5 +1,5 @@
-"""The N > 1 benchmark path on CPU: two gloo ranks launched like the driver launches bench.py
-(torchrun, 127.0.0.1). The path shards by replica, so there is no data-path collective; what is
+"""The N > 1 benchmark path on CPU: two gloo ranks launched the way a multi-GPU benchmark run
+launches bench.py (torchrun, 127.0.0.1). The path shards by replica, so there is no data-path collective; what is
 tested is the launch, the max-over-ranks timing reduction and that rank 0 alone prints."""
 import json
 import os
