@@ -107,3 +107,20 @@ def test_option_flags_match_header():
     assert _ffi.option_flags(cluster=4, lanes=4, scan=0) == (4 << 24) | (4 << 8)
     assert _ffi.option_flags(scan=4, mixed_kahan=True) == (4 << 28) | 2
     assert _ffi.STATUS_NAMES[27] == "PIS_ERR_TIMEOUT"
+    for name, value in (("PIS_OPT_TILE", 8), ("PIS_OPT_PLAIN_GRAPHS", 16), ("PIS_OPT_UNFUSED", 32)):
+        assert f"#define {name} {value}" in text
+    assert _ffi.option_flags(tiles=True) == 8
+    assert _ffi.option_flags(plain_graphs=True, unfused=True) == 16 | 32
+
+
+def test_stats_struct_matches_header():
+    # the ctypes mirror of pis_gpu_stats lists the header's fields in order
+    import ctypes
+    from pis_gb300 import _ffi
+    text = open(os.path.join(ROOT, "include", "pis_gpu.h")).read()
+    body = text[text.index("typedef struct {\n    int64_t n_atoms;"):text.index("} pis_gpu_stats;")]
+    names = [f[0] for f in _ffi.Stats._fields_]
+    for n in names:
+        assert n in body, n
+    assert names[-2:] == ["fused_step", "reserved_"]
+    assert ctypes.sizeof(_ffi.Stats) == 8 * 4 + 4 * 4 + 8 * 11 + 8
