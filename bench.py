@@ -445,7 +445,14 @@ def run_drift(args, melt_pos, melt_vel, types, h, tuned):
     n = len(melt_pos)
     g = GpuContext(TABLE, 1, skin=SKIN, precision="mixed", **tuned)
     g.set_state(melt_pos, types, [1.0], h, velocities=melt_vel)
+    # equilibrate to 2000 steps from the lattice before the NVE record (a liquid still relaxing
+    # from the melt drifts more), as the 256k states below
+    extra = max(0, 2000 - args.equil)
+    if extra:
+        g.compute_potential(want_forces=False)
+        g.run_timed(DT, extra)
     out["mixed_2m"] = drift_stats(energy_series(g, args.drift_steps, 500), n, 500)
+    out["mixed_2m"]["equilibration_steps"] = args.equil + extra
     g.close()
     pos, vel, L = lj_liquid(40, RHO, TSTAR, 4)
     ns = len(pos)
