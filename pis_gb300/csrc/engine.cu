@@ -3368,6 +3368,34 @@ pis_status Engine::compute_potential_slot(int only, std::string& err) {
     return reduce_state_slot(true, only, err);
 }
 
+// Force evaluation and reductions for a set of slots (each marked, then one kernel sequence for
+// all): the serving loop evaluates the jobs it admits between two graphs together. Every slot's
+// results are those of compute_potential_slot on it alone.
+pis_status Engine::compute_potential_slots(const std::vector<int>& slots, std::string& err) {
+    if (slots.empty()) return PIS_OK;
+    pis_status st = rebuild_block_map(err);
+    if (st) return st;
+    const DP& P = *d_;
+    const unsigned sg = (unsigned)((opt_.max_slots + 127) / 128);
+    for (int s : slots) LAUNCH(k_mark_eval, sg, 128, P, s, 1, 0);
+    LAUNCH(k_zero_forces, (unsigned)max_chunks_, opt_.blk, P);
+    enqueue_rebuild(false);
+    if (opt_.precision == PIS_PRECISION_MIXED)
+        launch_force_mixed(0);
+    else
+        launch_force_fp64(0);
+    LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 1);
+    for (int s : slots) LAUNCH(k_mark_eval, sg, 128, P, s, 0, 1);
+    if (opt_.precision == PIS_PRECISION_MIXED)
+        LAUNCH((k_integrate2<false, false>), (unsigned)max_chunks_, opt_.blk, P, 0);
+    else
+        LAUNCH((k_integrate2<false, true>), (unsigned)max_chunks_, opt_.blk, P, 0);
+    LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 2);
+    st = check(cudaGetLastError(), "launch", err);
+    if (st) return st;
+    return sync(err);
+}
+
 pis_status Engine::reduce_state(bool virial, std::string& err) { return reduce_state_slot(virial, -1, err); }
 
 pis_status Engine::reduce_state_slot(bool virial, int only, std::string& err) {

@@ -137,6 +137,8 @@ class Engine {
     pis_status compute_potential(std::string& err);
     // The same for one slot only (the others keep their state untouched).
     pis_status compute_potential_slot(int slot, std::string& err);
+    // The same for several slots at once (one kernel sequence; each slot's results as alone).
+    pis_status compute_potential_slots(const std::vector<int>& slots, std::string& err);
     // Run k velocity-Verlet steps on every active slot with steps_left > 0 (graph chunks).
     pis_status run(int64_t k, std::string& err);
     // KE and virial of every active slot at the current state.

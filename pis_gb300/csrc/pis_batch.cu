@@ -105,13 +105,15 @@ pis::SlotDesc lj_desc(const pis_lj_job& j, double L) {
     return d;
 }
 
-pis_status admit_desc(pis_batch* b, const pis::SlotDesc& d, const int32_t* types, const double* pos,
-                      const double* vel, int64_t steps, int32_t* slot_out) {
+// Place a job in the pool and set its step count; `evaluate`: also its first force evaluation
+// (otherwise the caller evaluates the new slots together, Engine::compute_potential_slots).
+pis_status place_desc(pis_batch* b, const pis::SlotDesc& d, const int32_t* types, const double* pos,
+                      const double* vel, int64_t steps, bool evaluate, int32_t* slot_out) {
     if (steps < 0) return bfail(b, PIS_ERR_INVALID_ARGUMENT, "negative step count");
     std::string err;
     int slot = b->eng.add_slot(d, types, pos, vel, nullptr, err);
     if (slot < 0) return bfail(b, (pis_status)(-slot), err);
-    pis_status st = b->eng.compute_potential_slot(slot, err);
+    pis_status st = evaluate ? b->eng.compute_potential_slot(slot, err) : PIS_OK;
     if (!st) st = b->eng.set_steps(slot, steps, err);
     if (st) {
         b->eng.remove_slot(slot);
@@ -121,6 +123,11 @@ pis_status admit_desc(pis_batch* b, const pis::SlotDesc& d, const int32_t* types
     b->atoms[slot] = d.n;
     if (slot_out) *slot_out = slot;
     return PIS_OK;
+}
+
+pis_status admit_desc(pis_batch* b, const pis::SlotDesc& d, const int32_t* types, const double* pos,
+                      const double* vel, int64_t steps, int32_t* slot_out) {
+    return place_desc(b, d, types, pos, vel, steps, true, slot_out);
 }
 
 double seconds_since(std::chrono::steady_clock::time_point t0) {
@@ -349,7 +356,8 @@ pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64
             return bfail(b, PIS_ERR_INVALID_ARGUMENT, "bad LJ job parameters");
         pis::SlotDesc d = lj_desc(job, p.L);
         std::vector<int32_t> types((size_t)d.n, 1);
-        pis_status st = admit_desc(b, d, types.data(), p.pos.data(), p.vel.data(), job.steps, slot);
+        // placed now, evaluated with the other jobs admitted before the next graph
+        pis_status st = place_desc(b, d, types.data(), p.pos.data(), p.vel.data(), job.steps, false, slot);
         ready.erase(q);
         return st;
     };
@@ -360,6 +368,7 @@ pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64
     while (finished < n) {
         arrivals();
         // admit in arrival order while the head of the queue fits
+        std::vector<int> fresh;
         while (!queue.empty()) {
             const int32_t q = queue.front();
             if (!pis_batch_fits_lj(b, &reqs[q].job)) {
@@ -381,7 +390,12 @@ pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64
                 continue;
             }
             slot_req[slot] = q;
+            fresh.push_back(slot);
             ++active;
+        }
+        if (!fresh.empty()) {
+            pis_status st = b->eng.compute_potential_slots(fresh, err);
+            if (st) return bfail(b, st, err);
         }
         if (active == 0) {
             if (next < order.size()) {
