@@ -61,7 +61,17 @@ pis_status pis_system_run(pis_system* s, const char* thermo_path);
 int64_t pis_system_steps(const pis_system* s);
 double pis_system_timestep(const pis_system* s);
 int32_t pis_system_ensemble(const pis_system* s); /* 0 NVE, 1 NVT, 2 NPT (simulation.rs:118-132) */
+/* Positions, velocities and forces (x,y,z per atom; any pointer may be NULL). Before the run
+ * has put the state on the GPU: the state contextualize built (positions as read, velocities as
+ * read or drawn by `velocity create`, zero forces). */
 pis_status pis_system_state(pis_system* s, double* pos, double* vel, double* force);
+/* The pair table contextualize built (the data file's PairCoeffs, replaced by `pair_style lj/cut`
+ * and its `pair_coeff` rows when those are given, src/system.rs:120-168): writes up to `cap`
+ * entries to `out` (may be NULL) and returns how many there are. */
+int32_t pis_system_pairs(const pis_system* s, pis_lj_pair* out, int32_t cap);
+/* The `dump` command's step and file name (run_dump, src/readers/input_file/commands.rs:485-496;
+ * defaults 1 and "dump.lammpstrj"); `file` receives at most cap - 1 characters. */
+pis_status pis_system_dump(const pis_system* s, int64_t* dump_step, char* file, int32_t cap);
 const char* pis_system_last_error(const pis_system* s);
 void pis_system_close(pis_system* s);
 

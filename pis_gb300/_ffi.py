@@ -36,6 +36,7 @@ class PisError(RuntimeError):
     def __init__(self, status: int, message: str):
         self.status = status
         self.name = STATUS_NAMES.get(status, f"status {status}")
+        self.message = message
         super().__init__(f"{self.name}: {message}")
 
 
@@ -134,6 +135,8 @@ HOST_SIGNATURES = [
     ("pis_system_timestep", C.c_double, [_VP]),
     ("pis_system_ensemble", C.c_int32, [_VP]),
     ("pis_system_state", C.c_int, [_VP, _DP, _DP, _DP]),
+    ("pis_system_pairs", C.c_int32, [_VP, C.POINTER(LJPair), C.c_int32]),
+    ("pis_system_dump", C.c_int, [_VP, C.POINTER(C.c_int64), C.c_char_p, C.c_int32]),
     ("pis_system_last_error", C.c_char_p, [_VP]),
     ("pis_system_close", None, [_VP]),
 ]

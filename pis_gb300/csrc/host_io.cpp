@@ -113,11 +113,41 @@ std::string format_f64(double v) {
     return neg ? "-" + out : out;
 }
 
+std::string int_parse_message(const std::string& t) {
+    // core::num::IntErrorKind for i32::from_str: an optional sign, then at least one digit; a
+    // token of digits that parse_i32 rejected overflowed
+    const char* why;
+    if (t.empty()) {
+        why = "cannot parse integer from empty string";
+    } else {
+        const size_t k = (t[0] == '+' || t[0] == '-') ? 1 : 0;
+        bool digits = k < t.size();
+        for (size_t q = k; q < t.size(); ++q)
+            if (t[q] < '0' || t[q] > '9') digits = false;
+        why = !digits ? "invalid digit found in string"
+              : t[0] == '-' ? "number too small to fit in target type"
+                            : "number too large to fit in target type";
+    }
+    return "Error parsing integer number from string " + t + ": " + why;
+}
+
+std::string float_parse_message(const std::string& t) {
+    return "Error parsing floating number from string " + t + ": " +
+           (t.empty() ? "cannot parse float from empty string" : "invalid float literal");
+}
+
+std::string open_error_message(const std::string& path, int os_errno) {
+    // the reference's format string closes with a stray ')' (src/errors.rs:7)
+    return "Failed to open input file '" + path + "': " + std::strerror(os_errno) + " (os error " +
+           std::to_string(os_errno) + "))";
+}
+
 // run_read_data (src/readers/input_file/commands.rs:147-384).
 pis_status read_data_file(const std::string& path, DataFile& d, std::string& err) {
+    errno = 0;
     std::ifstream in(path);
     if (!in) {
-        err = "Failed to open input file '" + path + "'";
+        err = open_error_message(path, errno ? errno : ENOENT);
         return PIS_ERR_IO;
     }
     d = DataFile();
@@ -137,7 +167,7 @@ pis_status read_data_file(const std::string& path, DataFile& d, std::string& err
         pis_status st = req(sp, k, tok);
         if (st) return st;
         if (!parse_i32(tok, v)) {
-            err = "Error parsing integer number from string " + tok;
+            err = int_parse_message(tok);
             return PIS_ERR_PARSE;
         }
         return PIS_OK;
@@ -158,7 +188,7 @@ pis_status read_data_file(const std::string& path, DataFile& d, std::string& err
         pis_status st = req(sp, k, tok);
         if (st) return st;
         if (!parse_f64(tok, v)) {
-            err = "Error parsing floating number from string " + tok;
+            err = float_parse_message(tok);
             return PIS_ERR_PARSE;
         }
         return PIS_OK;

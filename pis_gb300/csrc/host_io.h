@@ -23,6 +23,12 @@ struct DataFile {
 
 bool parse_i32(const std::string& t, int32_t& out);
 bool parse_f64(const std::string& t, double& out);
+// Messages of PisError::IntParseError / FloatParseError (src/errors.rs:29-41) for a token that
+// parse_i32 / parse_f64 rejected, with the text Rust's ParseIntError / ParseFloatError displays.
+std::string int_parse_message(const std::string& t);
+std::string float_parse_message(const std::string& t);
+// PisError::InputFileError (src/errors.rs:7): the path and the OS error as Rust's io::Error shows it.
+std::string open_error_message(const std::string& path, int os_errno);
 std::vector<std::string> split_ws(const std::string& line);
 std::string trim(const std::string& s);
 std::string format_f64(double v);

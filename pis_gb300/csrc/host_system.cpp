@@ -4,6 +4,8 @@
 // (src/simulation.rs:8-88) steps the ensemble, prints thermo lines and writes .lammpstrj dumps
 // (src/writers/dump_traj.rs:18-74). NVE and the Nose-Hoover-chain NVT (src/ensemble/nvt.rs) run;
 // NPT needs a triclinic box update, which the GPU engine does not support.
+#include <algorithm>
+#include <cerrno>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -93,7 +95,9 @@ struct pis_system {
     StartVelocity sv;
     bool have_style = false;
     std::vector<std::string> style_args;
+    int style_line = 0;
     std::vector<std::vector<std::string>> coeff_args;
+    std::vector<int> coeff_lines;
     NhcArgs nhc;
     MtkArgs mtk;
     int64_t dump_step = 1;
@@ -116,11 +120,25 @@ pis_status sfail(pis_system* s, pis_status st, const std::string& m) {
     return st;
 }
 
+// PisError::MissingArgument / NegativeValue / InvalidArgument (src/errors.rs:26-48)
+pis_status missing_argument(pis_system* s, int line) {
+    return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Missing argument on line " + std::to_string(line));
+}
+pis_status negative_value(pis_system* s, int32_t v, int line) {
+    return sfail(s, PIS_ERR_INVALID_ARGUMENT,
+                 "Negative value " + std::to_string(v) + " not allowed on line: " + std::to_string(line));
+}
+pis_status invalid_argument(pis_system* s, const std::string& t, int line) {
+    return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Invalid argument: " + t + " at line: " + std::to_string(line));
+}
+
 // One command line (src/readers/input_file/commands.rs:25-63, 66-144, 387-496).
 pis_status run_command(pis_system* s, const std::string& cmd, const std::vector<std::string>& a, int line) {
-    auto missing = [&]() { return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Missing argument on line " + std::to_string(line)); };
-    auto bad_f = [&](const std::string& t) { return sfail(s, PIS_ERR_PARSE, "Error parsing floating number from string " + t); };
-    auto bad_i = [&](const std::string& t) { return sfail(s, PIS_ERR_PARSE, "Error parsing integer number from string " + t); };
+    auto missing = [&]() { return missing_argument(s, line); };
+    auto bad_f = [&](const std::string& t) { return sfail(s, PIS_ERR_PARSE, pis::float_parse_message(t)); };
+    auto bad_i = [&](const std::string& t) { return sfail(s, PIS_ERR_PARSE, pis::int_parse_message(t)); };
+    auto negative = [&](int32_t v) { return negative_value(s, v, line); };
+    auto invalid = [&](const std::string& t) { return invalid_argument(s, t, line); };
     if (cmd == "timestep") {
         if (a.empty()) return missing();
         if (!parse_f64(a[0], s->timestep)) return bad_f(a[0]);
@@ -128,11 +146,11 @@ pis_status run_command(pis_system* s, const std::string& cmd, const std::vector<
         int32_t v;
         if (a.empty()) return missing();
         if (!parse_i32(a[0], v)) return bad_i(a[0]);
-        if (v < 0) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Negative value not allowed on line " + std::to_string(line));
+        if (v < 0) return negative(v);
         s->steps = v;
     } else if (cmd == "velocity") {
         if (a.size() < 2) return missing();
-        if (a[1] != "create") return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Invalid argument: " + a[1]);
+        if (a[1] != "create") return invalid(a[1]);
         StartVelocity v;
         v.present = true;
         size_t k = 2;
@@ -144,16 +162,16 @@ pis_status run_command(pis_system* s, const std::string& cmd, const std::vector<
         v.has_seed = true;
         v.seed = 0;
         if (k < a.size() && parse_i32(a[k], seed)) {
-            if (seed < 0) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Negative value not allowed");
+            if (seed < 0) return negative(seed);
             v.seed = seed;
             ++k;
         }
         while (k < a.size()) {
             const std::string& kw = a[k++];
-            if (kw != "dist") return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Invalid argument: " + kw);
+            if (kw != "dist") return invalid(kw);
             if (k >= a.size()) return missing();
             const std::string& d = a[k++];
-            if (d != "uniform" && d != "gaussian") return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Invalid argument: " + d);
+            if (d != "uniform" && d != "gaussian") return invalid(d);
         }
         s->sv = v;  // replaces whatever read_data set (commands.rs:139)
     } else if (cmd == "read_data") {
@@ -176,7 +194,7 @@ pis_status run_command(pis_system* s, const std::string& cmd, const std::vector<
         while (k < a.size()) {
             const std::string& kw = a[k++];
             double x[3];
-            if (kw != "temp" && kw != "iso") return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Invalid argument: " + kw);
+            if (kw != "temp" && kw != "iso") return invalid(kw);
             for (int q = 0; q < 3; ++q) {
                 if (k >= a.size()) return missing();
                 if (!parse_f64(a[k], x[q])) return bad_f(a[k]);
@@ -197,17 +215,20 @@ pis_status run_command(pis_system* s, const std::string& cmd, const std::vector<
     } else if (cmd == "pair_style") {
         s->have_style = true;
         s->style_args = a;
+        s->style_line = line;
         s->coeff_args.clear();
+        s->coeff_lines.clear();
     } else if (cmd == "pair_coeff") {
         if (!s->have_style)
             return sfail(s, PIS_ERR_MISSING_POTENTIAL,
                          "Potential manager not initialized - missing pair_style or pair_coeff commands");
         s->coeff_args.push_back(a);
+        s->coeff_lines.push_back(line);
     } else if (cmd == "dump") {
         if (a.size() < 4) return missing();
         int32_t v;
         if (!parse_i32(a[3], v)) return bad_i(a[3]);
-        if (v < 0) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Negative value not allowed");
+        if (v < 0) return negative(v);
         if (a.size() < 5) return missing();
         s->dump_step = v;
         s->dump_file = a[4];
@@ -236,26 +257,37 @@ pis_status contextualize(pis_system* s) {
     }
     s->table = s->data.pairs;  // the data file's PairCoeffs manager (commands.rs:367-369)
     if (s->have_style) {
-        if (s->style_args.empty()) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Missing argument");
+        // the arguments are parsed in order, each failure reported at its own line
+        // (src/system.rs:120-168)
+        if (s->style_args.empty()) return missing_argument(s, s->style_line);
         if (s->style_args[0] != "lj/cut")
             return sfail(s, PIS_ERR_UNKNOWN_PAIR_STYLE, "Unknown pair style: '" + s->style_args[0] + "'");
         double rc_global;
-        if (s->style_args.size() < 2) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Missing argument");
+        if (s->style_args.size() < 2) return missing_argument(s, s->style_line);
         if (!parse_f64(s->style_args[1], rc_global))
-            return sfail(s, PIS_ERR_PARSE, "Error parsing floating number from string " + s->style_args[1]);
+            return sfail(s, PIS_ERR_PARSE, pis::float_parse_message(s->style_args[1]));
         s->table.clear();
-        for (const auto& c : s->coeff_args) {
-            int32_t i, j;
-            double eps, sigma, rc;
-            if (c.size() < 4) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Missing argument");
-            if (!parse_i32(c[0], i) || !parse_i32(c[1], j)) return sfail(s, PIS_ERR_PARSE, "Error parsing integer");
-            if (i < 0 || j < 0) return sfail(s, PIS_ERR_INVALID_ARGUMENT, "Negative value not allowed");
-            if (!parse_f64(c[2], eps) || !parse_f64(c[3], sigma)) return sfail(s, PIS_ERR_PARSE, "Error parsing float");
+        for (size_t r = 0; r < s->coeff_args.size(); ++r) {
+            const std::vector<std::string>& c = s->coeff_args[r];
+            const int line = s->coeff_lines[r];
+            int32_t ij[2];
+            double x[2];
+            for (int q = 0; q < 2; ++q) {
+                if ((size_t)q >= c.size()) return missing_argument(s, line);
+                if (!parse_i32(c[q], ij[q])) return sfail(s, PIS_ERR_PARSE, pis::int_parse_message(c[q]));
+                if (ij[q] < 0) return negative_value(s, ij[q], line);
+            }
+            for (int q = 0; q < 2; ++q) {
+                if ((size_t)(q + 2) >= c.size()) return missing_argument(s, line);
+                if (!parse_f64(c[q + 2], x[q])) return sfail(s, PIS_ERR_PARSE, pis::float_parse_message(c[q + 2]));
+            }
+            const int32_t i = ij[0], j = ij[1];
+            double rc;
             if (c.size() < 5 || !parse_f64(c[4], rc)) rc = rc_global;
             // the reference keys the table by (i, j) as written and looks pairs up by (min, max):
             // a row written with i > j is never found, so it is not entered here either
             if (i > j) continue;
-            pis_lj_pair p{i, j, eps, sigma, rc, 1};
+            pis_lj_pair p{i, j, x[0], x[1], rc, 1};
             bool replaced = false;
             for (auto& q : s->table)
                 if (q.ti == i && q.tj == j) {
@@ -293,8 +325,13 @@ pis_status pis_system_open(const char* infile, int32_t precision, double skin, p
     auto s = std::make_unique<pis_system>();
     s->precision = precision;
     s->skin = skin;
+    errno = 0;
     std::ifstream in(infile);
-    if (!in) return PIS_ERR_IO;
+    if (!in) {
+        s->err = pis::open_error_message(infile, errno ? errno : ENOENT);
+        *out = s.release();
+        return PIS_ERR_IO;
+    }
     std::string raw;
     int line = 0;
     while (std::getline(in, raw)) {
@@ -328,8 +365,32 @@ const char* pis_system_last_error(const pis_system* s) { return s ? s->err.c_str
 void pis_system_close(pis_system* s) { delete s; }
 
 pis_status pis_system_state(pis_system* s, double* pos, double* vel, double* force) {
-    if (!s || !s->ctx) return PIS_ERR_STATE;
-    return pis_gpu_get_state(s->ctx, pos, vel, force);
+    if (!s) return PIS_ERR_INVALID_ARGUMENT;
+    if (s->ctx) return pis_gpu_get_state(s->ctx, pos, vel, force);
+    if (!s->have_atoms) return sfail(s, PIS_ERR_NO_ATOMS, "No atoms defined in input file");
+    const size_t m = 3 * (size_t)s->data.n;
+    if (pos) std::memcpy(pos, s->data.pos.data(), sizeof(double) * m);
+    if (vel) std::memcpy(vel, s->data.vel.data(), sizeof(double) * m);
+    if (force) std::memset(force, 0, sizeof(double) * m);
+    return PIS_OK;
+}
+
+int32_t pis_system_pairs(const pis_system* s, pis_lj_pair* out, int32_t cap) {
+    if (!s) return 0;
+    const int32_t n = (int32_t)s->table.size();
+    for (int32_t k = 0; out && k < n && k < cap; ++k) out[k] = s->table[k];
+    return n;
+}
+
+pis_status pis_system_dump(const pis_system* s, int64_t* dump_step, char* file, int32_t cap) {
+    if (!s) return PIS_ERR_INVALID_ARGUMENT;
+    if (dump_step) *dump_step = s->dump_step;
+    if (file && cap > 0) {
+        const size_t k = std::min(s->dump_file.size(), (size_t)cap - 1);
+        std::memcpy(file, s->dump_file.data(), k);
+        file[k] = '\0';
+    }
+    return PIS_OK;
 }
 
 pis_status pis_system_run(pis_system* s, const char* thermo_path) {
@@ -347,6 +408,10 @@ pis_status pis_system_run(pis_system* s, const char* thermo_path) {
     if (!dump) return sfail(s, PIS_ERR_IO, "Failed to create trajectory file '" + s->dump_file + "'");
     const pis::DataFile& d = s->data;
     const int64_t n = d.n;
+    if (s->ctx) {  // a second run starts again from the input's state
+        pis_gpu_destroy(s->ctx);
+        s->ctx = nullptr;
+    }
     pis_status st = pis_gpu_create(s->table.data(), (int32_t)s->table.size(), s->n_types, s->skin, s->precision, &s->ctx);
     if (st) return sfail(s, st, "pis_gpu_create failed");
     const double h[3] = {d.bounds[1] - d.bounds[0], d.bounds[3] - d.bounds[2], d.bounds[5] - d.bounds[4]};

@@ -113,6 +113,23 @@ class System:
             raise PisError(st, self._lib.pis_system_last_error(self._h).decode())
         return pos, vel, frc
 
+    def pairs(self) -> dict:
+        """The LJ table the input built: {(ti, tj): (epsilon, sigma, rcut)}."""
+        n = self._lib.pis_system_pairs(self._h, None, 0)
+        buf = (_ffi.LJPair * max(n, 1))()
+        self._lib.pis_system_pairs(self._h, buf, n)
+        return {(buf[k].ti, buf[k].tj): (buf[k].epsilon, buf[k].sigma, buf[k].rcut) for k in range(n)}
+
+    @property
+    def dump(self):
+        """(dump_step, file name) of the input's dump command."""
+        step = C.c_int64()
+        name = C.create_string_buffer(4096)
+        st = self._lib.pis_system_dump(self._h, C.byref(step), name, 4096)
+        if st != 0:
+            raise PisError(st, self._lib.pis_system_last_error(self._h).decode())
+        return int(step.value), name.value.decode()
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.pis_system_close(self._h)
