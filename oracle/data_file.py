@@ -10,7 +10,12 @@ including its quirks:
   ``1 2 eps sigma rcut`` therefore overwrites the (1,1) entry with eps=2, sigma=eps,
   rcut=sigma;
 * the default cutoff is 2.5 sigma (:267, :280);
-* a ``Velocities`` section switches off Maxwell-Boltzmann initialisation (:194-197).
+* a ``Velocities`` section switches off Maxwell-Boltzmann initialisation (:194-197);
+* errors carry the display strings of src/errors.rs with the 0-based line number that
+  ``reader.lines().enumerate()`` gives (:173), and parse errors end with the text Rust's
+  ``ParseIntError`` / ``ParseFloatError`` display;
+* one deviation: a ``Masses`` row whose type exceeds the declared type count indexes past the
+  end of the reference's vector (a panic); here it is an ``InvalidAtomType`` error.
 """
 from __future__ import annotations
 
@@ -28,25 +33,31 @@ class DataFileError(ValueError):
 
 
 def parse_int(tok: str) -> int:
-    """Rust ``str::parse::<i32>``."""
+    """Rust ``str::parse::<i32>`` (PisError::IntParseError, src/errors.rs:36-41)."""
     if not _INT_RE.match(tok):
-        raise DataFileError(f"Error parsing integer number from string {tok}")
+        why = "cannot parse integer from empty string" if not tok else "invalid digit found in string"
+        raise DataFileError(f"Error parsing integer number from string {tok}: {why}")
     v = int(tok)
-    if not (-(2 ** 31) <= v < 2 ** 31):
-        raise DataFileError(f"Error parsing integer number from string {tok}")
+    if v >= 2 ** 31:
+        raise DataFileError(f"Error parsing integer number from string {tok}: number too large to fit in target type")
+    if v < -(2 ** 31):
+        raise DataFileError(f"Error parsing integer number from string {tok}: number too small to fit in target type")
     return v
 
 
 def parse_float(tok: str) -> float:
-    """Rust ``str::parse::<f64>`` (decimal and inf/nan spellings, no hex)."""
+    """Rust ``str::parse::<f64>`` (decimal and inf/nan spellings, no hex; PisError::FloatParseError,
+    src/errors.rs:29-34)."""
     if not _FLOAT_RE.match(tok):
-        raise DataFileError(f"Error parsing floating number from string {tok}")
+        why = "cannot parse float from empty string" if not tok else "invalid float literal"
+        raise DataFileError(f"Error parsing floating number from string {tok}: {why}")
     return float(tok)
 
 
-def _usize(v: int) -> int:
+def _usize(v: int, line: int = 0) -> int:
+    """``Int32ToUsize::convert_to_usize`` (src/extensions.rs:37-44)."""
     if v < 0:
-        raise DataFileError(f"Negative value {v} not allowed")
+        raise DataFileError(f"Negative value {v} not allowed on line: {line}")
     return v
 
 
@@ -63,7 +74,7 @@ def read_data(path: str) -> dict:
 
     with open(path, "r") as fh:
         lines = fh.read().splitlines()
-    for line in lines:
+    for line_num, line in enumerate(lines):
         line = line.strip()
         if not line or line.startswith("#"):
             continue
@@ -78,13 +89,13 @@ def read_data(path: str) -> dict:
             continue
         if len(sp) > 1:
             if sp[1] == "atoms":
-                n_atoms = _usize(parse_int(sp[0]))
+                n_atoms = _usize(parse_int(sp[0]), line_num)
                 type_ids = np.zeros(n_atoms, dtype=np.int32)
                 positions = np.zeros((n_atoms, 3))
                 velocities = np.zeros((n_atoms, 3))
                 continue
             if sp[1] == "atom":
-                n_types = _usize(parse_int(sp[0]))
+                n_types = _usize(parse_int(sp[0]), line_num)
                 masses = (masses + [0.0] * n_types)[:n_types]
                 continue
         if len(sp) > 2:
@@ -100,11 +111,11 @@ def read_data(path: str) -> dict:
 
         def req(k):
             if k >= len(sp):
-                raise DataFileError("Missing argument")
+                raise DataFileError(f"Missing argument on line {line_num}")
             return sp[k]
 
         if section == "Masses":
-            t = _usize(parse_int(req(0)))
+            t = _usize(parse_int(req(0)), line_num)
             m = parse_float(req(1))
             if t < 1:
                 raise DataFileError(f"Atom type {t} out of range")
@@ -112,7 +123,7 @@ def read_data(path: str) -> dict:
                 raise DataFileError(f"Atom type {t} out of range")
             masses[t - 1] = m
         elif section == "PairCoeffs":
-            i = _usize(parse_int(req(0)))
+            i = _usize(parse_int(req(0)), line_num)
             try:
                 eps = parse_float(req(1))
                 single = True
@@ -126,7 +137,7 @@ def read_data(path: str) -> dict:
                     rc = 2.5 * sigma
                 table[(i, i)] = (eps, sigma, rc)
             else:
-                j = _usize(parse_int(req(1)))
+                j = _usize(parse_int(req(1)), line_num)
                 eps = parse_float(req(2))
                 sigma = parse_float(req(3))
                 try:
@@ -135,14 +146,14 @@ def read_data(path: str) -> dict:
                     rc = 2.5 * sigma
                 table[(i, j)] = (eps, sigma, rc)
         elif section == "Atoms":
-            aid = _usize(parse_int(req(0)))
+            aid = _usize(parse_int(req(0)), line_num)
             if aid == 0 or aid > n_atoms:
                 raise DataFileError(f"Atom count mismatch: expected {n_atoms}, found {aid}")
-            t = _usize(parse_int(req(1)))
+            t = _usize(parse_int(req(1)), line_num)
             type_ids[aid - 1] = t
             positions[aid - 1] = [parse_float(req(2)), parse_float(req(3)), parse_float(req(4))]
         elif section == "Velocities":
-            aid = _usize(parse_int(req(0)))
+            aid = _usize(parse_int(req(0)), line_num)
             if aid == 0 or aid > n_atoms:
                 raise DataFileError(f"Atom count mismatch: expected {n_atoms}, found {aid}")
             velocities[aid - 1] = [parse_float(req(1)), parse_float(req(2)), parse_float(req(3))]

@@ -105,3 +105,41 @@ def test_input_file_parsing(io, tmp_path):
     with pytest.raises(PisError) as e:
         io.System(str(inp))
     assert e.value.name == "PIS_ERR_MISSING_POTENTIAL"
+
+
+_HEAD = "# t\n2 atoms\n1 atom types\n0 4 xlo xhi\n0 4 ylo yhi\n0 4 zlo zhi\n"
+
+
+@pytest.mark.parametrize("text,status", [
+    ("x atoms\n", "PIS_ERR_PARSE"),
+    ("-2 atoms\n", "PIS_ERR_INVALID_ARGUMENT"),
+    ("99999999999 atoms\n", "PIS_ERR_PARSE"),
+    ("2 atoms\n1 atom types\n0 a xlo xhi\n", "PIS_ERR_PARSE"),
+    (_HEAD + "Masses\n1\n", "PIS_ERR_INVALID_ARGUMENT"),
+    (_HEAD + "Masses\n0 1.0\n", "PIS_ERR_INVALID_ATOM_TYPE"),
+    (_HEAD + "Masses\n2 1.0\n", "PIS_ERR_INVALID_ATOM_TYPE"),
+    (_HEAD + "Masses\n1 heavy\n", "PIS_ERR_PARSE"),
+    (_HEAD + "PairCoeffs\n1\n", "PIS_ERR_INVALID_ARGUMENT"),
+    (_HEAD + "PairCoeffs\n1 2 x 1.0\n", "PIS_ERR_PARSE"),
+    (_HEAD + "PairCoeffs\n1 a 1.0 1.0\n", "PIS_ERR_PARSE"),
+    (_HEAD + "PairCoeffs\n-1 1.0 1.0\n", "PIS_ERR_INVALID_ARGUMENT"),
+    (_HEAD + "Atoms\n3 1 0 0 0\n", "PIS_ERR_ATOM_COUNT"),
+    (_HEAD + "Atoms\n\n1 1 0 0\n", "PIS_ERR_INVALID_ARGUMENT"),
+    (_HEAD + "Atoms\n1 -1 0 0 0\n", "PIS_ERR_INVALID_ARGUMENT"),
+    (_HEAD + "Atoms\n1 1 0 0 0\nVelocities\n0 0 0 0\n", "PIS_ERR_ATOM_COUNT"),
+    (_HEAD + "Atoms\n1 1 0 0 0\nVelocities\n1 0 0 fast\n", "PIS_ERR_PARSE"),
+])
+def test_reader_error_messages_match_oracle(io, tmp_path, text, status):
+    # the library's reader and the oracle's restatement fail on the same line with the same
+    # PisError display string (src/errors.rs; 0-based data-file line numbers)
+    import oracle
+    from oracle.data_file import DataFileError
+    from pis_gb300 import PisError
+    p = tmp_path / "bad.txt"
+    p.write_text(text)
+    with pytest.raises(PisError) as e:
+        io.read_data(str(p))
+    with pytest.raises(DataFileError) as o:
+        oracle.read_data(str(p))
+    assert e.value.name == status
+    assert e.value.message == str(o.value)
