@@ -326,3 +326,20 @@ def test_read_data_velocities_switch_off_the_draw(pio, tmp_path):
         _, vel, _ = s.state(2)
         s.close()
         assert np.array_equal(vel, [[0.1, 0.2, 0.3], [0.4, 0.5, 0.6]])
+
+
+def test_reference_example_input(pio, monkeypatch):
+    # the reference's own run script (example/input.pis, run from the reference's root as its
+    # test_command.sh does): every command it uses parses, and contextualize builds its state
+    import os
+    from conftest import REFERENCE
+    if not os.path.exists(os.path.join(REFERENCE, "example", "input.pis")):
+        pytest.skip("reference sources not mounted")
+    monkeypatch.chdir(REFERENCE)
+    s = pio.System("example/input.pis")
+    assert s.timestep == 0.25 and s.steps == 3000 and s.ensemble == "NPT"
+    assert s.dump == (10, "dump.lammpstrj")
+    assert s.pairs() == {(1, 1): (0.238, 3.405, 8.5)}  # the data file's PairCoeffs
+    _, vel, _ = s.state(4000)
+    s.close()
+    assert np.array_equal(vel, pio.maxwell_boltzmann(np.full(4000, 39.948), 5.0, 12345))
