@@ -55,6 +55,11 @@ class _System(C.Structure):
     ]
 
 
+class _Nhc(C.Structure):
+    _fields_ = [("m", C.c_int32), ("t_start", C.c_double), ("t_end", C.c_double), ("t_target", C.c_double),
+                ("xi", C.c_double * 3), ("eta", C.c_double * 3), ("g", C.c_double * 3), ("q", C.c_double * 3)]
+
+
 _lib = None
 
 
@@ -98,6 +103,18 @@ def lib():
         L.or_fcc_lattice.argtypes = [d, C.c_int64, C.c_int64, C.c_int64, P(d)]
         L.or_remove_drift_and_rescale.argtypes = [S, d]
         L.or_num_threads_available.restype = C.c_int32
+        N = P(_Nhc)
+        L.or_nhc_init.argtypes = [N, d, d, d]
+        L.or_nhc_compute_forces.argtypes = [N, d, C.c_int64]
+        L.or_nhc_propagate_half_step.argtypes = [N, d]
+        L.or_nhc_kinetic_energy.argtypes = [N]
+        L.or_nhc_kinetic_energy.restype = d
+        L.or_nhc_potential_energy.argtypes = [N, C.c_int64]
+        L.or_nhc_potential_energy.restype = d
+        L.or_nhc_target.argtypes = [N, C.c_int64, C.c_int64]
+        L.or_verlet_step_nvt_nhc.argtypes = [S, d, N, C.c_int32, C.c_int32]
+        L.or_verlet_step_nvt_nhc.restype = d
+        L.or_run_nvt.argtypes = [S, d, C.c_int64, d, d, d, C.c_int32, C.c_int32, P(d), P(d), P(d), N]
         _lib = L
     return _lib
 
@@ -119,6 +136,36 @@ def lj_pair(eps, sigma, rcut, rij, shift=True):
     f = np.zeros(3)
     lib().or_lj_pair(eps, sigma, rcut, int(shift), _ptr(r, C.c_double), _ptr(u, C.c_double), _ptr(f, C.c_double))
     return float(u[0]), f
+
+
+class Nhc:
+    """The reference's NHThermostatChain (src/ensemble/nvt.rs), chain length 3."""
+
+    def __init__(self, t_start, t_end, tau):
+        self._c = _Nhc()
+        lib().or_nhc_init(C.byref(self._c), t_start, t_end, tau)
+
+    def __getattr__(self, name):
+        if name in ("xi", "eta", "g", "q"):
+            return list(getattr(self._c, name))
+        if name in ("t_start", "t_end", "t_target"):
+            return getattr(self._c, name)
+        raise AttributeError(name)
+
+    def compute_forces(self, kinetic_energy, n_atoms):
+        lib().or_nhc_compute_forces(C.byref(self._c), kinetic_energy, n_atoms)
+
+    def propagate_half_step(self, dt):
+        lib().or_nhc_propagate_half_step(C.byref(self._c), dt)
+
+    def kinetic_energy(self):
+        return lib().or_nhc_kinetic_energy(C.byref(self._c))
+
+    def potential_energy(self, n_atoms):
+        return lib().or_nhc_potential_energy(C.byref(self._c), n_atoms)
+
+    def calculate_target_temperature(self, step, steps):
+        lib().or_nhc_target(C.byref(self._c), step, steps)
 
 
 def fcc_lattice(a, nx, ny, nz) -> np.ndarray:
@@ -191,6 +238,20 @@ class System:
         ke = np.zeros(steps + 1)
         lib().or_run_nve(C.byref(self._s), dt, steps, manager, nthreads, _ptr(pe, C.c_double), _ptr(ke, C.c_double))
         return pe, ke
+
+    def verlet_step_nvt_nhc(self, dt, nhc, manager=OFFSET, nthreads=1) -> float:
+        self._refresh()
+        return lib().or_verlet_step_nvt_nhc(C.byref(self._s), dt, C.byref(nhc._c), manager, nthreads)
+
+    def run_nvt(self, dt, steps, t_start, t_end, tau, manager=OFFSET, nthreads=1):
+        """Simulation::run in the NVT ensemble: (pe, ke, hamiltonian) per step, entry 0 before
+        the first step, and the final thermostat."""
+        self._refresh()
+        pe, ke, ham = np.zeros(steps + 1), np.zeros(steps + 1), np.zeros(steps + 1)
+        nhc = Nhc(t_start, t_end, tau)
+        lib().or_run_nvt(C.byref(self._s), dt, steps, t_start, t_end, tau, manager, nthreads,
+                         _ptr(pe, C.c_double), _ptr(ke, C.c_double), _ptr(ham, C.c_double), C.byref(nhc._c))
+        return pe, ke, ham, nhc
 
     def full_list(self):
         """Reference full neighbour list at rcut: list of sorted-as-built index arrays."""

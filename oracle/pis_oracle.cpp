@@ -556,6 +556,105 @@ void or_run_nve(or_system* sys, double dt, int64_t steps, int32_t manager, int32
     }
 }
 
+// Nose-Hoover chain thermostat, src/ensemble/nvt.rs, with the chain length 3 that
+// NHThermostatChain::new_from_args (:99-112) builds and its literal arithmetic: q_i =
+// KB T tau^2 / 10^i (:37-42), forces (:59-70), the half-step that assigns xi rather than
+// integrating it (:72-80, eta is never advanced), thermostat kinetic and potential energy
+// (:82-97) and the linear target-temperature ramp (:114-124).
+static const double KB = 0.0083144621;  // src/constants.rs:3
+
+struct or_nhc {
+    int32_t m;
+    double t_start, t_end, t_target;
+    double xi[3], eta[3], g[3], q[3];
+};
+
+void or_nhc_init(or_nhc* c, double t_start, double t_end, double tau) {
+    c->m = 3;
+    c->t_start = t_start;
+    c->t_end = t_end;
+    c->t_target = t_start;
+    const double q_value = KB * c->t_target * (tau * tau);
+    double p = 1.0;  // 10^i by repeated multiplication (powi)
+    for (int i = 0; i < 3; ++i) {
+        c->xi[i] = 0.0;
+        c->eta[i] = 0.0;
+        c->g[i] = 0.0;
+        c->q[i] = q_value / p;
+        p = p * 10.0;
+    }
+}
+
+void or_nhc_compute_forces(or_nhc* c, double kinetic_energy, int64_t n_atoms) {
+    c->g[0] = 2.0 * kinetic_energy - ((double)(n_atoms * 3)) * KB * c->t_target;
+    for (int j = 1; j < c->m; ++j) c->g[j] = c->q[j - 1] * (c->xi[j - 1] * c->xi[j - 1]) - KB * c->t_target;
+}
+
+void or_nhc_propagate_half_step(or_nhc* c, double dt) {
+    const int j = c->m - 1;
+    c->xi[j] = 0.5 * dt * c->g[j] / c->q[j];
+    for (int l = j - 1; l >= 0; --l) c->xi[l] = (0.5 * dt * c->g[l] / c->q[l]) * std::exp(-0.25 * dt * c->xi[l + 1]);
+}
+
+double or_nhc_kinetic_energy(const or_nhc* c) {
+    double e = 0.0;
+    for (int i = 0; i < c->m; ++i) e += 0.5 * c->q[i] * (c->xi[i] * c->xi[i]);
+    return e;
+}
+
+double or_nhc_potential_energy(const or_nhc* c, int64_t n_atoms) {
+    double e = (double)(n_atoms * 3) * KB * c->t_target * c->eta[0];
+    for (int i = 1; i < c->m; ++i) e += KB * c->t_target * c->eta[i];
+    return e;
+}
+
+void or_nhc_target(or_nhc* c, int64_t step, int64_t steps) {
+    c->t_target = c->t_start + ((c->t_end - c->t_start) / (double)steps) * (double)step;
+}
+
+// PotentialManager::verlet_step_nvt_nhc, src/potentials/potential.rs:35-58: thermostat half
+// step, velocities scaled by exp(-dt xi_0 / 2), the NVE step, the same scale again, then the
+// thermostat half step on the new kinetic energy.
+double or_verlet_step_nvt_nhc(or_system* sys, double dt, or_nhc* c, int32_t manager, int32_t nthreads) {
+    double kinetic_energy = or_kinetic_energy(sys);
+    or_nhc_compute_forces(c, kinetic_energy, sys->n);
+    or_nhc_propagate_half_step(c, dt);
+    const double scale = std::exp(-0.5 * dt * c->xi[0]);
+    for (int64_t k = 0; k < 3 * sys->n; ++k) sys->vel[k] = sys->vel[k] * scale;
+    const double pe = or_verlet_step_nve(sys, dt, manager, nthreads);
+    for (int64_t k = 0; k < 3 * sys->n; ++k) sys->vel[k] = sys->vel[k] * scale;
+    kinetic_energy = or_kinetic_energy(sys);
+    or_nhc_compute_forces(c, kinetic_energy, sys->n);
+    or_nhc_propagate_half_step(c, dt);
+    return pe;
+}
+
+// Simulation::run for the NVT ensemble (src/simulation.rs:8-39, :41-64, :66-88, :90-115): the
+// initial compute_potential, then per step verlet_step_nvt_nhc followed by the target ramp
+// (calculate_target_temperature(i, steps)), and the printed energies. pe_out[0] / ke_out[0] are
+// the initial energies and ham_out[0] their sum; entry k >= 1 holds step k's potential energy,
+// kinetic energy and Hamiltonian PE + KE + thermostat KE + thermostat PE. Outputs may be null;
+// `c` (may be null) receives the final thermostat state.
+void or_run_nvt(or_system* sys, double dt, int64_t steps, double t_start, double t_end, double tau,
+                int32_t manager, int32_t nthreads, double* pe_out, double* ke_out, double* ham_out, or_nhc* c) {
+    or_nhc local;
+    or_nhc* nhc = c ? c : &local;
+    or_nhc_init(nhc, t_start, t_end, tau);
+    const double pe0 = or_compute_potential(sys, manager, nthreads);
+    const double ke0 = or_kinetic_energy(sys);
+    if (pe_out) pe_out[0] = pe0;
+    if (ke_out) ke_out[0] = ke0;
+    if (ham_out) ham_out[0] = pe0 + ke0;
+    for (int64_t i = 0; i < steps; ++i) {
+        const double pe = or_verlet_step_nvt_nhc(sys, dt, nhc, manager, nthreads);
+        or_nhc_target(nhc, i, steps);
+        const double ke = or_kinetic_energy(sys);
+        if (pe_out) pe_out[i + 1] = pe;
+        if (ke_out) ke_out[i + 1] = ke;
+        if (ham_out) ham_out[i + 1] = pe + ke + or_nhc_kinetic_energy(nhc) + or_nhc_potential_energy(nhc, sys->n);
+    }
+}
+
 // FCC supercell in the order of src/bin/sapphire/main.rs:61-76 (ix, iy, iz, then basis
 // (0,0,0), (0,1/2,1/2), (1/2,0,1/2), (1/2,1/2,0)); positions = h * (cell + basis), h = a I.
 void or_fcc_lattice(double a, int64_t nx, int64_t ny, int64_t nz, double* pos) {
