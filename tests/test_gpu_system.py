@@ -75,6 +75,36 @@ def test_cli_matches_library_run(tmp_path, oracle_lib, cuda_lib):
     assert open(t_cli).read() == open(t_lib).read()
 
 
+def _check_nvt_thermo(rows, pe0, s, o, pe_ref, ke_ref, ham_ref, steps):
+    n = len(s["pos"])
+    assert abs(pe0 - pe_ref[0]) <= 1e-12 * abs(pe_ref[0])
+    assert rows.shape == (steps, 6) and list(rows[:, 0]) == list(range(1, steps + 1))
+    # thermo prints {:.3}: compare at that resolution
+    assert np.allclose(rows[:, 1], np.round(pe_ref[1:], 3), rtol=0, atol=1.5e-3)
+    assert np.allclose(rows[:, 2], np.round(ke_ref[1:], 3), rtol=0, atol=1.5e-3)
+    assert np.allclose(rows[:, 3], np.round(ham_ref[1:], 3), rtol=0, atol=1.5e-3)
+    assert np.allclose(rows[:, 4], np.round(2 * ke_ref[1:] / (3 * n * KB), 3), rtol=0, atol=1.5e-3)
+    assert abs(rows[-1, 5] - round(o.pressure(ke_ref[-1]), 3)) <= 1.5e-3
+
+
+def test_nvt_run_matches_oracle(tmp_path, oracle_lib, cuda_lib):
+    # verlet_step_nvt_nhc and the NVT branch of Simulation::run (src/potentials/potential.rs:35-58,
+    # src/simulation.rs:41-115) against the oracle's restatement: per-step PE, KE, Hamiltonian,
+    # T and the final P, with the thermostat ramping its target from T* = 1.0 to 1.2 (tau* = 0.5)
+    from pis_gb300.io import System
+    s = melted(liquid(nc=6, seed=21), 100, 0.005)
+    t0, t1, tau, steps = 1.0 / KB, 1.2 / KB, 0.5, 30
+    inp, _ = _write_inputs(tmp_path, s, steps=steps, extra=f"fix f1 all nvt temp {t0!r} {t1!r} {tau}\n")
+    sysm = System(str(inp), precision="fp64")
+    assert sysm.ensemble == "NVT"
+    thermo = tmp_path / "thermo.txt"
+    sysm.run(str(thermo))
+    pe0, rows = _parse_thermo(thermo)
+    o = to_oracle(s)
+    pe_ref, ke_ref, ham_ref, _ = o.run_nvt(0.005, steps, t0, t1, tau)
+    _check_nvt_thermo(rows, pe0, s, o, pe_ref, ke_ref, ham_ref, steps)
+
+
 def test_nvt_runs_and_thermostats(tmp_path, oracle_lib, cuda_lib):
     from pis_gb300.io import System
     s = liquid(nc=6, seed=19)
