@@ -151,17 +151,21 @@ def make_state(cells, seed):
     return pos, vel, L
 
 
-def cpu_sample(pos, vel, L, steps, threads):
-    """Oracle restatement of the reference's multithreaded manager, timed on host cores."""
+def cpu_sample(pos, vel, L, threads, manager, min_seconds=10.0, max_steps=50):
+    """The oracle's restatement of a reference force manager stepping the state on host cores:
+    whole NVE steps until at least ``min_seconds`` have passed (or ``max_steps``), after the
+    initial force evaluation. Returns (atom-steps/s, steps, seconds)."""
     import oracle
     n = len(pos)
     s = oracle.System(pos, np.ones(n, np.int32), [1.0], np.eye(3) * L, TABLE, velocities=vel)
-    s.compute_potential(manager=oracle.PARALLEL, nthreads=threads)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        s.verlet_step_nve(DT, manager=oracle.PARALLEL, nthreads=threads)
-    dt = time.perf_counter() - t0
-    return n * steps / dt, dt
+    s.compute_potential(manager=manager, nthreads=threads)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        s.verlet_step_nve(DT, manager=manager, nthreads=threads)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds or steps >= max_steps:
+            return n * steps / el, steps, el
 
 
 def run_reference(args, rank, world):
@@ -332,10 +336,14 @@ def main():
         import oracle
         oracle.build()
         threads = oracle.num_threads_available()
-        v_cpu, el = cpu_sample(melt_pos, melt_vel, L, 2, threads)
+        v_cpu, k_cpu, el = cpu_sample(melt_pos, melt_vel, L, threads, oracle.PARALLEL)
+        v_ser, k_ser, el_ser = cpu_sample(melt_pos, melt_vel, L, 1, oracle.OFFSET)
         cpu = {"value": v_cpu, "unit": "atom-steps/s", "cores": threads, "kind": "port",
-               "sample": f"2 NVE steps of the same {n}-atom liquid ({el:.1f} s), LJVParallelManager restated "
-                         "with OpenMP (oracle/pis_oracle.cpp)"}
+               "sample": f"{k_cpu} NVE steps of the same {n}-atom liquid ({el:.1f} s), LJVParallelManager "
+                         "restated with OpenMP (oracle/pis_oracle.cpp)",
+               "serial": {"value": v_ser, "unit": "atom-steps/s", "cores": 1, "kind": "port",
+                          "sample": f"{k_ser} NVE step(s) of the same liquid ({el_ser:.1f} s), LJVOffsetManager "
+                                    "(the CLI's manager) restated serially (oracle/pis_oracle.cpp)"}}
 
     if rank == 0:
         line = {
