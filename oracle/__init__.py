@@ -10,7 +10,9 @@ built by ``oracle/Makefile`` into ``oracle/_build/liboracle.so``) and
 
 Parity status: "parity unpinned" against reference outputs - the reference is a Rust
 crate that cannot be built here and its tests pin no physics. The oracle is anchored on
-known-answer tests derived from the reference's example inputs instead.
+known-answer tests derived from the reference's example inputs instead, and its answers on
+three seeded states and on those inputs are committed under tests/golden (written by
+tests/golden/make_golden.py, which checks the known answers first).
 """
 from __future__ import annotations
 

@@ -11,7 +11,8 @@
 // "parity unpinned" with respect to reference outputs. It is anchored instead on
 // known-answer tests derived from the reference's example inputs (FCC shell counts,
 // closed-form lattice energies, Newton's third law, agreement between the five
-// reference force managers) - see tests/test_oracle_known_answers.py.
+// reference force managers) - see tests/test_oracle_known_answers.py - and its answers on
+// seeded states and on those inputs are committed under tests/golden.
 //
 // Operation order follows the Rust source literally and this file must be compiled
 // with -ffp-contract=off: Rust never fuses a*b+c into an FMA, and GCC on aarch64
