@@ -13,8 +13,8 @@ Two differences of form, not of behaviour: the reference's tests call each comma
 argument list directly, so they reach an empty list; through a file, a line with fewer than two
 tokens is skipped before any command sees it (src/system.rs:75-77), which these tests check
 instead. And the reference's context fields are not exposed one by one: the tests observe them
-through what the driver builds from them (steps, timestep, ensemble, the pair table, the dump
-step and file, the start velocities).
+through what ``pis_system_open`` builds from them (steps, timestep, ensemble, the pair table,
+the dump step and file, the start velocities).
 """
 import numpy as np
 import pytest
