@@ -6,10 +6,10 @@ Test infrastructure only. Each ``*.npz`` fixture holds a small seeded state and 
 FP64 answers for it (forces, energy, virial, neighbour sets, a short NVE trajectory), so that
 the parity tests can check the CUDA path against committed numbers on a machine without the
 oracle's sources or the reference's files. ``examples.json`` holds known answers taken from the
-reference's example inputs (``example/data.txt``, ``example/data_run.txt``, ``example/example.txt``,
-``example/argon4000.txt``): the parsed pair tables with the PairCoeffs quirk, the oracle's energy
-and forces on the two small files, and the FCC order, shell count and lattice energy of the two
-argon files. Those inputs are read from the reference sources (``REFERENCE_DIR``, default
+reference's example inputs (``example/data.txt``, ``example/data_run.txt``,
+``example/example.txt``, ``example/example2.txt``, ``example/argon4000.txt``): the parsed pair
+tables with the PairCoeffs quirk, the oracle's energy and forces on the two small files, and the
+FCC order, shell count and lattice energy of the argon files. Those inputs are read from the reference sources (``REFERENCE_DIR``, default
 ``/root/reference``); the script refuses to write if they are absent or if the oracle disagrees
 with a closed form, so a fixture never records an unpinned oracle.
 
@@ -172,6 +172,15 @@ def example_answers():
                          table=_json_table(d["table"]), max_dev_from_generator=dev,
                          neighbours_per_atom=54, pe=pe, pe_per_atom_closed_form=closed,
                          max_abs_force=float(np.abs(s.force).max()))
+    # example2.txt: the same 500-atom lattice with no PairCoeffs section, so the table comes from
+    # the input's pair_style / pair_coeff (system.rs:120-168) and the data file's manager is empty
+    p = path("example2.txt")
+    d = oracle.read_data(p)
+    gen = fcc_lattice(5.41, 5, 5, 5)
+    dev = float(np.abs(np.asarray(d["positions"]) - gen).max())
+    assert d["n_atoms"] == 500 and dev <= 1e-12 and d["table"] == {} and d["start_velocities"]
+    out["example2.txt"] = dict(sha256=_sha256(p), n_atoms=d["n_atoms"], lattice_a=5.41, cells=5, table=[],
+                               max_dev_from_generator=dev, masses=list(map(float, d["masses"])))
     return out
 
 

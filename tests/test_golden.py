@@ -93,7 +93,7 @@ def test_argon_lattice_example_answers(oracle_lib, name, nc):
     assert np.all(np.diff(off) == ex["neighbours_per_atom"])
 
 
-@pytest.mark.parametrize("name", ["data.txt", "data_run.txt", "example.txt", "argon4000.txt"])
+@pytest.mark.parametrize("name", ["data.txt", "data_run.txt", "example.txt", "example2.txt", "argon4000.txt"])
 def test_examples_match_reference_files(oracle_lib, name):
     # where the reference sources are mounted: its example file is the one the answers came from
     import hashlib

@@ -343,3 +343,24 @@ def test_reference_example_input(pio, monkeypatch):
     _, vel, _ = s.state(4000)
     s.close()
     assert np.array_equal(vel, pio.maxwell_boltzmann(np.full(4000, 39.948), 5.0, 12345))
+
+
+def test_pair_style_supplies_the_table_a_data_file_lacks(pio, tmp_path):
+    # example/example2.txt has no PairCoeffs: the input's pair_style / pair_coeff build the table,
+    # the global cutoff filling the missing per-pair one
+    import os
+    from conftest import REFERENCE
+    from golden_data import examples
+    from pis_gb300.lattice import fcc_lattice
+    data = os.path.join(REFERENCE, "example", "example2.txt")
+    if not os.path.exists(data):
+        pytest.skip("reference sources not mounted")
+    ex = examples()["example2.txt"]
+    s = _open(pio, tmp_path, f"read_data {data}\npair_style lj/cut 8.5\npair_coeff 1 1 0.238 3.405\n")
+    assert s.pairs() == {(1, 1): (0.238, 3.405, 8.5)}
+    pos, _, _ = s.state(ex["n_atoms"])
+    s.close()
+    assert np.abs(pos - fcc_lattice(ex["lattice_a"], 5, 5, 5)).max() <= ex["max_dev_from_generator"]
+    s = _open(pio, tmp_path, f"read_data {data}\n")
+    assert s.pairs() == {}
+    s.close()
