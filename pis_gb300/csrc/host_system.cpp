@@ -395,9 +395,10 @@ pis_status pis_system_dump(const pis_system* s, int64_t* dump_step, char* file, 
 
 pis_status pis_system_run(pis_system* s, const char* thermo_path) {
     if (!s) return PIS_ERR_INVALID_ARGUMENT;
-    if (!s->have_atoms) return sfail(s, PIS_ERR_NO_ATOMS, "No atoms defined in input file");
+    // System::run takes the manager before Simulation::run asks for the atoms (src/system.rs:177-181)
     if (s->table.empty())
         return sfail(s, PIS_ERR_MISSING_POTENTIAL, "Potential manager not initialized - missing pair_style or pair_coeff commands");
+    if (!s->have_atoms) return sfail(s, PIS_ERR_NO_ATOMS, "No atoms defined in input file");
     const int ens = pis_system_ensemble(s);
     if (ens == 2)
         return sfail(s, PIS_ERR_UNSUPPORTED, "NPT needs a triclinic box update, which the GPU engine does not support");
