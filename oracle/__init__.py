@@ -62,6 +62,10 @@ class _Nhc(C.Structure):
                 ("xi", C.c_double * 3), ("eta", C.c_double * 3), ("g", C.c_double * 3), ("q", C.c_double * 3)]
 
 
+class _Mtk(C.Structure):
+    _fields_ = [("p_target", C.c_double * 9), ("momentum", C.c_double * 9), ("w", C.c_double)]
+
+
 _lib = None
 
 
@@ -117,6 +121,20 @@ def lib():
         L.or_verlet_step_nvt_nhc.argtypes = [S, d, N, C.c_int32, C.c_int32]
         L.or_verlet_step_nvt_nhc.restype = d
         L.or_run_nvt.argtypes = [S, d, C.c_int64, d, d, d, C.c_int32, C.c_int32, P(d), P(d), P(d), N]
+        B = P(_Mtk)
+        L.or_expm3.argtypes = [P(d), P(d)]
+        L.or_mtk_init.argtypes = [B, d, d, C.c_int64, d]
+        L.or_pressure_tensor.argtypes = [S, P(d)]
+        L.or_mtk_delta_momentum.argtypes = [B, S, d, P(d)]
+        L.or_mtk_scale.argtypes = [B, d, C.c_int32, P(d)]
+        L.or_mtk_kinetic_energy.argtypes = [B]
+        L.or_mtk_kinetic_energy.restype = d
+        L.or_mtk_potential_energy.argtypes = [B, P(d)]
+        L.or_mtk_potential_energy.restype = d
+        L.or_scale_box.argtypes = [S, P(d)]
+        L.or_verlet_step_npt_mtk.argtypes = [S, d, B, N, C.c_int32, C.c_int32]
+        L.or_verlet_step_npt_mtk.restype = d
+        L.or_run_npt.argtypes = [S, d, C.c_int64, d, d, d, d, d, C.c_int32, C.c_int32, P(d), P(d), P(d), P(d)]
         _lib = L
     return _lib
 
@@ -168,6 +186,56 @@ class Nhc:
 
     def calculate_target_temperature(self, step, steps):
         lib().or_nhc_target(C.byref(self._c), step, steps)
+
+
+def expm3(a) -> np.ndarray:
+    """3x3 matrix exponential (scaling and squaring with Pade approximants, Higham 2005)."""
+    m = np.ascontiguousarray(a, dtype=np.float64).reshape(9)
+    out = np.zeros(9)
+    lib().or_expm3(_ptr(m, C.c_double), _ptr(out, C.c_double))
+    return out.reshape(3, 3)
+
+
+class Mtk:
+    """The reference's MTKBarostat (src/ensemble/npt.rs)."""
+
+    def __init__(self, p_start, tau, n_atoms, t_target):
+        self._c = _Mtk()
+        lib().or_mtk_init(C.byref(self._c), p_start, tau, n_atoms, t_target)
+
+    @property
+    def w(self):
+        return self._c.w
+
+    @property
+    def momentum(self):
+        return np.array(self._c.momentum).reshape(3, 3)
+
+    @momentum.setter
+    def momentum(self, m):
+        self._c.momentum[:] = list(np.asarray(m, dtype=np.float64).reshape(9))
+
+    @property
+    def p_target(self):
+        return np.array(self._c.p_target).reshape(3, 3)
+
+    def delta_momentum(self, system, dt):
+        system._refresh()
+        out = np.zeros(9)
+        lib().or_mtk_delta_momentum(C.byref(self._c), C.byref(system._s), dt, _ptr(out, C.c_double))
+        return out.reshape(3, 3)
+
+    def scale(self, dt, velocity_scaling):
+        out = np.zeros(9)
+        lib().or_mtk_scale(C.byref(self._c), dt, int(bool(velocity_scaling)), _ptr(out, C.c_double))
+        return out.reshape(3, 3)
+
+    def kinetic_energy(self):
+        return lib().or_mtk_kinetic_energy(C.byref(self._c))
+
+    def potential_energy(self, h):
+        hh = np.ascontiguousarray(h, dtype=np.float64).reshape(9)
+        return lib().or_mtk_potential_energy(C.byref(self._c), _ptr(hh, C.c_double))
 
 
 def fcc_lattice(a, nx, ny, nz) -> np.ndarray:
@@ -254,6 +322,39 @@ class System:
         lib().or_run_nvt(C.byref(self._s), dt, steps, t_start, t_end, tau, manager, nthreads,
                          _ptr(pe, C.c_double), _ptr(ke, C.c_double), _ptr(ham, C.c_double), C.byref(nhc._c))
         return pe, ke, ham, nhc
+
+    def pressure_tensor(self) -> np.ndarray:
+        self._refresh()
+        out = np.zeros(9)
+        lib().or_pressure_tensor(C.byref(self._s), _ptr(out, C.c_double))
+        return out.reshape(3, 3)
+
+    def _pull_box(self):
+        self.h[:] = np.array(self._s.h).reshape(3, 3)
+        self.hinv[:] = np.array(self._s.hinv).reshape(3, 3)
+
+    def scale_box(self, m):
+        self._refresh()
+        mm = np.ascontiguousarray(m, dtype=np.float64).reshape(9)
+        lib().or_scale_box(C.byref(self._s), _ptr(mm, C.c_double))
+        self._pull_box()
+
+    def verlet_step_npt_mtk(self, dt, mtk, nhc, manager=OFFSET, nthreads=1) -> float:
+        self._refresh()
+        pe = lib().or_verlet_step_npt_mtk(C.byref(self._s), dt, C.byref(mtk._c), C.byref(nhc._c), manager, nthreads)
+        self._pull_box()
+        return pe
+
+    def run_npt(self, dt, steps, t_start, t_end, tau_t, p_start, tau_p, manager=OFFSET, nthreads=1):
+        """Simulation::run in the NPT ensemble: (pe, ke, hamiltonian, boxes) per step, entry 0
+        before the first step."""
+        self._refresh()
+        pe, ke, ham = np.zeros(steps + 1), np.zeros(steps + 1), np.zeros(steps + 1)
+        boxes = np.zeros((steps + 1, 3, 3))
+        lib().or_run_npt(C.byref(self._s), dt, steps, t_start, t_end, tau_t, p_start, tau_p, manager, nthreads,
+                         _ptr(pe, C.c_double), _ptr(ke, C.c_double), _ptr(ham, C.c_double), _ptr(boxes, C.c_double))
+        self._pull_box()
+        return pe, ke, ham, boxes
 
     def full_list(self):
         """Reference full neighbour list at rcut: list of sorted-as-built index arrays."""

@@ -656,6 +656,256 @@ void or_run_nvt(or_system* sys, double dt, int64_t steps, double t_start, double
     }
 }
 
+// ---- NPT: the Martyna-Tobias-Klein barostat of src/ensemble/npt.rs ----------------------------
+// 3x3 matrices are row-major arrays of the mathematical matrix (h: box vectors as columns).
+
+static void m3_mul(const double* a, const double* b, double* c) {
+    double t[9];
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) t[3 * r + q] = a[3 * r] * b[q] + a[3 * r + 1] * b[3 + q] + a[3 * r + 2] * b[6 + q];
+    std::memcpy(c, t, sizeof(t));
+}
+
+static void m3_symmetrize(const double* a, double* out) {  // src/math.rs symmetrize: (A + A^T) * 0.5
+    double t[9];
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) t[3 * r + q] = (a[3 * r + q] + a[3 * q + r]) * 0.5;
+    std::memcpy(out, t, sizeof(t));
+}
+
+// Solve P X = Q for 3x3 X (Gaussian elimination with partial pivoting, column by column).
+static void m3_solve(const double* p_in, const double* q_in, double* x) {
+    double a[9], b[9];
+    std::memcpy(a, p_in, sizeof(a));
+    std::memcpy(b, q_in, sizeof(b));
+    for (int k = 0; k < 3; ++k) {
+        int piv = k;
+        for (int r = k + 1; r < 3; ++r)
+            if (std::fabs(a[3 * r + k]) > std::fabs(a[3 * piv + k])) piv = r;
+        if (piv != k)
+            for (int q = 0; q < 3; ++q) {
+                std::swap(a[3 * k + q], a[3 * piv + q]);
+                std::swap(b[3 * k + q], b[3 * piv + q]);
+            }
+        for (int r = k + 1; r < 3; ++r) {
+            const double f = a[3 * r + k] / a[3 * k + k];
+            for (int q = 0; q < 3; ++q) {
+                a[3 * r + q] -= f * a[3 * k + q];
+                b[3 * r + q] -= f * b[3 * k + q];
+            }
+        }
+    }
+    for (int q = 0; q < 3; ++q)
+        for (int r = 2; r >= 0; --r) {
+            double v = b[3 * r + q];
+            for (int c = r + 1; c < 3; ++c) v -= a[3 * r + c] * x[3 * c + q];
+            x[3 * r + q] = v / a[3 * r + r];
+        }
+}
+
+// Matrix exponential (Matrix3::exp, npt.rs:55): the published scaling-and-squaring method with
+// diagonal Pade approximants of degree 3, 5, 7, 9 or 13 chosen by the 1-norm (N. J. Higham,
+// "The scaling and squaring method for the matrix exponential revisited", SIAM J. Matrix Anal.
+// Appl. 26 (2005), Algorithm 2.3). nalgebra's own selection logic is not restated, so results
+// agree with the reference to rounding, not bit for bit.
+void or_expm3(const double* a_in, double* out) {
+    static const double theta[4] = {1.495585217958292e-2, 2.539398330063230e-1, 9.504178996162932e-1,
+                                    2.097847961257068e0};
+    static const double theta13 = 5.371920351148152e0;
+    static const double b3[4] = {120.0, 60.0, 12.0, 1.0};
+    static const double b5[6] = {30240.0, 15120.0, 3360.0, 420.0, 30.0, 1.0};
+    static const double b7[8] = {17297280.0, 8648640.0, 1995840.0, 277200.0, 25200.0, 1512.0, 56.0, 1.0};
+    static const double b9[10] = {17643225600.0, 8821612800.0, 2075673600.0, 302702400.0, 30270240.0,
+                                  2162160.0, 110880.0, 3960.0, 90.0, 1.0};
+    static const double b13[14] = {64764752532480000.0, 32382376266240000.0, 7771770303897600.0,
+                                   1187353796428800.0, 129060195264000.0, 10559470521600.0, 670442572800.0,
+                                   33522128640.0, 1323241920.0, 40840800.0, 960960.0, 16380.0, 182.0, 1.0};
+    static const double* bs[4] = {b3, b5, b7, b9};
+    static const int ms[4] = {3, 5, 7, 9};
+    double a[9];
+    std::memcpy(a, a_in, sizeof(a));
+    double norm1 = 0.0;
+    for (int q = 0; q < 3; ++q) norm1 = std::max(norm1, std::fabs(a[q]) + std::fabs(a[3 + q]) + std::fabs(a[6 + q]));
+    const double eye[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    double u[9], v[9];
+    int squarings = 0;
+    int pick = -1;
+    for (int k = 0; k < 4; ++k)
+        if (norm1 <= theta[k]) {
+            pick = k;
+            break;
+        }
+    if (pick >= 0) {
+        // powers A^0, A^2, ..., A^(m-1): U = A sum_j b_{2j+1} A^{2j}, V = sum_j b_{2j} A^{2j}
+        const int m = ms[pick];
+        const double* b = bs[pick];
+        double a2[9], pw[9], us[9] = {0}, vs[9] = {0};
+        m3_mul(a, a, a2);
+        std::memcpy(pw, eye, sizeof(pw));
+        for (int j = 0; 2 * j <= m - 1; ++j) {
+            for (int e = 0; e < 9; ++e) {
+                us[e] += b[2 * j + 1] * pw[e];
+                vs[e] += b[2 * j] * pw[e];
+            }
+            m3_mul(pw, a2, pw);
+        }
+        m3_mul(a, us, u);
+        std::memcpy(v, vs, sizeof(v));
+    } else {
+        squarings = std::max(0, (int)std::ceil(std::log2(norm1 / theta13)));
+        const double sc = std::ldexp(1.0, -squarings);
+        for (double& x : a) x *= sc;
+        const double* b = b13;
+        double a2[9], a4[9], a6[9], t1[9], t2[9];
+        m3_mul(a, a, a2);
+        m3_mul(a2, a2, a4);
+        m3_mul(a4, a2, a6);
+        for (int e = 0; e < 9; ++e) t1[e] = b[13] * a6[e] + b[11] * a4[e] + b[9] * a2[e];
+        m3_mul(a6, t1, t1);
+        for (int e = 0; e < 9; ++e) t1[e] += b[7] * a6[e] + b[5] * a4[e] + b[3] * a2[e] + b[1] * eye[e];
+        m3_mul(a, t1, u);
+        for (int e = 0; e < 9; ++e) t2[e] = b[12] * a6[e] + b[10] * a4[e] + b[8] * a2[e];
+        m3_mul(a6, t2, t2);
+        for (int e = 0; e < 9; ++e) v[e] = t2[e] + b[6] * a6[e] + b[4] * a4[e] + b[2] * a2[e] + b[0] * eye[e];
+    }
+    double p[9], q[9];
+    for (int e = 0; e < 9; ++e) {
+        p[e] = v[e] - u[e];
+        q[e] = v[e] + u[e];
+    }
+    m3_solve(p, q, out);
+    for (int k = 0; k < squarings; ++k) m3_mul(out, out, out);
+}
+
+struct or_mtk {
+    double p_target[9];
+    double momentum[9];
+    double w;
+};
+
+// MTKBarostat::new / new_from_args (npt.rs:23-40, :68-88): target pressure p_start * I, zero
+// momentum, mass W = 3N KB T tau^2 with T the thermostat's start temperature (300 without one).
+void or_mtk_init(or_mtk* b, double p_start, double tau, int64_t n_atoms, double t_target) {
+    for (int e = 0; e < 9; ++e) {
+        b->p_target[e] = (e % 4 == 0) ? p_start : 0.0;
+        b->momentum[e] = 0.0;
+    }
+    b->w = ((double)(3 * n_atoms)) * KB * t_target * (tau * tau);
+}
+
+// Atoms::pressure_tensor (src/atoms/properties.rs:45-59): (V V^T + R F^T) / volume. The kinetic
+// tensor carries no masses, as in the reference.
+void or_pressure_tensor(const or_system* sys, double* p) {
+    double k[9] = {0}, w[9];
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) {
+            double sum = 0.0;
+            for (int64_t i = 0; i < sys->n; ++i) sum += sys->vel[3 * i + a] * sys->vel[3 * i + c];
+            k[3 * a + c] = sum;
+        }
+    or_virial_tensor(sys, w);
+    const double vol = std::fabs(or_determinant3(sys->h));
+    for (int e = 0; e < 9; ++e) p[e] = (k[e] + w[e]) / vol;
+}
+
+// delta_momentum (npt.rs:42-47): symmetrize((P - P_target) * (V * 0.5 * dt)).
+void or_mtk_delta_momentum(const or_mtk* b, const or_system* sys, double dt, double* out) {
+    double p[9];
+    or_pressure_tensor(sys, p);
+    const double f = std::fabs(or_determinant3(sys->h)) * 0.5 * dt;
+    for (int e = 0; e < 9; ++e) p[e] = (p[e] - b->p_target[e]) * f;
+    m3_symmetrize(p, out);
+}
+
+// scale (npt.rs:49-56): exp(symmetrize(momentum / W) * factor * dt), factor -0.5 for the
+// velocities and 1 for the box.
+void or_mtk_scale(const or_mtk* b, double dt, int32_t velocity_scaling, double* out) {
+    double e[9];
+    for (int k = 0; k < 9; ++k) e[k] = b->momentum[k] / b->w;
+    m3_symmetrize(e, e);
+    const double factor = velocity_scaling ? -0.5 : 1.0;
+    for (int k = 0; k < 9; ++k) e[k] = e[k] * factor * dt;
+    or_expm3(e, out);
+}
+
+// kinetic_energy (npt.rs:58-60): tr(M M^T) / (2 W); potential_energy (:62-64): tr(P_target^T h).
+double or_mtk_kinetic_energy(const or_mtk* b) {
+    double t = 0.0;
+    for (int k = 0; k < 9; ++k) t += b->momentum[k] * b->momentum[k];
+    return t / (2.0 * b->w);
+}
+
+double or_mtk_potential_energy(const or_mtk* b, const double* h) {
+    double t = 0.0;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) t += b->p_target[3 * c + r] * h[3 * c + r];
+    return t;
+}
+
+// Atoms::scale_box (src/atoms/transformations.rs:6-15): fractional coordinates s = h^-1 r, then
+// h = scale h, h^-1 = inverse(h), r = h s.
+void or_scale_box(or_system* sys, const double* scale) {
+    std::vector<double> frac((size_t)(3 * sys->n));
+    for (int64_t i = 0; i < sys->n; ++i) matvec(sys->hinv, sys->pos + 3 * i, frac.data() + 3 * i);
+    m3_mul(scale, sys->h, sys->h);
+    or_inverse3(sys->h, sys->hinv);
+    for (int64_t i = 0; i < sys->n; ++i) matvec(sys->h, frac.data() + 3 * i, sys->pos + 3 * i);
+}
+
+static void scale_velocities(or_system* sys, const double* m) {
+    for (int64_t i = 0; i < sys->n; ++i) {
+        double v[3];
+        matvec(m, sys->vel + 3 * i, v);
+        std::memcpy(sys->vel + 3 * i, v, sizeof(v));
+    }
+}
+
+// PotentialManager::verlet_step_npt_mtk (src/potentials/potential.rs:115-135).
+double or_verlet_step_npt_mtk(or_system* sys, double dt, or_mtk* b, or_nhc* c, int32_t manager, int32_t nthreads) {
+    double d[9], scale[9], scale_h[9];
+    or_mtk_delta_momentum(b, sys, dt, d);
+    for (int k = 0; k < 9; ++k) b->momentum[k] += d[k];
+    or_mtk_scale(b, dt, 1, scale);
+    scale_velocities(sys, scale);
+    or_mtk_scale(b, dt, 0, scale_h);
+    or_scale_box(sys, scale_h);
+    const double pe = or_verlet_step_nvt_nhc(sys, dt, c, manager, nthreads);
+    scale_velocities(sys, scale);
+    or_mtk_delta_momentum(b, sys, dt, d);
+    for (int k = 0; k < 9; ++k) b->momentum[k] += d[k];
+    return pe;
+}
+
+// Simulation::run for the NPT ensemble (src/simulation.rs:8-115): per step verlet_step_npt_mtk,
+// the thermostat's target ramp, and the Hamiltonian PE + KE + thermostat KE + PE + barostat KE +
+// PE. Entry 0 holds the initial energies. box_out (may be null) receives h after each step
+// (9 values per entry, entry 0 the initial box).
+void or_run_npt(or_system* sys, double dt, int64_t steps, double t_start, double t_end, double tau_t, double p_start,
+                double tau_p, int32_t manager, int32_t nthreads, double* pe_out, double* ke_out, double* ham_out,
+                double* box_out) {
+    or_nhc nhc;
+    or_nhc_init(&nhc, t_start, t_end, tau_t);
+    or_mtk b;
+    or_mtk_init(&b, p_start, tau_p, sys->n, t_start);
+    const double pe0 = or_compute_potential(sys, manager, nthreads);
+    const double ke0 = or_kinetic_energy(sys);
+    if (pe_out) pe_out[0] = pe0;
+    if (ke_out) ke_out[0] = ke0;
+    if (ham_out) ham_out[0] = pe0 + ke0;
+    if (box_out) std::memcpy(box_out, sys->h, sizeof(double) * 9);
+    for (int64_t i = 0; i < steps; ++i) {
+        const double pe = or_verlet_step_npt_mtk(sys, dt, &b, &nhc, manager, nthreads);
+        or_nhc_target(&nhc, i, steps);
+        const double ke = or_kinetic_energy(sys);
+        if (pe_out) pe_out[i + 1] = pe;
+        if (ke_out) ke_out[i + 1] = ke;
+        if (ham_out)
+            ham_out[i + 1] = pe + ke + or_nhc_kinetic_energy(&nhc) + or_nhc_potential_energy(&nhc, sys->n) +
+                             or_mtk_kinetic_energy(&b) + or_mtk_potential_energy(&b, sys->h);
+        if (box_out) std::memcpy(box_out + 9 * (i + 1), sys->h, sizeof(double) * 9);
+    }
+}
+
 // FCC supercell in the order of src/bin/sapphire/main.rs:61-76 (ix, iy, iz, then basis
 // (0,0,0), (0,1/2,1/2), (1/2,0,1/2), (1/2,1/2,0)); positions = h * (cell + basis), h = a I.
 void or_fcc_lattice(double a, int64_t nx, int64_t ny, int64_t nz, double* pos) {
