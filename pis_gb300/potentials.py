@@ -181,6 +181,32 @@ class LJGpuManager:
         self._synced = (id(atoms), atoms.touch())
         return float(pe[0])
 
+    def verlet_step_nvt_nhc(self, atoms, dt, chain) -> float:
+        """PotentialManager::verlet_step_nvt_nhc (src/potentials/potential.rs:35-58): thermostat
+        half step, velocities scaled by exp(-dt xi_0 / 2), the NVE step, the same scale, and the
+        thermostat half step on the new kinetic energy. ``chain`` is a
+        pis_gb300.ensemble.NHThermostatChain; the kinetic energies come from the device."""
+        import math
+        self._sync_in(atoms)
+        n = atoms.n_atoms
+        ke, _ = self.ctx.reductions()
+        chain.compute_forces(ke, n)
+        chain.propagate_half_step(dt)
+        scale = math.exp(-0.5 * dt * chain.xi[0])
+        m = np.diag([scale, scale, scale])
+        self.ctx.scale_velocities(m)
+        pe = self.ctx.verlet_step_nve(dt, 1)
+        self.ctx.scale_velocities(m)
+        ke, _ = self.ctx.reductions()
+        chain.compute_forces(ke, n)
+        chain.propagate_half_step(dt)
+        pos, vel, frc = self.ctx.get_state()
+        atoms.positions[:] = pos
+        atoms.velocities[:] = vel
+        atoms.forces[:] = frc
+        self._synced = (id(atoms), atoms.touch())
+        return float(pe[0])
+
     def run_nve(self, atoms, dt, steps):
         """``steps`` NVE steps with the state resident on the device; returns per-step PE."""
         self._sync_in(atoms)
