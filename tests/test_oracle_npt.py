@@ -118,3 +118,23 @@ def test_light_barostat_moves_the_box_towards_the_target(oracle_lib):
     assert k == ke[-1]
     assert ham[-1] == e + k + nhc.kinetic_energy() + nhc.potential_energy(p.n) + mtk.kinetic_energy() \
         + mtk.potential_energy(p.h)
+
+
+def test_managers_agree_on_a_sheared_box(oracle_lib):
+    # the barostat's symmetric box scaling makes the box triclinic: the oracle's min-image
+    # (s = h^-1 r, s -= round(s), r = h s) and fractional-coordinate binning must give every
+    # reference manager the all-pairs answer on a mildly sheared box with 4 cells per axis
+    import oracle
+    s = liquid(nc=6, seed=2)
+    L = s["h"][0, 0]
+    h = np.array([[L, 0.3, 0.2], [0.0, L, -0.25], [0.0, 0.0, L]])
+    rng = np.random.default_rng(1)
+    pos = np.mod(s["pos"] / L + rng.normal(0, 0.004, s["pos"].shape), 1.0) @ h.T
+    ref = oracle.System(pos, s["types"], s["masses"], h, s["table"])
+    pe_ref = ref.compute_potential(manager=oracle.ALLPAIRS)
+    for mgr in (oracle.OFFSET, oracle.VERLET27, oracle.FULLLIST, oracle.PARALLEL):
+        o = oracle.System(pos, s["types"], s["masses"], h, s["table"])
+        assert o.divide_into_cells(2.5) == (4, 4, 4)
+        pe = o.compute_potential(manager=mgr, nthreads=2)
+        assert abs(pe - pe_ref) <= 1e-13 * abs(pe_ref)
+        assert np.linalg.norm(o.force - ref.force) <= 1e-13 * np.linalg.norm(ref.force)
