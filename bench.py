@@ -34,6 +34,32 @@ sys.path.insert(0, ROOT)
 TABLE = {(1, 1): (1.0, 1.0, 2.5)}
 RHO, TSTAR, DT, SKIN = 0.8442, 0.72, 0.005, 0.3
 HBM_FALLBACK_GBS = 6800.0
+# Work per atom-step of the LJ pair loop: 23 flops per list entry (displacement, minimum image,
+# r^2, reciprocal, powers, force factor, force components, cutoff test) plus 3 for the energy of an
+# in-cutoff pair; compulsory bytes 4 per list entry plus 100 per atom (own position 24, velocity
+# read and write 48, force write 24, type 4).
+FLOPS_PER_CANDIDATE = 23
+FLOPS_PER_PAIR_ENERGY = 3
+ALG_BYTES_PER_ATOM = 100
+
+
+def probe_peaks():
+    """FP32 and FP64 pipe peaks (TFLOP/s) of this GPU, probed in this run by the library's
+    measurement hook (independent fused multiply-add chains on every SM)."""
+    import ctypes as C
+    from pis_gb300 import _ffi
+    a, b = C.c_double(), C.c_double()
+    if _ffi.lib().pis_gpu_probe_peaks(C.byref(a), C.byref(b)) != 0:
+        return None, None
+    return a.value, b.value
+
+
+def pipe_fraction(flops, kernel_ms, peak_tflops):
+    if not peak_tflops or not kernel_ms:
+        return None
+    achieved = flops / (kernel_ms * 1e-3) / 1e12
+    return {"achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s", "frac": achieved / peak_tflops,
+            "peak_source": "probed in this run"}
 
 
 def parse():
@@ -169,24 +195,36 @@ def cpu_sample(pos, vel, L, threads, manager, min_seconds=10.0, max_steps=50):
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the oracle's restatement of the reference's multithreaded manager
+    (LJVParallelManager, src/potentials/lennard_jones.rs:253-336, OpenMP on all host cores) on the
+    same workload. The start state is built without the GPU library (the oracle's copies of the
+    lattice order and of this project's velocity generator give the same arrays bit for bit) and
+    melted on the CPU for the same number of unreported steps as the GPU arm's melt (in FP64 here,
+    in mixed precision there: the same liquid statistically, not bit for bit)."""
     if rank != 0:
         return
     import oracle
     oracle.build()
     threads = oracle.num_threads_available()
-    pos, vel, L = make_state(args.cells, 1)
+    a = (4.0 / RHO) ** (1.0 / 3.0)
+    pos = oracle.fcc_lattice(a, args.cells, args.cells, args.cells)
     n = len(pos)
-    # bounded sample: each timed step of the 2M-atom system costs ~0.5 s on 16 cores
+    L = a * args.cells
+    vel = oracle.maxwell_boltzmann(np.ones(n), TSTAR / oracle.KB, 1)
+    s = oracle.System(pos, np.ones(n, np.int32), [1.0], np.eye(3) * L, TABLE, velocities=vel)
+    s.compute_potential(manager=oracle.PARALLEL, nthreads=threads)
+    t_melt = time.perf_counter()
+    for _ in range(args.equil):
+        s.verlet_step_nve(DT, manager=oracle.PARALLEL, nthreads=threads)
+    t_melt = time.perf_counter() - t_melt
+    # bounded sample: each step of the 2M-atom system costs ~0.5 s on 16 cores
     k = max(1, min(args.steps, 5))
     w = max(0, min(args.warmup, 3))
-    import oracle as O
-    s = O.System(pos, np.ones(n, np.int32), [1.0], np.eye(3) * L, TABLE, velocities=vel)
-    s.compute_potential(manager=O.PARALLEL, nthreads=threads)
     for _ in range(w):
-        s.verlet_step_nve(DT, manager=O.PARALLEL, nthreads=threads)
+        s.verlet_step_nve(DT, manager=oracle.PARALLEL, nthreads=threads)
     t0 = time.perf_counter()
     for _ in range(k):
-        s.verlet_step_nve(DT, manager=O.PARALLEL, nthreads=threads)
+        s.verlet_step_nve(DT, manager=oracle.PARALLEL, nthreads=threads)
     el = time.perf_counter() - t0
     v = n * k / el
     line = {
@@ -195,9 +233,9 @@ def run_reference(args, rank, world):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args, n),
         "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{k} NVE steps of the {n}-atom system from its FCC start state (same "
-                                   f"neighbour count per atom as the melted liquid) after {w} warm-up step(s), "
-                                   "LJVParallelManager restated with OpenMP (oracle/pis_oracle.cpp)"},
+                         "sample": f"{k} NVE steps of the {n}-atom liquid melted on the CPU for {args.equil} steps "
+                                   f"({t_melt:.0f} s, untimed), after {w} warm-up step(s); LJVParallelManager "
+                                   "restated with OpenMP (oracle/pis_oracle.cpp)"},
         "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -261,19 +299,24 @@ def main():
     stages_per = stages / args.steps
     list_per_atom = st["list_entries"] / n
     fused = bool(st.get("fused_step"))
+    step_kernel = "k_step_mixed" if fused else "k_force_mixed"
+    # Algorithmic bytes of one atom-step (the compulsory HBM traffic of a full-list step with FP64
+    # state): list indices 4 nn + own position 24 + velocity read/write 48 + force write 24 + type 4
+    # (= 4 nn + 100, about 404 B at nn = 76); neighbour-position gathers count as cache-resident.
+    force_bytes = n * ALG_BYTES_PER_ATOM + st["list_entries"] * 4
+    # what this implementation's layout moves per atom-step (double4 padding, the acceleration
+    # stream, build snapshot, FP32 coordinates), for comparison with the measured DRAM traffic
     if fused:
-        # fused step kernel, per atom: nn 4 + own cell-relative position 16 + force write 32 +
-        # velocity and acceleration read/write 2 x 64 + position read/write 64 + build snapshot 32 +
-        # build-time cell-relative position 16 + new cell-relative position 16, plus the list words
-        step_kernel, per_atom_bytes = "k_step_mixed", 4 + 16 + 32 + 64 + 64 + 64 + 32 + 16 + 16
+        impl_bytes = n * (4 + 16 + 32 + 64 + 64 + 64 + 32 + 16 + 16) + st["list_entries"] * 4
     else:
-        # force kernel: nn + own cell-relative position + force write, plus the list words
-        step_kernel, per_atom_bytes = "k_force_mixed", 4 + 16 + 32
-    force_bytes = n * per_atom_bytes + st["list_entries"] * 4
+        impl_bytes = n * (4 + 16 + 32) + st["list_entries"] * 4
     force_ms = stages_per[2]
     achieved = force_bytes / (force_ms * 1e-3) / 1e9
     pairs_per_step = 27.6 * n  # in-cutoff unordered pairs per step at rho* = 0.8442
     traffic = read_traffic("step_mixed" if fused else "force_mixed", n)
+    # FP32 work of the pair loop: 23 flops per list entry plus 3 per in-cutoff (full-list) pair
+    fp32_flops = n * (list_per_atom * FLOPS_PER_CANDIDATE + 2 * 27.6 * FLOPS_PER_PAIR_ENERGY)
+    fp32_peak, fp64_peak = probe_peaks()
 
     # ---- plain FP64 on the same state --------------------------------------------------------
     f64 = GpuContext(TABLE, 1, skin=SKIN, precision="fp64")
@@ -284,6 +327,11 @@ def main():
     ms64, _ = f64.run_timed(DT, k64)
     ms64 = max_over_ranks(ms64, world)
     v64 = world * n * k64 / (ms64 * 1e-3)
+    k64s = min(k64, 20)
+    _, st64 = f64.run_timed(DT, k64s, stages=True)
+    force64_ms = st64[2] / k64s
+    list64 = f64.stats()["list_entries"] / n  # half list
+    fp64_flops = n * (list64 * FLOPS_PER_CANDIDATE + 27.6 * FLOPS_PER_PAIR_ENERGY)
     f64f = GpuContext(TABLE, 1, skin=SKIN, precision="fp64", fp64_fast=True)
     f64f.set_state(melt_pos, types, [1.0], h, velocities=melt_vel)
     f64f.compute_potential(want_forces=False)
@@ -329,6 +377,7 @@ def main():
 
     drift = None if args.no_drift else run_drift(args, melt_pos, melt_vel, types, h, tuned)
     batched = None if args.no_batch else run_batched(args, rank, world)
+    mix_errors = None if (args.no_batch or args.no_drift) else run_batch_errors(args, tuned)
     served = None if (args.no_serve or rank != 0) else run_served(args)
 
     cpu = None
@@ -346,35 +395,48 @@ def main():
                                     "(the CLI's manager) restated serially (oracle/pis_oracle.cpp)"}}
 
     if rank == 0:
+        roofline = {"bound": "hbm", "kernel": step_kernel, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": achieved / hbm_peak, "peak_source": peak_src, "traffic": traffic,
+                    "algorithmic_bytes_per_launch": force_bytes,
+                    "implementation_bytes_per_launch": impl_bytes,
+                    "traffic_over_algorithmic": (traffic / force_bytes) if traffic else None,
+                    "fp32_pipe": pipe_fraction(fp32_flops, force_ms, fp32_peak),
+                    "fp64_pipe_plain_fp64_force": pipe_fraction(fp64_flops, force64_ms, fp64_peak)}
+        batched_summary = None
+        if batched:
+            batched_summary = {k: batched[k] for k in ("replicas", "atoms", "mixed", "fp64", "mixed_over_fp64")}
+            if mix_errors:
+                batched_summary["errors"] = mix_errors["summary"]
         line = {
             "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32-pair/f64-accumulate",
             "data": "synthetic", "config": workload_config(args, n),
             "precision": "mixed",
-            "pairs_per_s": world * pairs_per_step * args.steps / (ms * 1e-3),
-            "fp64": {"value": v64, "unit": "atom-steps/s", "steps": k64, "ms_per_step": ms64 / k64,
-                     "dtype": "f64", "list": "half"},
-            "fp64_fast": {"value": v64f, "unit": "atom-steps/s", "steps": k64, "dtype": "f64",
-                          "note": "FMA / Newton-reciprocal variant, same cutoff decisions"},
-            "mixed_over_fp64": value / v64,
-            "batched": batched,
+            # details first; the figures the summary keys below restate come last on the line
             "served": served,
-            "error_vs_fp64": {"force_rms_rel": force_rms, "pe_rel": pe_rel},
+            "drift": drift,
+            "batched_detail": batched,
+            "batched_errors_vs_fp64": mix_errors,
             "stages_ms_per_step": {"integrate1": stages_per[0], "rebuild": stages_per[1], "force": stages_per[2],
                                    "integrate2": stages_per[3], "reduce": stages_per[4]},
-            "rebuilds_per_step": rebuilds_per_step,
+            "fp64_stages_ms_per_step": [float(x) / k64s for x in st64],
             "tuned_options": tuned,
-            "drift": drift,
+            "rebuilds_per_step": rebuilds_per_step,
             "list_entries_per_atom": list_per_atom,
-            "roofline": {"bound": "hbm", "kernel": step_kernel, "achieved": achieved, "peak": hbm_peak,
-                         "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_src,
-                         "traffic": traffic, "algorithmic_bytes_per_launch": force_bytes},
+            "pairs_per_s": world * pairs_per_step * args.steps / (ms * 1e-3),
+            "fp64_fast": {"value": v64f, "unit": "atom-steps/s", "steps": k64, "dtype": "f64",
+                          "note": "FMA / Newton-reciprocal variant, same cutoff decisions"},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d / k_e2e,
                     "d2h_bytes_per_step": d2h / k_e2e, "seconds": e2e_s,
-                    "path": "pis_gpu_set_state + compute_potential + verlet_step_nve(K, per-step PE) + get_state, "
-                            "pinned host buffers"},
+                    "path": "set_state + compute_potential + verlet_step_nve(K) + get_state, pinned host buffers"},
+            "roofline": roofline,
+            "error_vs_fp64": {"force_rms_rel": force_rms, "pe_rel": pe_rel},
+            "batched": batched_summary,
+            "fp64": {"value": v64, "unit": "atom-steps/s", "steps": k64, "ms_per_step": ms64 / k64,
+                     "dtype": "f64", "list": "half"},
+            "mixed_over_fp64": value / v64,
             "gpu_launches": launches,
             "clocks": clk.summary(),
         }
@@ -421,6 +483,61 @@ def run_batched(args, rank, world):
         b.close()
     out["mixed_over_fp64"] = out["mixed"] / out["fp64"]
     return out
+
+
+def run_batch_errors(args, tuned, count=6):
+    """Error of the mixed path against FP64 on representative replicas of the 512-replica mix (the
+    smallest and largest systems, the median one, and the hottest, coldest and densest of the rest):
+    each replica is admitted to an FP64 pool and to a mixed pool from the same seed; force RMS and
+    energy error at step 0, then 10^4 NVE steps in each with the total energy every 500 steps and its
+    drift per atom per 10^4 steps."""
+    from pis_gb300.batch import Batch, lj_pool_cells
+    jobs = batch_jobs(seed=2024)
+    order = sorted(range(len(jobs)), key=lambda r: jobs[r].k)
+    pick = [order[0], order[-1], order[len(order) // 2]]
+    for key in (lambda r: jobs[r].t_star, lambda r: -jobs[r].t_star, lambda r: jobs[r].rho):
+        for r in sorted(range(len(jobs)), key=key, reverse=True):
+            if r not in pick:
+                pick.append(r)
+                break
+    pick = pick[:count]
+    steps, chunk = args.drift_steps, 500
+    sel = [jobs[r] for r in pick]
+    atoms = sum(4 * j.k ** 3 for j in sel)
+    cells = sum(lj_pool_cells(j.k, j.rho) for j in sel)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        kw = tuned if prec == "mixed" else {}
+        b = Batch(atoms + 1024, len(sel), cells + 1024, precision=prec, **kw)
+        slots = []
+        for j in sel:
+            j2 = type(j)(j.k, j.rho, j.t_star, j.rcut, j.skin, j.dt, steps, j.seed)
+            slots.append(b.admit_lj(j2))
+        first = [b.result(sl, 4 * j.k ** 3) for sl, j in zip(slots, sel)]
+        series = [[f["pe"] + f["ke"]] for f in first]
+        for _ in range(steps // chunk):
+            b.advance(chunk)
+            for q, sl in enumerate(slots):
+                r = b.result(sl, state=False)
+                series[q].append(r["pe"] + r["ke"])
+        res[prec] = (first, series)
+        b.close()
+    reps = []
+    for q, (r, j) in enumerate(zip(pick, sel)):
+        n = 4 * j.k ** 3
+        f64, fm = res["fp64"][0][q], res["mixed"][0][q]
+        d64 = drift_stats(np.array(res["fp64"][1][q]), n, chunk)["drift_per_atom_per_1e4_steps"]
+        dm = drift_stats(np.array(res["mixed"][1][q]), n, chunk)["drift_per_atom_per_1e4_steps"]
+        reps.append({"replica": r, "atoms": n, "rho": j.rho, "t_star": j.t_star,
+                     "force_rms_rel": float(np.sqrt(np.sum((fm["force"] - f64["force"]) ** 2) / np.sum(f64["force"] ** 2))),
+                     "pe_rel": abs(fm["pe"] - f64["pe"]) / abs(f64["pe"]),
+                     "drift_fp64": d64, "drift_mixed": dm})
+    summary = {"replicas": len(reps), "steps": steps,
+               "max_force_rms_rel": max(x["force_rms_rel"] for x in reps),
+               "max_pe_rel": max(x["pe_rel"] for x in reps),
+               "max_abs_drift_mixed": max(abs(x["drift_mixed"]) for x in reps),
+               "max_abs_drift_fp64": max(abs(x["drift_fp64"]) for x in reps)}
+    return {"per_replica": reps, "summary": summary}
 
 
 def energy_series(ctx, steps, chunk):

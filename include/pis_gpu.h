@@ -114,6 +114,11 @@ pis_status pis_gpu_create(const pis_lj_pair* table, int32_t n_pairs, int32_t n_t
                                  * context and batch of the process */
 #define PIS_OPT_UNFUSED 32 /* mixed precision, default kernel shape: separate force, kick and drift kernels
                             * in each step instead of the fused step kernel (same results bit for bit) */
+#define PIS_OPT_REF_ORDER 64 /* FP64 precision, full list: every atom's force terms are summed in the order of the
+                             * reference's cell walk (LJVOffsetManager::compute_potential,
+                             * src/potentials/lennard_jones.rs:186-244, cells at the largest cutoff,
+                             * src/atoms/neighbour_list.rs:9-165), so forces and trajectories equal the
+                             * reference's bit for bit; needs at least 3 cells of the largest cutoff per axis */
 #define PIS_OPT_CLUSTER(m) ((m) << 24) /* mixed path, neighbour-list shape: 1 = one list per atom,
                                         * 2 or 4 = one list per cluster of m spatially adjacent atoms
                                         * of a cell (each neighbour read serves m pairs);
@@ -147,7 +152,11 @@ pis_status pis_gpu_verlet_step_nve(pis_gpu_ctx* ctx, double dt, int64_t n_steps,
 pis_status pis_gpu_get_state(pis_gpu_ctx* ctx, double* pos, double* vel, double* force);
 
 /* Atoms::kinetic_energy and Atoms::virial_tensor (src/atoms/properties.rs:17-24, 49-51) of the
- * current device state; virial is row-major W[a][b] = sum_i r_i[a] F_i[b]. Either may be NULL. */
+ * current device state; virial is row-major W[a][b] = sum_i r_i[a] F_i[b]. Either may be NULL.
+ * In FP64 precision every energy and virial this library returns is an exact sum, independent of
+ * summation order: each term t quantised to sign(t) floor(|t| 2^104), the integers added exactly,
+ * the total rounded to the nearest double (NaN if a term is not finite or reaches 2^56). For terms
+ * of magnitude 2^-52 or more this is the exactly rounded sum of the reference's own terms. */
 pis_status pis_gpu_reductions(pis_gpu_ctx* ctx, double* ke, double* virial);
 
 /* Per-atom neighbour sets within each pair's cutoff at the current positions, in original atom
@@ -173,6 +182,11 @@ void pis_gpu_destroy(pis_gpu_ctx* ctx);
  * time the five stages of a step (integrate-1, list rebuild, forces, integrate-2, reductions),
  * summed over the steps, at the cost of one host sync per 50-step graph. */
 pis_status pis_gpu_run_timed(pis_gpu_ctx* ctx, double dt, int64_t n_steps, double* device_ms, double* stage_ms);
+
+/* Measurement hook (no counterpart in the reference): the arithmetic peak of the current GPU's
+ * FP32 and FP64 pipes in TFLOP/s (one fused multiply-add = 2 flops), measured with independent
+ * multiply-add chains on every SM; the denominators of the force kernels' pipe fractions. */
+pis_status pis_gpu_probe_peaks(double* fp32_tflops, double* fp64_tflops);
 
 /* Force evaluation that allocates no device memory (no counterpart in the reference). For callers
  * that cannot allocate device memory while running - a host whose framework owns the whole device

@@ -106,8 +106,17 @@ def lib():
         L.or_temperature.argtypes = [S, d]
         L.or_temperature.restype = d
         L.or_run_nve.argtypes = [S, d, C.c_int64, C.c_int32, C.c_int32, P(d), P(d)]
+        L.or_xsum_array.argtypes = [P(d), C.c_int64]
+        L.or_xsum_array.restype = d
+        L.or_exact_kinetic_energy.argtypes = [S]
+        L.or_exact_kinetic_energy.restype = d
+        L.or_exact_virial_tensor.argtypes = [S, P(d)]
+        L.or_compute_offset_exact.argtypes = [S, P(d)]
+        L.or_compute_offset_exact.restype = d
+        L.or_run_nve_exact.argtypes = [S, d, C.c_int64, P(d), P(d), P(d)]
         L.or_fcc_lattice.argtypes = [d, C.c_int64, C.c_int64, C.c_int64, P(d)]
         L.or_remove_drift_and_rescale.argtypes = [S, d]
+        L.or_gaussian_velocities.argtypes = [C.c_int64, P(d), d, C.c_uint64, P(d)]
         L.or_num_threads_available.restype = C.c_int32
         N = P(_Nhc)
         L.or_nhc_init.argtypes = [N, d, d, d]
@@ -238,6 +247,14 @@ class Mtk:
         return lib().or_mtk_potential_energy(C.byref(self._c), _ptr(hh, C.c_double))
 
 
+def xsum(values) -> float:
+    """The exact-sum definition shared with the GPU library: every term quantised to
+    sign(t) floor(|t| 2^104), summed exactly, rounded to the nearest double (NaN for a term of
+    magnitude >= 2^56 or a non-finite term)."""
+    v = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
+    return float(lib().or_xsum_array(_ptr(v, C.c_double), len(v)))
+
+
 def fcc_lattice(a, nx, ny, nz) -> np.ndarray:
     pos = np.zeros((nx * ny * nz * 4, 3))
     lib().or_fcc_lattice(a, nx, ny, nz, _ptr(pos, C.c_double))
@@ -308,6 +325,32 @@ class System:
         ke = np.zeros(steps + 1)
         lib().or_run_nve(C.byref(self._s), dt, steps, manager, nthreads, _ptr(pe, C.c_double), _ptr(ke, C.c_double))
         return pe, ke
+
+    def compute_potential_exact(self):
+        """compute_potential with the offset manager: forces as the reference leaves them;
+        returns (exact-sum energy, walk-order energy)."""
+        self._refresh()
+        out = np.zeros(1)
+        pe = lib().or_compute_offset_exact(C.byref(self._s), _ptr(out, C.c_double))
+        return float(out[0]), pe
+
+    def run_nve_exact(self, dt, steps):
+        """run_nve with the offset manager, energies as exact sums: (pe, ke, pe_walk_order)."""
+        self._refresh()
+        pe, ke, pw = np.zeros(steps + 1), np.zeros(steps + 1), np.zeros(steps + 1)
+        lib().or_run_nve_exact(C.byref(self._s), dt, steps, _ptr(pe, C.c_double), _ptr(ke, C.c_double),
+                               _ptr(pw, C.c_double))
+        return pe, ke, pw
+
+    def kinetic_energy_exact(self) -> float:
+        self._refresh()
+        return lib().or_exact_kinetic_energy(C.byref(self._s))
+
+    def virial_tensor_exact(self) -> np.ndarray:
+        self._refresh()
+        w = np.zeros(9)
+        lib().or_exact_virial_tensor(C.byref(self._s), _ptr(w, C.c_double))
+        return w.reshape(3, 3)
 
     def verlet_step_nvt_nhc(self, dt, nhc, manager=OFFSET, nthreads=1) -> float:
         self._refresh()
@@ -415,6 +458,21 @@ class System:
         h = np.diag([data["xhi"] - data["xlo"], data["yhi"] - data["ylo"], data["zhi"] - data["zlo"]])
         return System(data["positions"], data["type_ids"], data["masses"], h, data["table"],
                       velocities=data["velocities"], shift=shift)
+
+
+def maxwell_boltzmann(masses_per_atom, temperature, seed) -> np.ndarray:
+    """This project's seeded Maxwell-Boltzmann velocities (SplitMix64 + Box-Muller draw, then the
+    reference's drift removal and rescale, src/atoms/velocities.rs:35-59), computed without the GPU
+    library: the CPU baseline's start state."""
+    m = np.ascontiguousarray(masses_per_atom, dtype=np.float64)
+    n = len(m)
+    v = np.zeros((n, 3))
+    lib().or_gaussian_velocities(n, _ptr(m, C.c_double), float(temperature), int(seed), _ptr(v, C.c_double))
+    uniq = sorted(set(m.tolist()))
+    types = np.array([uniq.index(x) + 1 for x in m.tolist()], np.int32)
+    s = System(np.zeros((n, 3)), types, uniq, np.eye(3), {}, velocities=v)
+    s.remove_drift_and_rescale(temperature)
+    return s.vel.copy()
 
 
 def num_threads_available() -> int:

@@ -278,6 +278,111 @@ double or_compute_verlet27(or_system* sys) {
     return pe;
 }
 
+// ---- Exact sums (not part of the reference) -----------------------------------------------------
+// The reference adds energies in its cell-walk order and the virial through a blocked matrix
+// product; a parallel GPU sums in another order, so two correct programs differ in the last bits
+// of every reduction. To compare them without depending on the order, both sides can also form
+// one defined sum: each term t is quantised to q(t) = sign(t) * floor(|t| * 2^104) (an integer),
+// the integers are added exactly, and the result is the double nearest to (sum q) * 2^-104, ties
+// to even. A term of magnitude 2^56 or more, an infinity or a NaN makes the sum NaN. Terms of
+// magnitude 2^-52 or more are represented exactly, so for them this is the exactly rounded sum.
+// This implementation (four 64-bit two's-complement limbs, full carry on every add) is written
+// independently of the GPU library's (lazily carried 32-bit limbs), so each checks the other.
+typedef struct {
+    uint64_t w[4];
+    int64_t bad;
+} or_xsum;
+
+static const int XSUM_FRAC = 104;
+
+void or_xsum_clear(or_xsum* x) {
+    std::memset(x, 0, sizeof(*x));
+}
+
+void or_xsum_add(or_xsum* x, double t) {
+    if (!std::isfinite(t) || std::fabs(t) >= 0x1p56) {
+        x->bad++;
+        return;
+    }
+    if (t == 0.0) return;
+    int e = 0;
+    const double m = std::frexp(std::fabs(t), &e);  // |t| = m 2^e, m in [0.5, 1)
+    const uint64_t mant = (uint64_t)std::ldexp(m, 53);  // exact, in [2^52, 2^53)
+    const int sh = e - 53 + XSUM_FRAC;                // q = floor(mant * 2^sh)
+    uint64_t q[4] = {0, 0, 0, 0};
+    if (sh >= 0) {
+        const int w = sh / 64, b = sh % 64;
+        q[w] |= mant << b;
+        if (b && w + 1 < 4) q[w + 1] |= mant >> (64 - b);
+    } else if (sh > -64) {
+        q[0] = mant >> (-sh);
+    }
+    if (t < 0.0) {  // two's complement negation of the 256-bit q
+        unsigned carry = 1;
+        for (int k = 0; k < 4; ++k) {
+            const uint64_t v = ~q[k];
+            q[k] = v + carry;
+            carry = (carry && q[k] == 0) ? 1u : 0u;
+        }
+    }
+    unsigned __int128 c = 0;
+    for (int k = 0; k < 4; ++k) {
+        c += (unsigned __int128)x->w[k] + q[k];
+        x->w[k] = (uint64_t)c;
+        c >>= 64;
+    }
+}
+
+double or_xsum_value(const or_xsum* x) {
+    if (x->bad) return std::nan("");
+    uint64_t w[4] = {x->w[0], x->w[1], x->w[2], x->w[3]};
+    const bool neg = (w[3] >> 63) != 0;
+    if (neg) {
+        unsigned carry = 1;
+        for (int k = 0; k < 4; ++k) {
+            const uint64_t v = ~w[k];
+            w[k] = v + carry;
+            carry = (carry && w[k] == 0) ? 1u : 0u;
+        }
+    }
+    int p = -1;  // highest set bit
+    for (int k = 3; k >= 0 && p < 0; --k)
+        if (w[k]) p = 64 * k + 63 - __builtin_clzll(w[k]);
+    if (p < 0) return 0.0;
+    auto bit = [&](int i) -> uint64_t { return (w[i / 64] >> (i % 64)) & 1u; };
+    uint64_t mant = 0;
+    int lo = p - 52;  // lowest bit kept
+    if (lo <= 0) {
+        mant = w[0];  // p <= 52: the whole value fits in the mantissa
+        lo = 0;
+    } else {
+        for (int i = p; i >= lo; --i) mant = (mant << 1) | bit(i);
+        const uint64_t half = bit(lo - 1);
+        bool sticky = false;
+        for (int i = lo - 2; i >= 0 && !sticky; --i) sticky = bit(i) != 0;
+        if (half && (sticky || (mant & 1u))) {
+            mant += 1;
+            if (mant == (1ull << 53)) {
+                mant >>= 1;
+                lo += 1;
+            }
+        }
+    }
+    const double v = std::ldexp((double)mant, lo - XSUM_FRAC);
+    return neg ? -v : v;
+}
+
+// Exact sum of an array (for tests of the definition itself).
+double or_xsum_array(const double* v, int64_t n) {
+    or_xsum x;
+    or_xsum_clear(&x);
+    for (int64_t i = 0; i < n; ++i) or_xsum_add(&x, v[i]);
+    return or_xsum_value(&x);
+}
+
+// Sink for the exact energy sum of the offset manager's walk (set by the exact run loops).
+static or_xsum* g_pe_sink = nullptr;
+
 // LJVOffsetManager::compute_potential, src/potentials/lennard_jones.rs:186-244: the
 // production path. Cells at max_rcut, 14-offset half stencil, same-cell pairs need i > j.
 // Forces are accumulated (the caller zeroes them, src/potentials/potential.rs:24).
@@ -300,6 +405,7 @@ double or_compute_offset(or_system* sys) {
                             double u, f[3];
                             if (!eval_pair(sys, i, j, &u, f)) continue;
                             pe += u;
+                            if (g_pe_sink) or_xsum_add(g_pe_sink, u);
                             for (int d = 0; d < 3; ++d) {
                                 sys->force[3 * i + d] -= f[d];
                                 sys->force[3 * j + d] += f[d];
@@ -554,6 +660,61 @@ void or_run_nve(or_system* sys, double dt, int64_t steps, int32_t manager, int32
         double pe = or_verlet_step_nve(sys, dt, manager, nthreads);
         if (pe_out) pe_out[s] = pe;
         if (ke_out) ke_out[s] = or_kinetic_energy(sys);
+    }
+}
+
+// Exact-sum forms of the reductions (see or_xsum_add). Kinetic energy: the terms m_i |v_i|^2 are
+// summed and the total halved (halving is exact), so the sum does not depend on whether 1/2 is
+// applied per term; virial: W[a][b] = xsum_i r_i[a] F_i[b].
+double or_exact_kinetic_energy(const or_system* sys) {
+    or_xsum x;
+    or_xsum_clear(&x);
+    for (int64_t i = 0; i < sys->n; ++i) or_xsum_add(&x, mass_i(sys, i) * norm_squared(sys->vel + 3 * i));
+    return 0.5 * or_xsum_value(&x);
+}
+
+void or_exact_virial_tensor(const or_system* sys, double* w) {
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            or_xsum x;
+            or_xsum_clear(&x);
+            for (int64_t i = 0; i < sys->n; ++i) or_xsum_add(&x, sys->pos[3 * i + a] * sys->force[3 * i + b]);
+            w[3 * a + b] = or_xsum_value(&x);
+        }
+}
+
+// compute_potential with the offset manager (forces exactly as the reference's walk leaves them)
+// and the exact sum of the same pair energies; returns the walk-order sum, *pe_exact the exact one.
+double or_compute_offset_exact(or_system* sys, double* pe_exact) {
+    std::memset(sys->force, 0, sizeof(double) * 3 * (size_t)sys->n);
+    or_xsum x;
+    or_xsum_clear(&x);
+    g_pe_sink = &x;
+    const double pe = or_compute_offset(sys);
+    g_pe_sink = nullptr;
+    if (pe_exact) *pe_exact = or_xsum_value(&x);
+    return pe;
+}
+
+// or_run_nve with the offset manager, reporting exact sums: pe_out[k] the exact energy of step k
+// (entry 0 before the first step), ke_out[k] the exact kinetic energy after it, pe_walk_out[k]
+// the reference's own walk-order energy. The trajectory is the reference's (sums do not feed
+// back into an NVE step). Outputs may be null.
+void or_run_nve_exact(or_system* sys, double dt, int64_t steps, double* pe_out, double* ke_out, double* pe_walk_out) {
+    double pex = 0.0;
+    const double pe0 = or_compute_offset_exact(sys, &pex);
+    if (pe_out) pe_out[0] = pex;
+    if (pe_walk_out) pe_walk_out[0] = pe0;
+    if (ke_out) ke_out[0] = or_exact_kinetic_energy(sys);
+    or_xsum x;
+    for (int64_t s = 1; s <= steps; ++s) {
+        or_xsum_clear(&x);
+        g_pe_sink = &x;
+        const double pe = or_verlet_step_nve(sys, dt, OR_OFFSET, 1);
+        g_pe_sink = nullptr;
+        if (pe_out) pe_out[s] = or_xsum_value(&x);
+        if (pe_walk_out) pe_walk_out[s] = pe;
+        if (ke_out) ke_out[s] = or_exact_kinetic_energy(sys);
     }
 }
 
@@ -938,6 +1099,42 @@ void or_remove_drift_and_rescale(or_system* sys, double temperature) {
     double t = or_temperature(sys, ke);
     double lambda = std::sqrt(temperature / t);
     for (int64_t k = 0; k < 3 * sys->n; ++k) sys->vel[k] *= lambda;
+}
+
+// The raw Gaussian draw of this project's velocity generator (SplitMix64 stream, Box-Muller pairs,
+// sigma = sqrt(KB T / m); not the reference's rand SmallRng stream, which is not reproduced), so the
+// CPU baseline can rebuild the benchmark's start state without loading the GPU library. Followed by
+// or_remove_drift_and_rescale it gives the library's pis_maxwell_boltzmann bit for bit on one
+// machine (same libm).
+static uint64_t splitmix64_next(uint64_t& x) {
+    uint64_t z = (x += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+void or_gaussian_velocities(int64_t n, const double* m_per_atom, double temperature, uint64_t seed, double* v) {
+    uint64_t state = seed * 0x2545f4914f6cdd1dull + 0x51ed27fa2cbb8d3ull;
+    auto uniform = [&]() { return ((splitmix64_next(state) >> 11) + 0.5) * (1.0 / 9007199254740992.0); };
+    double spare = 0.0;
+    bool have = false;
+    for (int64_t i = 0; i < n; ++i) {
+        const double sigma = std::sqrt(KB * temperature / m_per_atom[i]);
+        for (int d = 0; d < 3; ++d) {
+            double z;
+            if (have) {
+                z = spare;
+                have = false;
+            } else {
+                const double u1 = uniform(), u2 = uniform();
+                const double r = std::sqrt(-2.0 * std::log(u1));
+                z = r * std::cos(2.0 * M_PI * u2);
+                spare = r * std::sin(2.0 * M_PI * u2);
+                have = true;
+            }
+            v[3 * i + d] = sigma * z;
+        }
+    }
 }
 
 int32_t or_num_threads_available(void) {

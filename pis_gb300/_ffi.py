@@ -23,11 +23,11 @@ LIST_KIND = {"default": 0, "half": 1, "full": 2}
 
 
 def option_flags(fp64_fast=False, mixed_kahan=False, lanes=0, batch=0, tma=False, cluster=0, scan=0,
-                 tiles=False, plain_graphs=False, unfused=False) -> int:
+                 tiles=False, plain_graphs=False, unfused=False, ref_order=False) -> int:
     """PIS_OPT_* bits of include/pis_gpu.h for the variant knobs."""
     return ((1 if fp64_fast else 0) | (2 if mixed_kahan else 0) | (4 if tma else 0) | (8 if tiles else 0)
-            | (16 if plain_graphs else 0) | (32 if unfused else 0) | (int(lanes) << 8) | (int(batch) << 16) | (int(cluster) << 24)
-            | (int(scan) << 28))
+            | (16 if plain_graphs else 0) | (32 if unfused else 0) | (64 if ref_order else 0) | (int(lanes) << 8)
+            | (int(batch) << 16) | (int(cluster) << 24) | (int(scan) << 28))
 
 
 class PisError(RuntimeError):
@@ -96,6 +96,7 @@ SIGNATURES = [
     ("pis_gpu_last_error", C.c_char_p, [_VP]),
     ("pis_gpu_destroy", None, [_VP]),
     ("pis_gpu_run_timed", C.c_int, [_VP, C.c_double, C.c_int64, _DP, _DP]),
+    ("pis_gpu_probe_peaks", C.c_int, [_DP, _DP]),
     ("pis_gpu_compute_potential_noalloc", C.c_int, [C.POINTER(LJPair), C.c_int32, C.c_int32, C.c_int64, _VP, _VP, _DP,
                                                     _VP, _VP, _VP]),
     ("pis_batch_create", C.c_int, [C.c_int64, C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.POINTER(_VP)]),

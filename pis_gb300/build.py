@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libpis_gpu.so")
 
-CU_SOURCES = ["engine.cu", "pis_gpu.cu", "pis_batch.cu", "noalloc.cu"]
+CU_SOURCES = ["engine.cu", "pis_gpu.cu", "pis_batch.cu", "noalloc.cu", "probe.cu"]
 CXX_SOURCES = ["host_io.cpp", "host_system.cpp"]
 CLI_SOURCE = "pis_gpu_run.cpp"
 CLI = os.path.join(OUT_DIR, "pis_gpu_run")

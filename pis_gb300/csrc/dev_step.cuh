@@ -593,14 +593,16 @@ __device__ __forceinline__ double rcp_newton(double x) {
 
 template <bool FULL, bool FAST, int LPA>
 __global__ void __launch_bounds__(256) k_force_fp64(const DP P, int respect_steps) {
-    __shared__ double sh[32];
+    __shared__ long long shx[XS_WORDS * 8];
     auto tile = cg::tiled_partition<LPA>(cg::this_thread_block());
     int s, i;
     const bool live = group_atom_of<LPA>(P, s, i);
     if (s < 0) return;
     if (!slot_runs(P, s, respect_steps)) return;  // uniform per block (one slot per chunk)
     const int gl = (int)tile.thread_rank();
-    double e = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    XAcc e;  // pair energies as an exact sum (order-independent)
+    xacc_zero(e);
     if (live) {
         const SysParams& sp = P.sp[s];
         const int cur = P.st[s].cur;
@@ -659,7 +661,6 @@ __global__ void __launch_bounds__(256) k_force_fp64(const DP P, int respect_step
                 fx = __dsub_rn(fx, gx);
                 fy = __dsub_rn(fy, gy);
                 fz = __dsub_rn(fz, gz);
-                e = __dadd_rn(e, u);
             } else {
                 gx = c * rx;
                 gy = c * ry;
@@ -667,8 +668,8 @@ __global__ void __launch_bounds__(256) k_force_fp64(const DP P, int respect_step
                 fx -= gx;
                 fy -= gy;
                 fz -= gz;
-                e += u;
             }
+            xacc_add(e, u);
             if (!FULL) {
                 atomicAdd(&P.frc[j].x, gx);
                 atomicAdd(&P.frc[j].y, gy);
@@ -691,8 +692,123 @@ __global__ void __launch_bounds__(256) k_force_fp64(const DP P, int respect_step
             atomicAdd(&P.frc[i].z, fz);
         }
     }
-    double tot = block_sum<256>(e, sh);
-    if (threadIdx.x == 0) P.pe_part[blockIdx.x] = tot;
+    xacc_block_store<256>(e, P.xpe_part + (int64_t)blockIdx.x * XS_WORDS, shx);
+}
+
+// FP64 forces in the reference's own order (PIS_OPT_REF_ORDER): forces bit-identical to
+// LJVOffsetManager::compute_potential (src/potentials/lennard_jones.rs:186-244).
+// The reference walks its cells at max_rcut (cx outermost, cz innermost; src/atoms/neighbour_list.rs:
+// 9-63), the 14 forward offsets of each cell in their fixed order (:94-165), then i over the home
+// cell's atoms and j over the neighbour cell's atoms, both in ascending atom index; it subtracts
+// f = c r_ij from F_i and adds it to F_j. Seen from one atom a, every pair term is subtracted as
+// F_a -= c r_ab (r_ab = minimum image of r_b - r_a): when a is the walk's j, f is computed from
+// r_ba = -r_ab exactly, so F_a + f = F_a - c r_ab bit for bit. The sequence of terms reaching F_a is
+// ordered by the walk's key (visit rank of the i atom's cell, offset index, then the partner's
+// index), which depends only on the pair and the current cells. So each thread collects the keys
+// of its in-range list entries, sorts them, and subtracts the terms in that order from zero: the
+// same roundings in the same order as the reference, hence the same forces, trajectory and
+// energies for every step. Needs >= 3 reference cells per axis (below that the reference visits a
+// neighbour cell twice) and a full list.
+// Key (64 bits): cell visit rank (25) | offset index (4) | partner's original index (26) | list slot (9).
+__device__ __forceinline__ int ref_fwd_index(int dx, int dy, int dz) {
+    // index of (dx, dy, dz) in FORWARD_NEIGHBOUR_OFFSETS, -1 when it is a backward offset
+    if (dz == 1) return 5 + (dy + 1) * 3 + (dx + 1);
+    if (dz == 0 && dy == 1) return 2 + (dx + 1);
+    if (dz == 0 && dy == 0) return dx == 0 ? 0 : (dx == 1 ? 1 : -1);
+    return -1;
+}
+// Reference cell of a wrapped position: floor(s_d n_d) with s = h^-1 r, saturated at 0 as Rust's
+// `f64 as usize`, then modulo n_d (src/atoms/neighbour_list.rs:17-33).
+__device__ __forceinline__ int ref_cell_axis(double x, double hinv, int n) {
+    long long c = __double2ll_rd(__dmul_rn(__dmul_rn(hinv, x), (double)n));
+    if (c < 0) c = 0;
+    return (int)(c % n);
+}
+__device__ __forceinline__ int ref_wrap_delta(int d, int n) {
+    if (d > 1) d -= n;
+    if (d < -1) d += n;
+    return d;
+}
+constexpr int REF_MAX_ENTRIES = 256;  // in-range pairs per atom (local memory: 2 KB per thread)
+
+__global__ void __launch_bounds__(256) k_force_fp64_ref(const DP P, int respect_steps) {
+    __shared__ long long shx[XS_WORDS * 8];
+    int s, i;
+    const bool live = atom_of(P, s, i);
+    if (s < 0) return;
+    if (!slot_runs(P, s, respect_steps)) return;
+    XAcc e;
+    xacc_zero(e);
+    if (live) {
+        uint64_t keys[REF_MAX_ENTRIES];
+        const SysParams& sp = P.sp[s];
+        const int cur = P.st[s].cur;
+        const double4_32a* __restrict__ pos = P.pos[cur];
+        const int32_t* __restrict__ oid = P.id[cur];
+        const double4_32a pi = pos[i];
+        const LJDev* tab = P.tab + sp.tab0 + type_of(pi.w) * sp.nt;
+        const double hx = sp.h[0], hy = sp.h[1], hz = sp.h[2];
+        const double ix = sp.hinv[0], iy = sp.hinv[1], iz = sp.hinv[2];
+        const int nx = sp.rnc[0], ny = sp.rnc[1], nz = sp.rnc[2];
+        const int ax = ref_cell_axis(pi.x, ix, nx), ay = ref_cell_axis(pi.y, iy, ny), az = ref_cell_axis(pi.z, iz, nz);
+        const uint64_t rank_a = (uint64_t)((ax * ny + ay) * nz + az);
+        const int nn = P.nn[i];
+        const int64_t npad = P.npad;
+        int m = 0;
+        for (int k = 0; k < nn; ++k) {
+            const int j = (int)(P.nbr[(int64_t)k * npad + i] & JMASK);
+            const double4_32a pj = pos[j];
+            const LJDev& T = tab[type_of(pj.w)];
+            if (!T.present) continue;
+            const double rx = min_image_axis(__dsub_rn(pj.x, pi.x), hx, ix);
+            const double ry = min_image_axis(__dsub_rn(pj.y, pi.y), hy, iy);
+            const double rz = min_image_axis(__dsub_rn(pj.z, pi.z), hz, iz);
+            const double r2 = norm2_ref(rx, ry, rz);
+            if (r2 > T.rc2_hi || (r2 >= T.rc2_lo && sqrt(r2) > T.rcut)) continue;
+            const int bx = ref_cell_axis(pj.x, ix, nx), by = ref_cell_axis(pj.y, iy, ny), bz = ref_cell_axis(pj.z, iz, nz);
+            const int dx = ref_wrap_delta(bx - ax, nx), dy = ref_wrap_delta(by - ay, ny), dz = ref_wrap_delta(bz - az, nz);
+            int o = ref_fwd_index(dx, dy, dz);
+            uint64_t rank = rank_a;
+            if (o < 0) {  // the partner's cell is the walk's home cell
+                o = ref_fwd_index(-dx, -dy, -dz);
+                rank = (uint64_t)((bx * ny + by) * nz + bz);
+            }
+            const uint64_t key = (rank << 39) | ((uint64_t)(o & 15) << 35) | ((uint64_t)oid[j] << 9) | (uint64_t)k;
+            if (m < REF_MAX_ENTRIES) keys[m] = key;
+            ++m;
+        }
+        if (m > REF_MAX_ENTRIES) {
+            atomicOr(&P.st[s].flags, FLAG_LIST_OVERFLOW);
+            m = REF_MAX_ENTRIES;
+        }
+        for (int a = 1; a < m; ++a) {  // insertion sort (a few dozen keys)
+            const uint64_t v = keys[a];
+            int b = a - 1;
+            while (b >= 0 && keys[b] > v) {
+                keys[b + 1] = keys[b];
+                --b;
+            }
+            keys[b + 1] = v;
+        }
+        double fx = 0.0, fy = 0.0, fz = 0.0;
+        for (int a = 0; a < m; ++a) {
+            const int k = (int)(keys[a] & 511u);
+            const int j = (int)(P.nbr[(int64_t)k * npad + i] & JMASK);
+            const double4_32a pj = pos[j];
+            const LJ64 L = lj64_load(tab[type_of(pj.w)]);
+            const double rx = min_image_axis(__dsub_rn(pj.x, pi.x), hx, ix);
+            const double ry = min_image_axis(__dsub_rn(pj.y, pi.y), hy, iy);
+            const double rz = min_image_axis(__dsub_rn(pj.z, pi.z), hz, iz);
+            double u, c;
+            lj_fp64(L, norm2_ref(rx, ry, rz), u, c);
+            fx = __dsub_rn(fx, __dmul_rn(c, rx));
+            fy = __dsub_rn(fy, __dmul_rn(c, ry));
+            fz = __dsub_rn(fz, __dmul_rn(c, rz));
+            xacc_add(e, u);
+        }
+        P.frc[i] = make_double4_32a(fx, fy, fz, 0.0);
+    }
+    xacc_block_store<256>(e, P.xpe_part + (int64_t)blockIdx.x * XS_WORDS, shx);
 }
 
 // Mixed precision forces, full list: FP32 pair arithmetic on cell-relative coordinates

@@ -36,6 +36,7 @@ __device__ __forceinline__ double twice_ke_mixed(const double4_32a& v) {
 template <bool UPDATE, bool EXACT>
 __global__ void k_integrate2(const DP P, int respect_steps) {
     __shared__ double sh[32];
+    __shared__ long long shx[XS_WORDS * 8];
     int s, i;
     bool live = atom_of(P, s, i);
     if (s < 0) return;
@@ -73,6 +74,23 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
         // sum of (0.5 m) |v|^2 (properties.rs:17-24) bit for bit
         ke = EXACT ? __dmul_rn(m, norm2_ref(v.x, v.y, v.z)) : twice_ke_mixed(v);
         if (st.want_virial) p = P.pos[cur][i];
+    }
+    if (EXACT) {
+        // FP64 path: exact sums of m |v|^2 (halved at the step end) and of r_i[a] F_i[b]
+        XAcc x;
+        xacc_zero(x);
+        if (live) xacc_add(x, ke);
+        xacc_block_store<256>(x, P.xke_part + (int64_t)blockIdx.x * XS_WORDS, shx);
+        if (st.want_virial) {
+            const double r[3] = {p.x, p.y, p.z}, g[3] = {f.x, f.y, f.z};
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    xacc_zero(x);
+                    if (live) xacc_add(x, __dmul_rn(r[a], g[b]));
+                    xacc_block_store<256>(x, P.xvir_part + ((int64_t)blockIdx.x * 9 + a * 3 + b) * XS_WORDS, shx);
+                }
+        }
+        return;
     }
     double tot = block_sum<256>(ke, sh);
     if (threadIdx.x == 0) P.ke_part[blockIdx.x] = 0.5 * tot;
@@ -175,8 +193,30 @@ __global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixe
 // Per-slot end of a step (or of a force evaluation): deterministic sums of the chunk partials,
 // energy history, NaN check (PisError::NaNEnergy, src/errors.rs:87-88), counters.
 // mode 0: step; mode 1: force evaluation only (PE); mode 2: KE/virial only.
+// Exact-sum partials of a slot: words of partials first .. first + count - 1 (XS_WORDS each, `stride`
+// apart) added and converted. All threads must call it; the value is valid in thread 0.
+__device__ __forceinline__ double xacc_slot_value(const long long* part, int64_t first, int64_t count, int stride,
+                                                  long long* shx) {
+    XAcc a;
+    xacc_zero(a);
+    for (int64_t c = threadIdx.x; c < count; c += END_THREADS) {
+        const long long* q = part + (first + c) * stride;
+#pragma unroll
+        for (int z = 0; z < XS_LIMBS; ++z) a.l[z] += q[z];
+        a.bad += q[XS_LIMBS];
+    }
+    __shared__ long long tot[XS_WORDS];
+    xacc_block_store<END_THREADS>(a, tot, shx);
+    __syncthreads();
+    double v = 0.0;
+    if (threadIdx.x == 0) v = xacc_value(tot);
+    __syncthreads();
+    return v;
+}
+
 __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) {
     __shared__ double sh[32];
+    __shared__ long long shx[XS_WORDS * (END_THREADS / 32)];
     int s = blockIdx.x;
     const SysParams& sp = P.sp[s];
     if (!sp.active) return;
@@ -185,6 +225,36 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
     if (mode != 0 && !st.eval) return;
     double pe = 0.0, ke = 0.0;
     const int F = P.pe_stride;
+    if (P.exact_sums) {
+        // FP64 pools: exact sums (PE over the force kernel's blocks, m |v|^2 and r_i F_i per chunk)
+        double w[9];
+        const bool vir = st.want_virial && mode != 1;
+        if (mode != 2) pe = xacc_slot_value(P.xpe_part, (int64_t)sp.ch0 * F, (int64_t)sp.nch * F, XS_WORDS, shx);
+        if (mode != 1) ke = 0.5 * xacc_slot_value(P.xke_part, sp.ch0, sp.nch, XS_WORDS, shx);
+        if (vir)
+            for (int q = 0; q < 9; ++q)
+                w[q] = xacc_slot_value(P.xvir_part + (int64_t)q * XS_WORDS, sp.ch0, sp.nch, 9 * XS_WORDS, shx);
+        if (threadIdx.x == 0) {
+            if (mode != 2) {
+                if (P.full_list) pe *= 0.5;
+                st.pe = pe;
+            }
+            if (mode != 1) st.ke = ke;
+            if (vir)
+                for (int q = 0; q < 9; ++q) st.virial[q] = w[q];
+            if ((mode != 2 && pe != pe) || (mode != 1 && ke != ke)) st.flags |= FLAG_NAN;
+            if (mode == 2) {
+                st.eval = 0;
+                st.want_virial = 0;
+            }
+            if (mode == 0) {
+                P.pe_hist[(int64_t)s * P.hist + (st.steps_done % P.hist)] = pe;
+                st.steps_done += 1;
+                st.steps_left -= 1;
+            }
+        }
+        return;
+    }
     if (mode != 2) {
         if (P.cl_force) {  // cluster kernels: cl_lanes partials per cluster chunk
             const int L = P.cl_lanes;

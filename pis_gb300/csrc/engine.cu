@@ -100,7 +100,11 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         return PIS_ERR_INVALID_ARGUMENT;
     }
     half_ = opt.list_kind == PIS_LIST_HALF ||
-            (opt.list_kind == PIS_LIST_DEFAULT && opt.precision == PIS_PRECISION_FP64);
+            (opt.list_kind == PIS_LIST_DEFAULT && opt.precision == PIS_PRECISION_FP64 && !opt.ref_order);
+    if (opt.ref_order && (opt.precision != PIS_PRECISION_FP64 || half_ || opt.lpa != 1 || opt.fp64_fast)) {
+        err = "reference-order forces need the FP64 path with a full list, one thread per atom, exact arithmetic";
+        return PIS_ERR_UNSUPPORTED;
+    }
     if (opt.precision == PIS_PRECISION_MIXED && half_) {
         err = "the mixed-precision path uses a full list";
         return PIS_ERR_UNSUPPORTED;
@@ -147,6 +151,10 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     }
     cap_ = opt.list_cap > 0 ? opt.list_cap : 192;
     cap_ = (cap_ + 31) / 32 * 32;  // whole row groups for every lanes-per-atom choice
+    if (opt.ref_order && cap_ > 512) {
+        err = "reference-order forces keep a 9-bit list slot per entry: list capacity must be at most 512";
+        return PIS_ERR_UNSUPPORTED;
+    }
     npad_ = (int64_t)align_up((size_t)opt.max_atoms, 32);
     if ((double)npad_ * (double)cap_ >= 4294967296.0) {
         err = "neighbour list of the pool exceeds 2^32 entries (atoms x capacity)";
@@ -212,6 +220,12 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         {(void**)&d_->ctl, 256},
     };
     if (fused_) items.push_back({&prel_buf_[1], 16 * NA});
+    const bool exact = opt.precision == PIS_PRECISION_FP64;
+    if (exact) {
+        items.push_back({(void**)&d_->xpe_part, 8 * XS_WORDS * NCH * 32});
+        items.push_back({(void**)&d_->xke_part, 8 * XS_WORDS * NCH});
+        items.push_back({(void**)&d_->xvir_part, 8 * XS_WORDS * 9 * NCH});
+    }
     if (clm_) {
         items.push_back({(void**)&d_->cl_atom, 4 * NCL});
         items.push_back({(void**)&d_->cl_start, 4 * NC});
@@ -233,6 +247,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         base += align_up(it.bytes, 256);
     }
     d_->keep = nullptr;
+    d_->exact_sums = exact ? 1 : 0;
     d_->npad = npad_;
     d_->cap = (int32_t)cap_;
     d_->hist = opt.hist;
@@ -514,6 +529,27 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     p.walk27 = 1;
     for (int a = 0; a < 3; ++a)
         if (nc[a] < 2 || (nc[a] == 2 && !(p.h[a] > 2.0 * std::sqrt((double)p.frlist2) * (1.0 + 1e-5)))) p.walk27 = 0;
+    // the reference's own cell grid at the largest cutoff (Atoms::divide_into_cells,
+    // src/atoms/neighbour_list.rs:45-57: floor(|h column| / rcut), at least 1)
+    double rc_max = 0.0;  // PairPotentialManager::max_rcut (src/potentials/potential.rs:170-179)
+    for (auto& e : d.table)
+        if (e.present && rc_max < e.rcut) rc_max = e.rcut;
+    for (int a = 0; a < 3; ++a) {
+        const double col[3] = {d.h[a], d.h[3 + a], d.h[6 + a]};
+        const double len = std::sqrt(col[0] * col[0] + col[1] * col[1] + col[2] * col[2]);
+        const double q = std::floor(len / rc_max);
+        p.rnc[a] = q < 1.0 ? 1 : (q > 1e9 ? 1000000000 : (int)q);
+    }
+    if (opt_.ref_order) {
+        const double cells = (double)p.rnc[0] * p.rnc[1] * p.rnc[2];
+        if (p.rnc[0] < 3 || p.rnc[1] < 3 || p.rnc[2] < 3 || cells >= 33554432.0) {
+            give_range(free_atoms_, a0, d.n);
+            give_range(free_cells_, c0, ncell + 1);
+            for (int k = 0; k < nt * nt; ++k) free_tab_[tab0 + k] = 1;
+            err = "reference-order forces need 3 to 2^25 reference cells (at the largest cutoff), at least 3 per axis";
+            return -PIS_ERR_UNSUPPORTED;
+        }
+    }
     // chunks
     p.nch = (int32_t)((d.n + opt_.blk - 1) / opt_.blk);
     p.ch0 = 0;  // assigned by the block map
@@ -943,6 +979,10 @@ void Engine::launch_force_mixed(int r) {
 
 void Engine::launch_force_fp64(int r) {
     const unsigned ch = (unsigned)max_chunks_;
+    if (opt_.ref_order) {
+        LAUNCH(k_force_fp64_ref, ch, 256, *d_, r);
+        return;
+    }
 #define PIS_CALL(L) launch_fp64_t<L>(*d_, half_, opt_.fp64_fast, ch, stream_, r)
     PIS_LPA_DISPATCH(opt_.lpa, PIS_CALL)
 #undef PIS_CALL

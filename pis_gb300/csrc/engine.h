@@ -60,6 +60,7 @@ struct SysParams {
     float frlist2;     // FP32 list radius squared, padded so the FP32 test is a superset
     float fsub[3];     // 4 / cell edge: sub-cell index scale of the in-cell atom order
     int32_t walk27;    // the 27-cell walk of the thread-per-atom build is valid (see add_slot)
+    int32_t rnc[3];    // the reference's own cell grid at the largest cutoff (reference-order forces)
 };
 
 // Device-side pair parameters: FP64 quantities computed exactly as the reference does per pair,
@@ -110,6 +111,7 @@ struct PoolOptions {
                                // many atoms (2 or 4; 0 or 1 = per atom)
     bool unfused = false;      // mixed, default kernel shape: separate force, kick and drift kernels
                                // (otherwise one fused step kernel does all three)
+    bool ref_order = false;    // FP64, full list: forces summed in the reference's own order
 };
 
 class Engine {

@@ -28,6 +28,7 @@ struct pis_gpu_ctx {
     bool cell_tiles = false;
     bool plain_graphs = false;
     bool unfused = false;
+    bool ref_order = false;
     std::unique_ptr<pis::Engine> eng;
     pis::PoolOptions pool;  // options the current engine was created with
     int slot = -1;
@@ -64,7 +65,7 @@ bool same_pool(const pis::PoolOptions& a, const pis::PoolOptions& b) {
            a.mixed_kahan == b.mixed_kahan && a.lpa == b.lpa && a.mix_batch == b.mix_batch &&
            a.list_tma == b.list_tma && a.cluster == b.cluster && a.build_cluster == b.build_cluster &&
            a.cell_tiles == b.cell_tiles && a.plain_graphs == b.plain_graphs &&
-           a.unfused == b.unfused;
+           a.unfused == b.unfused && a.ref_order == b.ref_order;
 }
 
 pis_status flags_to_status(pis_gpu_ctx* ctx, const pis::SysState& ss) {
@@ -117,7 +118,7 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
     if (!ctx) return PIS_ERR_INVALID_ARGUMENT;
     if (list_kind < PIS_LIST_DEFAULT || list_kind > PIS_LIST_FULL)
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown list kind");
-    if (flags & ~(PIS_OPT_FP64_FAST | PIS_OPT_MIXED_KAHAN | PIS_OPT_LIST_TMA | PIS_OPT_TILE | PIS_OPT_PLAIN_GRAPHS | PIS_OPT_UNFUSED |
+    if (flags & ~(PIS_OPT_FP64_FAST | PIS_OPT_MIXED_KAHAN | PIS_OPT_LIST_TMA | PIS_OPT_TILE | PIS_OPT_PLAIN_GRAPHS | PIS_OPT_UNFUSED | PIS_OPT_REF_ORDER |
                   PIS_OPT_LANES(0xff) | PIS_OPT_BATCH(0xff) | PIS_OPT_CLUSTER(0xf) | PIS_OPT_SCAN(0x7)))
         return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "unknown option flag");
     const int batch = (flags >> 16) & 0xff;
@@ -143,6 +144,11 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
     ctx->cell_tiles = (flags & PIS_OPT_TILE) != 0;
     ctx->plain_graphs = (flags & PIS_OPT_PLAIN_GRAPHS) != 0;
     ctx->unfused = (flags & PIS_OPT_UNFUSED) != 0;
+    ctx->ref_order = (flags & PIS_OPT_REF_ORDER) != 0;
+    if (ctx->ref_order && (ctx->precision != PIS_PRECISION_FP64 || list_kind == PIS_LIST_HALF || ctx->lpa != 1 ||
+                           ctx->fp64_fast))
+        return fail(ctx, PIS_ERR_UNSUPPORTED,
+                    "reference-order forces need FP64 precision, a full list, one thread per atom, exact arithmetic");
     if (ctx->cell_tiles && (ctx->precision != PIS_PRECISION_MIXED || ctx->lpa != 1 || ctx->list_tma || ctx->cluster))
         return fail(ctx, PIS_ERR_UNSUPPORTED, "neighbour-cell tiles need the mixed path, thread per atom, per-atom lists");
     if (ctx->cluster && (ctx->precision != PIS_PRECISION_MIXED || (ctx->lpa != 1 && ctx->lpa != ctx->cluster) ||
@@ -192,6 +198,7 @@ pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_id
     opt.cell_tiles = ctx->cell_tiles;
     opt.plain_graphs = ctx->plain_graphs;
     opt.unfused = ctx->unfused;
+    opt.ref_order = ctx->ref_order;
     opt.max_atoms = n;
     opt.max_slots = 1;
     int64_t ncell = 1;

@@ -26,7 +26,7 @@ class GpuContext:
 
     def __init__(self, table, n_types, skin=0.3, precision="fp64", list_kind="default", shift=True,
                  fp64_fast=False, mixed_kahan=False, lanes=0, batch=0, tma=False, cluster=0, scan=0, tiles=False,
-                 plain_graphs=False, unfused=False):
+                 plain_graphs=False, unfused=False, ref_order=False):
         self._lib = _ffi.lib()
         self.n_types = int(n_types)
         pairs = (_ffi.LJPair * len(table))()
@@ -41,7 +41,7 @@ class GpuContext:
         self.n = 0
         self.precision = precision
         flags = _ffi.option_flags(fp64_fast, mixed_kahan, lanes, batch, tma, cluster, scan, tiles,
-                                  plain_graphs, unfused)
+                                  plain_graphs, unfused, ref_order)
         if list_kind != "default" or flags:
             self._check(self._lib.pis_gpu_set_options(self._h, _ffi.LIST_KIND[list_kind], flags))
 

@@ -9,8 +9,8 @@ oracle's sources or the reference's files. ``examples.json`` holds known answers
 reference's example inputs (``example/data.txt``, ``example/data_run.txt``,
 ``example/example.txt``, ``example/example2.txt``, ``example/argon4000.txt``): the parsed pair
 tables with the PairCoeffs quirk, the oracle's energy and forces on the two small files, and the
-FCC order, shell count and lattice energy of the argon files. Those inputs are read from the reference sources (``REFERENCE_DIR``, default
-``/root/reference``); the script refuses to write if they are absent or if the oracle disagrees
+FCC order, shell count and lattice energy of the argon files. Those inputs are read from the
+reference sources (the directory in ``PIS_REFERENCE_DIR``; there is no default); the script refuses to write if they are absent or if the oracle disagrees
 with a closed form, so a fixture never records an unpinned oracle.
 
 Fixture arrays (float64 unless noted):
@@ -45,7 +45,7 @@ for p in (ROOT, TESTS):
 
 from golden_data import FIXTURES, neighbour_digest, table_rows  # noqa: E402
 
-REFERENCE_DIR = os.environ.get("REFERENCE_DIR", "/root/reference")
+REFERENCE_DIR = os.environ.get("PIS_REFERENCE_DIR", "")
 
 
 def oracle_answers(sysd, dt, steps, skin):
@@ -112,7 +112,7 @@ def example_answers():
     def path(name):
         p = os.path.join(REFERENCE_DIR, "example", name)
         if not os.path.exists(p):
-            raise SystemExit(f"reference example {p} not found: set REFERENCE_DIR to the reference sources")
+            raise SystemExit(f"reference example {p} not found: set PIS_REFERENCE_DIR to the reference sources")
         return p
 
     out = {}

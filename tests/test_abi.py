@@ -107,9 +107,11 @@ def test_option_flags_match_header():
     assert _ffi.option_flags(cluster=4, lanes=4, scan=0) == (4 << 24) | (4 << 8)
     assert _ffi.option_flags(scan=4, mixed_kahan=True) == (4 << 28) | 2
     assert _ffi.STATUS_NAMES[27] == "PIS_ERR_TIMEOUT"
-    for name, value in (("PIS_OPT_TILE", 8), ("PIS_OPT_PLAIN_GRAPHS", 16), ("PIS_OPT_UNFUSED", 32)):
+    for name, value in (("PIS_OPT_TILE", 8), ("PIS_OPT_PLAIN_GRAPHS", 16), ("PIS_OPT_UNFUSED", 32),
+                        ("PIS_OPT_REF_ORDER", 64)):
         assert f"#define {name} {value}" in text
     assert _ffi.option_flags(tiles=True) == 8
+    assert _ffi.option_flags(ref_order=True) == 64
     assert _ffi.option_flags(plain_graphs=True, unfused=True) == 16 | 32
 
 

@@ -86,3 +86,41 @@ def test_cpu_sample_is_bounded(oracle_lib):
     assert v > 0 and steps >= 1 and (el >= 0.05 or steps == 500)
     v1, steps1, _ = bench.cpu_sample(pos, vel, L, 1, oracle.OFFSET, min_seconds=0.0, max_steps=3)
     assert steps1 == 1 and v1 > 0  # at least one whole step, even with no time bound
+
+
+def test_reference_arm_state_equals_gpu_arm_state(oracle_lib):
+    # the reference arm rebuilds the start state without the GPU library: lattice and velocities
+    # equal the GPU arm's bit for bit
+    import oracle
+    from pis_gb300.lattice import lj_liquid
+    pos, vel, L = lj_liquid(5, bench.RHO, bench.TSTAR, 1)
+    a = (4.0 / bench.RHO) ** (1.0 / 3.0)
+    assert np.array_equal(oracle.fcc_lattice(a, 5, 5, 5), pos)
+    assert np.array_equal(oracle.maxwell_boltzmann(np.ones(len(pos)), bench.TSTAR / oracle.KB, 1), vel)
+    assert L == a * 5
+
+
+def test_reference_arm_does_not_load_the_gpu_library(oracle_lib, tmp_path):
+    # a small reference-arm run in a fresh process: one JSON line, and libpis_gpu.so never mapped
+    import subprocess
+    import sys
+    code = ("import argparse, bench\n"
+            "a = argparse.Namespace(cells=6, equil=2, steps=1, warmup=1, gpus=1)\n"
+            "bench.run_reference(a, 0, 1)\n"
+            "print('mapped' if 'libpis_gpu' in open('/proc/self/maps').read() else 'unmapped')\n")
+    out = subprocess.run([sys.executable, "-c", code], cwd=bench.ROOT, capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.strip().splitlines()
+    rec = json.loads(lines[0])
+    assert rec["impl"] == "reference" and rec["config"]["atoms"] == 864 and rec["cpu_baseline"]["kind"] == "port"
+    assert lines[-1] == "unmapped"
+
+
+def test_roofline_bytes_follow_the_per_atom_step_count():
+    # compulsory bytes of one atom-step: 4 per list entry + 100 (position 24, velocity 48, force 24,
+    # type 4) -> about 410 B at 77.6 entries; flops 23 per entry + 3 per in-cutoff pair -> ~1,950
+    assert bench.ALG_BYTES_PER_ATOM + 4 * 77.6 == pytest.approx(410.4)
+    assert 77.6 * bench.FLOPS_PER_CANDIDATE + 55.3 * bench.FLOPS_PER_PAIR_ENERGY == pytest.approx(1950.7, abs=1)
+    f = bench.pipe_fraction(2e12, 100.0, 40.0)
+    assert f["achieved"] == pytest.approx(20.0) and f["frac"] == pytest.approx(0.5)
+    assert bench.pipe_fraction(1.0, 0.0, 40.0) is None

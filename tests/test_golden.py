@@ -99,7 +99,7 @@ def test_examples_match_reference_files(oracle_lib, name):
     import hashlib
     import oracle
     path = os.path.join(REFERENCE, "example", name)
-    if not os.path.exists(path):
+    if not REFERENCE or not os.path.exists(path):
         pytest.skip("reference sources not mounted")
     ex = examples()[name]
     with open(path, "rb") as f:

@@ -333,7 +333,7 @@ def test_reference_example_input(pio, monkeypatch):
     # test_command.sh does): every command it uses parses, and contextualize builds its state
     import os
     from conftest import REFERENCE
-    if not os.path.exists(os.path.join(REFERENCE, "example", "input.pis")):
+    if not REFERENCE or not os.path.exists(os.path.join(REFERENCE, "example", "input.pis")):
         pytest.skip("reference sources not mounted")
     monkeypatch.chdir(REFERENCE)
     s = pio.System("example/input.pis")
@@ -353,7 +353,7 @@ def test_pair_style_supplies_the_table_a_data_file_lacks(pio, tmp_path):
     from golden_data import examples
     from pis_gb300.lattice import fcc_lattice
     data = os.path.join(REFERENCE, "example", "example2.txt")
-    if not os.path.exists(data):
+    if not REFERENCE or not os.path.exists(data):
         pytest.skip("reference sources not mounted")
     ex = examples()["example2.txt"]
     s = _open(pio, tmp_path, f"read_data {data}\npair_style lj/cut 8.5\npair_coeff 1 1 0.238 3.405\n")
