@@ -131,6 +131,15 @@ pis_status pis_gpu_create(const pis_lj_pair* table, int32_t n_pairs, int32_t n_t
  * next set_state. */
 pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flags);
 
+/* Neighbour-list capacity (no counterpart in the reference, which rebuilds its cells at every
+ * evaluation and keeps no list): per_atom entries per atom (0, the default, sizes it from the mean
+ * density: 1.6 x the expected count + 32). With auto_grow = 1 (the default) an evaluation or a run
+ * of steps whose list outgrows the capacity is repeated from its own start with a larger list (the
+ * state before it is kept on the device), so the results are those of a run that never overflowed;
+ * with auto_grow = 0 it returns PIS_ERR_LIST_OVERFLOW and its results are invalid. per_atom takes
+ * effect at the next set_state, auto_grow at once. */
+pis_status pis_gpu_set_list_capacity(pis_gpu_ctx* ctx, int32_t per_atom, int32_t auto_grow);
+
 /* Upload the Atoms state (src/atoms/new.rs:9-17). force may be NULL (zero forces, as the
  * data-file reader leaves them, src/readers/input_file/commands.rs:367). The only
  * AoS <-> device-layout transpose happens here and in pis_gpu_get_state. */
@@ -147,6 +156,15 @@ pis_status pis_gpu_compute_potential(pis_gpu_ctx* ctx, double* pe_out, double* f
  * pe_out, if non-NULL, receives the potential energy each step returns (n_steps values).
  * The state stays on the device; chunks of steps run as captured CUDA graphs. */
 pis_status pis_gpu_verlet_step_nve(pis_gpu_ctx* ctx, double dt, int64_t n_steps, double* pe_out);
+
+/* pis_gpu_verlet_step_nve with the thermo of every step kept on the device and read back once per
+ * run (Simulation::output prints PE, KE, H, T and P after each step, src/simulation.rs:66-88):
+ * ke_out receives Atoms::kinetic_energy (src/atoms/properties.rs:17-24) after each step and
+ * virial_trace_out the trace of Atoms::virial_tensor (:49-51), sum_i r_i . F_i, which with KE gives
+ * the pressure (:61-65). Any output may be NULL; the trace costs one more block sum per step and is
+ * only formed when virial_trace_out is given. */
+pis_status pis_gpu_verlet_step_nve_thermo(pis_gpu_ctx* ctx, double dt, int64_t n_steps, double* pe_out,
+                                          double* ke_out, double* virial_trace_out);
 
 /* Download positions / velocities / forces (3 x N each, any may be NULL). */
 pis_status pis_gpu_get_state(pis_gpu_ctx* ctx, double* pos, double* vel, double* force);
@@ -191,15 +209,21 @@ pis_status pis_gpu_probe_peaks(double* fp32_tflops, double* fp64_tflops);
 /* Force evaluation that allocates no device memory (no counterpart in the reference). For callers
  * that cannot allocate device memory while running - a host whose framework owns the whole device
  * memory pool, or a real-time loop where cudaMalloc's latency and implicit synchronisation are not
- * allowed. Same result as pis_gpu_compute_potential (FP64, reference arithmetic) on buffers the
- * caller owns: d_type_ids (n, 1-based), d_pos (3 x n) are device inputs; d_forces (3 x n) and d_pe
- * (1 value) are device outputs; table and h_colmajor are host arrays; stream is a cudaStream_t
- * (NULL = default stream) and the call returns once the work is enqueued on it.
+ * allowed. Same result as pis_gpu_compute_potential (FP64, reference arithmetic, the energy as the
+ * same exact sum) on buffers the caller owns: d_type_ids (n, 1-based), d_pos (3 x n) are device
+ * inputs; d_forces (3 x n) and d_pe (1 value) are device outputs; table and h_colmajor are host
+ * arrays; stream is a cudaStream_t (NULL = default stream) and the call returns once the work is
+ * enqueued on it. Type ids must lie in [1, n_types]: the device cannot report a bad one through the
+ * return value, so an atom with an id outside that range gets zero force, its pairs are skipped and
+ * *d_pe is NaN.
  * Limits of the fixed scratch: n <= 262144 atoms, at most 65536 cells at the largest cutoff, at
  * least 3 cells per axis, at most 4 atom types; larger inputs return PIS_ERR_INVALID_ARGUMENT
  * (PIS_ERR_BOX_TOO_SMALL below 3 cells). The scratch is one device array shared by every call on
  * a device: calls that overlap on the GPU race and must be serialised by the caller. The first
- * call on a device looks up the scratch address; make it before any stream capture. */
+ * call on a device looks up the scratch address in the device's primary context and keeps it for
+ * the life of that context (calls after cudaDeviceReset are not supported); make the first call
+ * before any stream capture. A launch error already pending from the caller's earlier work is
+ * neither reported nor cleared. */
 pis_status pis_gpu_compute_potential_noalloc(const pis_lj_pair* table, int32_t n_pairs, int32_t n_types, int64_t n,
                                              const int32_t* d_type_ids, const double* d_pos,
                                              const double* h_colmajor, double* d_forces, double* d_pe,

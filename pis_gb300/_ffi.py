@@ -82,10 +82,12 @@ _DP = C.POINTER(C.c_double)
 SIGNATURES = [
     ("pis_gpu_create", C.c_int, [C.POINTER(LJPair), C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(_VP)]),
     ("pis_gpu_set_options", C.c_int, [_VP, C.c_int32, C.c_int32]),
+    ("pis_gpu_set_list_capacity", C.c_int, [_VP, C.c_int32, C.c_int32]),
     ("pis_gpu_set_state", C.c_int, [_VP, C.c_int64, C.POINTER(C.c_int32), _DP, _DP, _DP, _DP, _DP,
                                     C.POINTER(C.c_uint8)]),
     ("pis_gpu_compute_potential", C.c_int, [_VP, _DP, _DP]),
     ("pis_gpu_verlet_step_nve", C.c_int, [_VP, C.c_double, C.c_int64, _DP]),
+    ("pis_gpu_verlet_step_nve_thermo", C.c_int, [_VP, C.c_double, C.c_int64, _DP, _DP, _DP]),
     ("pis_gpu_get_state", C.c_int, [_VP, _DP, _DP, _DP]),
     ("pis_gpu_reductions", C.c_int, [_VP, _DP, _DP]),
     ("pis_gpu_neighbour_list", C.c_int, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int64,

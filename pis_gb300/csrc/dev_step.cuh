@@ -462,7 +462,10 @@ __device__ __forceinline__ void k_build_body(const DP& P, int blk, int step_mode
         }
     }
     if (gl == 0) {
-        if (cnt > cap) atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
+        if (cnt > cap) {
+            atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
+            atomicMax(&st.need_nn, cnt);
+        }
         P.nn[i] = cnt > cap ? cap : cnt;
     }
 }
@@ -545,7 +548,10 @@ __device__ __forceinline__ void build1_chunk(const DP& P, int blk, int step_mode
             }
         }
     }
-    if (cnt > cap) atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
+    if (cnt > cap) {
+        atomicOr(&st.flags, FLAG_LIST_OVERFLOW);
+        atomicMax(&st.need_nn, cnt);
+    }
     P.nn[i] = cnt > cap ? cap : cnt;
 }
 // only_two_cell: just the slots with a two-cell axis (the two-stage build covers the others).

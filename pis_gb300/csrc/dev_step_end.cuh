@@ -33,6 +33,12 @@ __device__ __forceinline__ double twice_ke_mixed(const double4_32a& v) {
     return __dmul_rn(v.w, fma(v.x, v.x, fma(v.y, v.y, __dmul_rn(v.z, v.z))));
 }
 
+// r_i . F_i, the atom's share of the virial trace (the pressure of Atoms::pressure,
+// src/atoms/properties.rs:61-65, needs only tr W)
+__device__ __forceinline__ double virial_trace(const double4_32a& p, const double4_32a& f) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(p.x, f.x), __dmul_rn(p.y, f.y)), __dmul_rn(p.z, f.z));
+}
+
 template <bool UPDATE, bool EXACT>
 __global__ void k_integrate2(const DP P, int respect_steps) {
     __shared__ double sh[32];
@@ -73,14 +79,20 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
         // m |v|^2 here and the factor 1/2 on the block sum: halving is exact, so this equals the
         // sum of (0.5 m) |v|^2 (properties.rs:17-24) bit for bit
         ke = EXACT ? __dmul_rn(m, norm2_ref(v.x, v.y, v.z)) : twice_ke_mixed(v);
-        if (st.want_virial) p = P.pos[cur][i];
+        if (st.want_virial || st.thermo) p = P.pos[cur][i];
     }
+    const bool trace = UPDATE && st.thermo;
     if (EXACT) {
         // FP64 path: exact sums of m |v|^2 (halved at the step end) and of r_i[a] F_i[b]
         XAcc x;
         xacc_zero(x);
         if (live) xacc_add(x, ke);
         xacc_block_store<256>(x, P.xke_part + (int64_t)blockIdx.x * XS_WORDS, shx);
+        if (trace) {
+            xacc_zero(x);
+            if (live) xacc_add(x, virial_trace(p, f));
+            xacc_block_store<256>(x, P.xtr_part + (int64_t)blockIdx.x * XS_WORDS, shx);
+        }
         if (st.want_virial) {
             const double r[3] = {p.x, p.y, p.z}, g[3] = {f.x, f.y, f.z};
             for (int a = 0; a < 3; ++a)
@@ -94,6 +106,10 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
     }
     double tot = block_sum<256>(ke, sh);
     if (threadIdx.x == 0) P.ke_part[blockIdx.x] = 0.5 * tot;
+    if (trace) {
+        const double t = block_sum<256>(live ? virial_trace(p, f) : 0.0, sh);
+        if (threadIdx.x == 0) P.tr_part[blockIdx.x] = t;
+    }
     if (st.want_virial) {
         double r[3] = {p.x, p.y, p.z}, g[3] = {f.x, f.y, f.z};
 #pragma unroll
@@ -150,11 +166,16 @@ __global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixe
         mixed_atom_forces<ACC, 1, ONE, MIX_BATCH, step_list_prefetch<MIX_BATCH>(), FUSED_LQ>(P, sp, i, 0, shift, acc);
     const bool drift = DRIFT && st.steps_left > 1;
     const bool want_virial = st.want_virial != 0;
+    const bool want_trace = st.thermo != 0;
     double ke = 0.0;
     double4_32a p = make_double4_32a(0.0, 0.0, 0.0, 0.0), f = p;
     if (live) {
         f = make_double4_32a(acc.fx, acc.fy, acc.fz, 0.0);
-        P.frc[i] = f;
+        // The forces themselves are only read by the host (downloads happen between graphs) and by
+        // the unfused kick, never inside a fused run: a = F/m carries them to the next step. So they
+        // are stored only in a step that does not drift - the last step of every graph and of every
+        // slot's run - which saves a 32-byte store per atom on the other steps.
+        if (!drift) P.frc[i] = f;
         const int cur = st.cur;
         double4_32a v = P.vel[cur][i];
         const double4_32a a = P.acc[cur][i];
@@ -164,7 +185,7 @@ __global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixe
         P.vel[cur][i] = v;
         P.acc[cur][i] = make_double4_32a(bx, by, bz, a.w);
         ke = twice_ke_mixed(v);
-        if (want_virial || drift) p = P.pos[cur][i];
+        if (want_virial || want_trace || drift) p = P.pos[cur][i];
         if (drift) {
             double x, y, z;
             drift_mixed(sp, p, v, bx, by, bz, x, y, z);
@@ -178,6 +199,10 @@ __global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixe
     if (threadIdx.x == 0) P.pe_part[blockIdx.x] = pe_tot;
     const double ke_tot = block_sum<256>(ke, sh);
     if (threadIdx.x == 0) P.ke_part[blockIdx.x] = 0.5 * ke_tot;
+    if (want_trace) {
+        const double t = block_sum<256>(live ? virial_trace(p, f) : 0.0, sh);
+        if (threadIdx.x == 0) P.tr_part[blockIdx.x] = t;
+    }
     if (want_virial) {
         double r[3] = {p.x, p.y, p.z}, g[3] = {f.x, f.y, f.z};
 #pragma unroll
@@ -234,6 +259,8 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
         if (vir)
             for (int q = 0; q < 9; ++q)
                 w[q] = xacc_slot_value(P.xvir_part + (int64_t)q * XS_WORDS, sp.ch0, sp.nch, 9 * XS_WORDS, shx);
+        double tr = 0.0;
+        if (mode == 0 && st.thermo) tr = xacc_slot_value(P.xtr_part, sp.ch0, sp.nch, XS_WORDS, shx);
         if (threadIdx.x == 0) {
             if (mode != 2) {
                 if (P.full_list) pe *= 0.5;
@@ -248,7 +275,10 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
                 st.want_virial = 0;
             }
             if (mode == 0) {
-                P.pe_hist[(int64_t)s * P.hist + (st.steps_done % P.hist)] = pe;
+                const int64_t h = (int64_t)s * P.hist + (st.steps_done % P.hist);
+                P.pe_hist[h] = pe;
+                P.ke_hist[h] = ke;
+                if (st.thermo) P.tr_hist[h] = tr;
                 st.steps_done += 1;
                 st.steps_left -= 1;
             }
@@ -276,6 +306,11 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
             w[q] = block_sum<END_THREADS>(a, sh);
         }
     }
+    double tr = 0.0;
+    if (mode == 0 && st.thermo) {
+        for (int c = threadIdx.x; c < sp.nch; c += END_THREADS) tr += P.tr_part[sp.ch0 + c];
+        tr = block_sum<END_THREADS>(tr, sh);
+    }
     if (threadIdx.x == 0) {
         if (mode != 2) {
             if (P.full_list) pe *= 0.5;
@@ -290,7 +325,10 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
             st.want_virial = 0;
         }
         if (mode == 0) {
-            P.pe_hist[(int64_t)s * P.hist + (st.steps_done % P.hist)] = pe;
+            const int64_t h = (int64_t)s * P.hist + (st.steps_done % P.hist);
+            P.pe_hist[h] = pe;
+            P.ke_hist[h] = ke;
+            if (st.thermo) P.tr_hist[h] = tr;
             st.steps_done += 1;
             st.steps_left -= 1;
         }

@@ -66,6 +66,8 @@ Engine::~Engine() {
         for (auto e : kv.second.ev) cudaEventDestroy(e);
     }
     if (d_ && d_->keep) cudaFree(d_->keep);
+    if (nbr_own_) cudaFree(nbr_own_);
+    if (save_) cudaFree(save_);
     if (mem_) cudaFree(mem_);
     if (stream_) cudaStreamDestroy(stream_);
     if (side_) cudaStreamDestroy(side_);
@@ -217,6 +219,8 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         {(void**)&d_->st, sizeof(SysState) * NS}, {(void**)&d_->tab, sizeof(LJDev) * (size_t)opt.max_types_total},
         {(void**)&d_->pe_part, 8 * std::max(NCH * 32, NCC * 4)}, {(void**)&d_->ke_part, 8 * NCH},
         {(void**)&d_->vir_part, 72 * NCH}, {(void**)&d_->pe_hist, 8 * NS * (size_t)opt.hist},
+        {(void**)&d_->ke_hist, 8 * NS * (size_t)opt.hist}, {(void**)&d_->tr_hist, 8 * NS * (size_t)opt.hist},
+        {(void**)&d_->tr_part, 8 * NCH},
         {(void**)&d_->ctl, 256},
     };
     if (fused_) items.push_back({&prel_buf_[1], 16 * NA});
@@ -225,6 +229,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         items.push_back({(void**)&d_->xpe_part, 8 * XS_WORDS * NCH * 32});
         items.push_back({(void**)&d_->xke_part, 8 * XS_WORDS * NCH});
         items.push_back({(void**)&d_->xvir_part, 8 * XS_WORDS * 9 * NCH});
+        items.push_back({(void**)&d_->xtr_part, 8 * XS_WORDS * NCH});
     }
     if (clm_) {
         items.push_back({(void**)&d_->cl_atom, 4 * NCL});
@@ -275,6 +280,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     }
     hp_.assign(NS, SysParams{});
     slot_rlist_.assign(NS, 0.0);
+    slot_rcmax_.assign(NS, 0.0);
     free_atoms_.clear();
     free_cells_.clear();
     free_atoms_[0] = NA;
@@ -324,6 +330,23 @@ static void cell_grid(const SlotDesc& d, double rlist, int nc[3]) {
         double q = std::floor(L / rlist);
         nc[a] = q < 1.0 ? 1 : (q > 2000.0 ? 2000 : (int)q);
     }
+}
+
+// The reference's own cell grid at the largest cutoff (Atoms::divide_into_cells,
+// src/atoms/neighbour_list.rs:45-57: floor(|h column| / rcut), at least 1), for the reference-order
+// forces. h is row-major.
+static void reference_cells(const double* h, double rc_max, int32_t rnc[3]) {
+    for (int a = 0; a < 3; ++a) {
+        const double col[3] = {h[a], h[3 + a], h[6 + a]};
+        const double len = std::sqrt(col[0] * col[0] + col[1] * col[1] + col[2] * col[2]);
+        const double q = std::floor(len / rc_max);
+        rnc[a] = q < 1.0 ? 1 : (q > 1e9 ? 1000000000 : (int)q);
+    }
+}
+// The reference-order keys need at least 3 cells per axis and fewer than 2^25 cells.
+static bool reference_cells_ok(const int32_t rnc[3]) {
+    const double cells = (double)rnc[0] * rnc[1] * rnc[2];
+    return rnc[0] >= 3 && rnc[1] >= 3 && rnc[2] >= 3 && cells < 33554432.0;
 }
 
 static double slot_rlist(const SlotDesc& d) {
@@ -534,15 +557,9 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     double rc_max = 0.0;  // PairPotentialManager::max_rcut (src/potentials/potential.rs:170-179)
     for (auto& e : d.table)
         if (e.present && rc_max < e.rcut) rc_max = e.rcut;
-    for (int a = 0; a < 3; ++a) {
-        const double col[3] = {d.h[a], d.h[3 + a], d.h[6 + a]};
-        const double len = std::sqrt(col[0] * col[0] + col[1] * col[1] + col[2] * col[2]);
-        const double q = std::floor(len / rc_max);
-        p.rnc[a] = q < 1.0 ? 1 : (q > 1e9 ? 1000000000 : (int)q);
-    }
+    reference_cells(d.h, rc_max, p.rnc);
     if (opt_.ref_order) {
-        const double cells = (double)p.rnc[0] * p.rnc[1] * p.rnc[2];
-        if (p.rnc[0] < 3 || p.rnc[1] < 3 || p.rnc[2] < 3 || cells >= 33554432.0) {
+        if (!reference_cells_ok(p.rnc)) {
             give_range(free_atoms_, a0, d.n);
             give_range(free_cells_, c0, ncell + 1);
             for (int k = 0; k < nt * nt; ++k) free_tab_[tab0 + k] = 1;
@@ -559,6 +576,7 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     p.cch0 = 0;  // assigned by the block map
     hp_[slot] = p;
     slot_rlist_[slot] = rlist;
+    slot_rcmax_[slot] = rc_max;
 
     // atom state: the caller's x,y,z-per-atom arrays and types go to the device as they are, and
     // k_load_slot builds the device layout
@@ -1303,6 +1321,36 @@ pis_status Engine::read_states(std::vector<SysState>& out, std::string& err) {
     return sync(err);
 }
 
+pis_status Engine::set_thermo(int slot, bool on, std::string& err) {
+    const int32_t v = on ? 1 : 0;
+    pis_status st = check(cudaMemcpyAsync(&d_->st[slot].thermo, &v, 4, cudaMemcpyHostToDevice, stream_), "thermo", err);
+    if (st) return st;
+    return sync(err);
+}
+
+pis_status Engine::read_history(int slot, int64_t n, double* pe, double* ke, double* trace, std::string& err) {
+    SysState ss;
+    pis_status st = read_state(slot, ss, err);
+    if (st) return st;
+    if (n > opt_.hist || n > ss.steps_done) {
+        err = "history holds fewer steps than requested";
+        return PIS_ERR_INVALID_ARGUMENT;
+    }
+    double* outs[3] = {pe, ke, trace};
+    double* rings[3] = {d_->pe_hist, d_->ke_hist, d_->tr_hist};
+    std::vector<double> ring(opt_.hist);
+    for (int r = 0; r < 3; ++r) {
+        if (!outs[r]) continue;
+        st = check(cudaMemcpyAsync(ring.data(), rings[r] + (int64_t)slot * opt_.hist, 8 * opt_.hist,
+                                   cudaMemcpyDeviceToHost, stream_), "history", err);
+        if (st) return st;
+        st = sync(err);
+        if (st) return st;
+        for (int64_t q = 0; q < n; ++q) outs[r][q] = ring[(ss.steps_done - n + q) % opt_.hist];
+    }
+    return PIS_OK;
+}
+
 pis_status Engine::read_pe_history(int slot, int64_t n, double* out, std::string& err) {
     SysState ss;
     pis_status st = read_state(slot, ss, err);
@@ -1462,6 +1510,111 @@ pis_status Engine::neighbour_sets_cluster(int slot, const SysState& ss, std::vec
     return PIS_OK;
 }
 
+// Checkpoint of one slot: its current positions, velocities, accelerations, forces and original
+// indices (device order) and its SysState. Restoring writes them back into the buffer set they came
+// from and asks for a list rebuild, so the next step starts exactly from the saved state.
+pis_status Engine::save_state(int slot, std::string& err) {
+    const SysParams& p = hp_[slot];
+    const size_t NA = (size_t)opt_.max_atoms;
+    if (!save_) {
+        pis_status st = check(cudaMalloc(&save_, (4 * 32 + 4) * NA), "checkpoint allocation", err);
+        if (st) return st;
+    }
+    pis_status st = read_state(slot, save_state_, err);
+    if (st) return st;
+    const int cur = save_state_.cur;
+    char* b = (char*)save_;
+    const size_t n32 = 32 * (size_t)p.n, a32 = 32 * (size_t)p.a0;
+    const void* src[4] = {d_->pos[cur], d_->vel[cur], d_->acc[cur], d_->frc};
+    for (int k = 0; k < 4; ++k) {
+        st = check(cudaMemcpyAsync(b + 32 * NA * k, (const char*)src[k] + a32, n32, cudaMemcpyDeviceToDevice, stream_),
+                   "checkpoint", err);
+        if (st) return st;
+    }
+    st = check(cudaMemcpyAsync(b + 128 * NA, d_->id[cur] + p.a0, 4 * (size_t)p.n, cudaMemcpyDeviceToDevice, stream_),
+               "checkpoint", err);
+    if (st) return st;
+    save_slot_ = slot;
+    return PIS_OK;
+}
+
+pis_status Engine::restore_state(int slot, std::string& err) {
+    if (save_slot_ != slot || !save_) {
+        err = "no checkpoint of this slot";
+        return PIS_ERR_STATE;
+    }
+    const SysParams& p = hp_[slot];
+    const size_t NA = (size_t)opt_.max_atoms;
+    SysState ss = save_state_;
+    const int cur = ss.cur;
+    const char* b = (const char*)save_;
+    const size_t n32 = 32 * (size_t)p.n, a32 = 32 * (size_t)p.a0;
+    void* dst[4] = {d_->pos[cur], d_->vel[cur], d_->acc[cur], d_->frc};
+    pis_status st = PIS_OK;
+    for (int k = 0; k < 4; ++k) {
+        st = check(cudaMemcpyAsync((char*)dst[k] + a32, b + 32 * NA * k, n32, cudaMemcpyDeviceToDevice, stream_),
+                   "restore", err);
+        if (st) return st;
+    }
+    st = check(cudaMemcpyAsync(d_->id[cur] + p.a0, b + 128 * NA, 4 * (size_t)p.n, cudaMemcpyDeviceToDevice, stream_),
+               "restore", err);
+    if (st) return st;
+    ss.rebuild = 1;
+    ss.flags = 0;
+    ss.need_nn = 0;
+    st = check(cudaMemcpyAsync(d_->st + slot, &ss, sizeof(ss), cudaMemcpyHostToDevice, stream_), "restore", err);
+    if (st) return st;
+    return sync(err);
+}
+
+// A larger per-atom list: entry k of atom i sits at (k / lq) * npad * lq + i * lq + k % lq whatever
+// the capacity, so the grown array only adds rows of groups; graphs captured with the old pointer
+// and capacity are dropped.
+pis_status Engine::grow_list(int64_t new_cap, std::string& err) {
+    if (opt_.cluster) {
+        err = "the cluster-list variant does not grow its list";
+        return PIS_ERR_UNSUPPORTED;
+    }
+    new_cap = (new_cap + 31) / 32 * 32;
+    if (new_cap <= cap_) return PIS_OK;
+    if ((double)npad_ * (double)new_cap >= 4294967296.0) {
+        err = "neighbour list of the pool would exceed 2^32 entries (atoms x capacity)";
+        return PIS_ERR_NO_MEMORY;
+    }
+    void* p = nullptr;
+    pis_status st = check(cudaMalloc(&p, 4 * (size_t)npad_ * (size_t)new_cap), "list allocation", err);
+    if (st) return st;
+    st = sync(err);
+    if (st) {
+        cudaFree(p);
+        return st;
+    }
+    if (nbr_own_) cudaFree(nbr_own_);
+    nbr_own_ = p;
+    d_->nbr = (uint32_t*)p;
+    if (d_->keep) {  // the export mask is sized by the capacity: reallocated on next use
+        cudaFree(d_->keep);
+        d_->keep = nullptr;
+    }
+    d_->cap = (int32_t)new_cap;
+    cap_ = new_cap;
+    for (auto& kv : graphs_) {
+        cudaGraphExecDestroy(kv.second.exec);
+        for (auto e : kv.second.ev) cudaEventDestroy(e);
+    }
+    graphs_.clear();
+    // every slot's list is rebuilt at its next step or evaluation
+    std::vector<SysState> all;
+    st = read_states(all, err);
+    if (st) return st;
+    for (int s = 0; s < opt_.max_slots; ++s)
+        if (hp_[s].active) all[s].rebuild = 1;
+    st = check(cudaMemcpyAsync(d_->st, all.data(), sizeof(SysState) * all.size(), cudaMemcpyHostToDevice, stream_),
+               "list growth", err);
+    if (st) return st;
+    return sync(err);
+}
+
 pis_status Engine::scale_velocities(int slot, const double* m, std::string& err) {
     LAUNCH(k_scale_vel, (unsigned)max_chunks_, opt_.blk, *d_, slot, m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8]);
     pis_status st = check(cudaGetLastError(), "scale velocities", err);
@@ -1476,7 +1629,8 @@ pis_status Engine::scale_box(int slot, const double* m, std::string& err) {
                 err = "box scaling must keep the box orthorhombic (diagonal matrix)";
                 return PIS_ERR_UNSUPPORTED;
             }
-    SysParams& p = hp_[slot];
+    SysParams p = hp_[slot];
+    const double oh[3] = {p.hinv[0], p.hinv[1], p.hinv[2]};
     double nh[3] = {m[0] * p.h[0], m[4] * p.h[1], m[8] * p.h[2]};
     double rl = slot_rlist_[slot];
     for (int a = 0; a < 3; ++a)
@@ -1484,12 +1638,9 @@ pis_status Engine::scale_box(int slot, const double* m, std::string& err) {
             err = "scaled box is shorter than 2 (rcut + skin)";
             return PIS_ERR_BOX_TOO_SMALL;
         }
-    LAUNCH(k_scale_pos, (unsigned)max_chunks_, opt_.blk, *d_, slot, p.hinv[0], p.hinv[1], p.hinv[2], nh[0], nh[1], nh[2]);
     // new h and h^-1; the cell grid keeps its counts, the cell edge follows the box
     for (int a = 0; a < 3; ++a) {
         p.h[a] = nh[a];
-        int ncnew = (int)std::floor(nh[a] / rl);
-        (void)ncnew;
         p.cs[a] = nh[a] / p.nc[a];
         p.fcs[a] = (float)p.cs[a];
         p.fsub[a] = (float)(4.0 / p.cs[a]);
@@ -1502,11 +1653,22 @@ pis_status Engine::scale_box(int slot, const double* m, std::string& err) {
             err = "box shrank below the cell size; re-create the state to re-grid";
             return PIS_ERR_UNSUPPORTED;
         }
+    {
+        const double hm[9] = {p.h[0], 0.0, 0.0, 0.0, p.h[1], 0.0, 0.0, 0.0, p.h[2]};
+        reference_cells(hm, slot_rcmax_[slot], p.rnc);
+        if (opt_.ref_order && !reference_cells_ok(p.rnc)) {
+            err = "reference-order forces need at least 3 cells of the largest cutoff per axis";
+            return PIS_ERR_UNSUPPORTED;
+        }
+    }
     // the 27-cell walk's two-cell condition (add_slot) for the new edges
     p.walk27 = 1;
     for (int a = 0; a < 3; ++a)
         if (p.nc[a] < 2 || (p.nc[a] == 2 && !(p.h[a] > 2.0 * std::sqrt((double)p.frlist2) * (1.0 + 1e-5)))) p.walk27 = 0;
-    pis_status st = check(cudaMemcpyAsync(d_->sp + slot, &p, sizeof(SysParams), cudaMemcpyHostToDevice, stream_), "params", err);
+    LAUNCH(k_scale_pos, (unsigned)max_chunks_, opt_.blk, *d_, slot, oh[0], oh[1], oh[2], nh[0], nh[1], nh[2]);
+    hp_[slot] = p;
+    pis_status st = check(cudaMemcpyAsync(d_->sp + slot, &hp_[slot], sizeof(SysParams), cudaMemcpyHostToDevice, stream_),
+                          "params", err);
     if (st) return st;
     int32_t one = 1;
     st = check(cudaMemcpyAsync(&d_->st[slot].rebuild, &one, 4, cudaMemcpyHostToDevice, stream_), "params", err);

@@ -79,6 +79,8 @@ struct SysState {
     int32_t want_virial;  // compute sum_i r_i F_i^T in the next reductions
     int32_t eval;         // slot takes part in the next host-requested evaluation / reduction
     int32_t ncl;          // clusters of the current build (cluster-list path)
+    int32_t need_nn;      // longest per-atom list a build asked for (more than the capacity on overflow)
+    int32_t thermo;       // steps also record KE and the virial trace sum_i r_i . F_i in history rings
     int64_t steps_left;   // steps still to take; a slot at 0 is frozen during run()
     int64_t steps_done;
     int64_t rebuilds;
@@ -153,9 +155,20 @@ class Engine {
     pis_status read_states(std::vector<SysState>& st, std::string& err);
     // Last n energies of the slot's history ring (oldest first).
     pis_status read_pe_history(int slot, int64_t n, double* out, std::string& err);
+    // Last n steps' potential energy, kinetic energy and virial trace (the latter two recorded while
+    // the slot's thermo flag is set); any output may be null.
+    pis_status read_history(int slot, int64_t n, double* pe, double* ke, double* trace, std::string& err);
+    pis_status set_thermo(int slot, bool on, std::string& err);
     pis_status neighbour_sets(int slot, std::vector<int64_t>& offsets, std::vector<int32_t>& idx,
                               std::string& err);
     pis_status list_entries(int slot, int64_t& total, std::string& err);
+    // List-overflow recovery: keep a device copy of one slot's state, put it back (the list is
+    // rebuilt at the next step), and enlarge the per-atom list capacity (the list layout does not
+    // depend on the capacity, so only its allocation grows; captured graphs are dropped).
+    pis_status save_state(int slot, std::string& err);
+    pis_status restore_state(int slot, std::string& err);
+    pis_status grow_list(int64_t new_cap, std::string& err);
+    bool per_atom_list() const { return !opt_.cluster; }
     pis_status scale_velocities(int slot, const double* m, std::string& err);
     pis_status scale_box(int slot, const double* m, std::string& err);
     const SysParams& params(int slot) const { return hp_[slot]; }
@@ -215,6 +228,7 @@ class Engine {
     std::vector<SysParams> hp_;
     std::vector<int> slot_tab_size_;
     std::vector<double> slot_rlist_;
+    std::vector<double> slot_rcmax_;  // largest cutoff of each slot's pair table
     // free-space bookkeeping (first fit over atom and cell index ranges)
     std::map<int64_t, int64_t> free_atoms_, free_cells_, free_clusters_;
     std::vector<int> free_tab_;
@@ -238,6 +252,10 @@ class Engine {
     bool fused_ = false;       // mixed steps run the fused force + kick + drift kernel
     bool list_groups_ = false; // the per-atom list is stored in groups of consecutive entries
     void* prel_buf_[2] = {nullptr, nullptr};  // the two cell-relative coordinate buffers (fused steps)
+    void* nbr_own_ = nullptr;   // a grown neighbour list (allocated apart from the pool)
+    void* save_ = nullptr;      // checkpoint of one slot's per-atom arrays (allocated on first use)
+    int save_slot_ = -1;
+    SysState save_state_{};
 };
 
 }  // namespace pis

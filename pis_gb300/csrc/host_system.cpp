@@ -12,6 +12,7 @@
 #include <fstream>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "host_io.h"
@@ -430,6 +431,45 @@ pis_status pis_system_run(pis_system* s, const char* thermo_path) {
     Nhc nhc;
     if (ens == 1) nhc.init(s->nhc.t_start, s->nhc.t_end, s->nhc.tau);
     const double dt = s->timestep;
+    if (ens == 0) {
+        // NVE: runs of up to 1000 steps (or up to the next dump) with every step's PE, KE and virial
+        // trace kept on the device and read back once per run; each dump's positions are
+        // downloaded at its step and written by a worker thread while the GPU runs on.
+        const int64_t run_max = 1000;
+        std::vector<double> pe_k(run_max), ke_k(run_max), tr_k(run_max);
+        std::vector<double> dump_pos[2] = {std::vector<double>(3 * n), std::vector<double>(3 * n)};
+        std::thread writer;
+        int buf = 0;
+        for (int64_t i = 0; i < s->steps;) {
+            int64_t k = std::min(run_max, s->steps - i);
+            if (s->dump_step > 0) k = std::min(k, s->dump_step - (i % s->dump_step));
+            st = pis_gpu_verlet_step_nve_thermo(s->ctx, dt, k, pe_k.data(), ke_k.data(), tr_k.data());
+            if (st) {
+                if (writer.joinable()) writer.join();
+                return sfail(s, st, pis_gpu_last_error(s->ctx));
+            }
+            if (s->dump_step > 0 && ((i + k) % s->dump_step) == 0) {
+                if (writer.joinable()) writer.join();  // the buffer written two dumps ago is free again
+                st = pis_gpu_get_state(s->ctx, dump_pos[buf].data(), nullptr, nullptr);
+                if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
+                const double* pp = dump_pos[buf].data();
+                const int64_t step = i + k;
+                writer = std::thread([&dump, step, n, &d, pp, h] { write_dump(dump, step, n, d.type_ids.data(), pp, h); });
+                buf ^= 1;
+            }
+            for (int64_t q = 0; q < k; ++q) {
+                const double ke = ke_k[q];
+                const double temp = (2.0 * ke) / ((double)(3 * n) * KB);
+                const double press = (2.0 * ke + tr_k[q]) / (3.0 * vol);
+                std::fprintf(th, "%lld %.3f %.3f %.3f %.3f %.3f\n", (long long)(i + q + 1), pe_k[q], ke, pe_k[q] + ke, temp,
+                             press);
+            }
+            i += k;
+        }
+        if (writer.joinable()) writer.join();
+        std::fflush(th);
+        return dump.good() ? PIS_OK : sfail(s, PIS_ERR_IO, "Failed to write trajectory file");
+    }
     for (int64_t i = 0; i < s->steps; ++i) {
         double ke = 0.0, w[9];
         if (ens == 1) {

@@ -12,7 +12,11 @@
 // built at the largest cutoff every call (as LJVOffsetManager does, src/potentials/
 // lennard_jones.rs:186-244), every atom walks its 27 neighbour cells and sums F_i -= f over all
 // j != i with the reference's FP64 pair arithmetic (src/potentials/lennard_jones.rs:33-55,
-// src/simulation_box.rs:17-27), and PE is half the sum of the per-atom energies.
+// src/simulation_box.rs:17-27), and PE is half the exact sum of the pair energies (the FP64 path's
+// order-independent sum, so it equals pis_gpu_compute_potential's energy bit for bit).
+// Type ids outside [1, n_types] cannot be reported by the call, which returns once the work is
+// enqueued: the kernels skip every pair of such an atom (its force is zero) and write NaN as the
+// energy, so the caller sees the fault in its output.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -20,6 +24,10 @@
 #include <mutex>
 
 #include "pis_gpu.h"
+#include "xsum.cuh"
+
+using pis::XAcc;
+using pis::XS_WORDS;
 
 namespace {
 
@@ -37,7 +45,8 @@ constexpr size_t NA_OFF_SLOT = NA_OFF_START + 4 * ((size_t)NA_MAX_CELLS + 64);
 constexpr size_t NA_OFF_CELL = NA_OFF_SLOT + 4 * (size_t)NA_MAX_ATOMS;
 constexpr size_t NA_OFF_SORTED = NA_OFF_CELL + 4 * (size_t)NA_MAX_ATOMS;
 constexpr size_t NA_OFF_PE = NA_OFF_SORTED + 4 * (size_t)NA_MAX_ATOMS;
-constexpr size_t NA_SCRATCH_BYTES = NA_OFF_PE + 8 * (size_t)NA_MAX_BLOCKS;  // about 3.4 MB
+constexpr size_t NA_OFF_STATUS = NA_OFF_PE + 8 * XS_WORDS * (size_t)NA_MAX_BLOCKS;
+constexpr size_t NA_SCRATCH_BYTES = NA_OFF_STATUS + 256;  // about 3.5 MB
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_SCRATCH_BYTES];
 
@@ -59,7 +68,8 @@ struct NaScratch {
     int32_t* slot;
     int32_t* cell;
     int32_t* sorted;
-    double* pe;
+    long long* pe;    // per-block exact-sum partials of the pair energies (XS_WORDS words each)
+    int32_t* status;  // nonzero when a type id was out of range in this call
 };
 
 __device__ __forceinline__ NaScratch na_carve(unsigned char* base) {
@@ -69,7 +79,8 @@ __device__ __forceinline__ NaScratch na_carve(unsigned char* base) {
     s.slot = (int32_t*)(base + NA_OFF_SLOT);
     s.cell = (int32_t*)(base + NA_OFF_CELL);
     s.sorted = (int32_t*)(base + NA_OFF_SORTED);
-    s.pe = (double*)(base + NA_OFF_PE);
+    s.pe = (long long*)(base + NA_OFF_PE);
+    s.status = (int32_t*)(base + NA_OFF_STATUS);
     return s;
 }
 
@@ -81,6 +92,7 @@ __device__ __forceinline__ double na_min_image(double r, double h, double hinv) 
 
 __global__ void na_clear(unsigned char* base, int ncells) {
     NaScratch s = na_carve(base);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *s.status = 0;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncells; c += gridDim.x * blockDim.x) s.count[c] = 0;
 }
 
@@ -156,76 +168,80 @@ __global__ void __launch_bounds__(NA_THREADS) na_force(unsigned char* base, cons
                                                        const double* __restrict__ pos,
                                                        const int32_t* __restrict__ types, double* forces) {
     NaScratch s = na_carve(base);
-    __shared__ double sh[32];
+    __shared__ long long shx[XS_WORDS * (NA_THREADS / 32)];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double e = 0.0;
+    XAcc e;
+    pis::xacc_zero(e);
     if (i < P.n) {
         const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
         const int ti = types[i] - 1;
         const int lc = s.cell[i];
         const int cx = lc % P.nc[0], cy = (lc / P.nc[0]) % P.nc[1], cz = lc / (P.nc[0] * P.nc[1]);
         double fx = 0.0, fy = 0.0, fz = 0.0;
-        for (int oz = -1; oz <= 1; ++oz)
-            for (int oy = -1; oy <= 1; ++oy)
-                for (int ox = -1; ox <= 1; ++ox) {
-                    const int nb = (na_wrap(cz + oz, P.nc[2]) * P.nc[1] + na_wrap(cy + oy, P.nc[1])) * P.nc[0] +
-                                   na_wrap(cx + ox, P.nc[0]);
-                    for (int q = s.start[nb]; q < s.start[nb + 1]; ++q) {
-                        const int j = s.sorted[q];
-                        if (j == i) continue;
-                        const NaPair& L = P.pair[ti * P.nt + (types[j] - 1)];
-                        if (!L.present) continue;
-                        double rx = na_min_image(__dsub_rn(pos[3 * j], xi), P.h[0], P.hinv[0]);
-                        double ry = na_min_image(__dsub_rn(pos[3 * j + 1], yi), P.h[1], P.hinv[1]);
-                        double rz = na_min_image(__dsub_rn(pos[3 * j + 2], zi), P.h[2], P.hinv[2]);
-                        double r2 = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
-                        if (sqrt(r2) > L.rcut) continue;
-                        double inv = __ddiv_rn(1.0, r2);
-                        double s2 = __dmul_rn(L.sigma2, inv);
-                        double vdw = __dmul_rn(s2, __dmul_rn(s2, s2));
-                        double rep = __dmul_rn(vdw, vdw);
-                        double u = __dsub_rn(__dmul_rn(L.eps4, __dsub_rn(rep, vdw)), L.ucut);
-                        double c = __dmul_rn(__dmul_rn(L.eps24, __dsub_rn(__dmul_rn(2.0, rep), vdw)), inv);
-                        fx = __dsub_rn(fx, __dmul_rn(c, rx));
-                        fy = __dsub_rn(fy, __dmul_rn(c, ry));
-                        fz = __dsub_rn(fz, __dmul_rn(c, rz));
-                        e += u;
+        bool bad = ti < 0 || ti >= P.nt;
+        if (!bad)
+            for (int oz = -1; oz <= 1; ++oz)
+                for (int oy = -1; oy <= 1; ++oy)
+                    for (int ox = -1; ox <= 1; ++ox) {
+                        const int nb = (na_wrap(cz + oz, P.nc[2]) * P.nc[1] + na_wrap(cy + oy, P.nc[1])) * P.nc[0] +
+                                       na_wrap(cx + ox, P.nc[0]);
+                        for (int q = s.start[nb]; q < s.start[nb + 1]; ++q) {
+                            const int j = s.sorted[q];
+                            if (j == i) continue;
+                            const int tj = types[j] - 1;
+                            if (tj < 0 || tj >= P.nt) {  // flagged below; the pair is skipped
+                                bad = true;
+                                continue;
+                            }
+                            const NaPair& L = P.pair[ti * P.nt + tj];
+                            if (!L.present) continue;
+                            double rx = na_min_image(__dsub_rn(pos[3 * j], xi), P.h[0], P.hinv[0]);
+                            double ry = na_min_image(__dsub_rn(pos[3 * j + 1], yi), P.h[1], P.hinv[1]);
+                            double rz = na_min_image(__dsub_rn(pos[3 * j + 2], zi), P.h[2], P.hinv[2]);
+                            double r2 =
+                                __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
+                            if (sqrt(r2) > L.rcut) continue;
+                            double inv = __ddiv_rn(1.0, r2);
+                            double s2 = __dmul_rn(L.sigma2, inv);
+                            double vdw = __dmul_rn(s2, __dmul_rn(s2, s2));
+                            double rep = __dmul_rn(vdw, vdw);
+                            double u = __dsub_rn(__dmul_rn(L.eps4, __dsub_rn(rep, vdw)), L.ucut);
+                            double c = __dmul_rn(__dmul_rn(L.eps24, __dsub_rn(__dmul_rn(2.0, rep), vdw)), inv);
+                            fx = __dsub_rn(fx, __dmul_rn(c, rx));
+                            fy = __dsub_rn(fy, __dmul_rn(c, ry));
+                            fz = __dsub_rn(fz, __dmul_rn(c, rz));
+                            pis::xacc_add(e, u);
+                        }
                     }
-                }
+        if (bad) atomicOr(s.status, 1);
         forces[3 * i] = fx;
         forces[3 * i + 1] = fy;
         forces[3 * i + 2] = fz;
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = e;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double r = threadIdx.x < NA_THREADS / 32 ? sh[threadIdx.x] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-        if (threadIdx.x == 0) s.pe[blockIdx.x] = r;
-    }
+    pis::xacc_block_store<NA_THREADS>(e, s.pe + (int64_t)blockIdx.x * XS_WORDS, shx);
 }
 
-__global__ void na_finish(unsigned char* base, int nblocks, double* pe_out) {
+// Energy: half the exact sum of the blocks' partials (every pair appears twice); NaN when a type id
+// was out of range.
+__global__ void __launch_bounds__(256) na_finish(unsigned char* base, int nblocks, double* pe_out) {
     NaScratch s = na_carve(base);
-    __shared__ double sh[32];
-    double v = 0.0;
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) v += s.pe[b];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double r = threadIdx.x < (int)(blockDim.x / 32) ? sh[threadIdx.x] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-        if (threadIdx.x == 0) *pe_out = 0.5 * r;
+    __shared__ long long shx[XS_WORDS * 8];
+    __shared__ long long tot[XS_WORDS];
+    XAcc a;
+    pis::xacc_zero(a);
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        const long long* q = s.pe + (int64_t)b * XS_WORDS;
+        for (int z = 0; z < pis::XS_LIMBS; ++z) a.l[z] += q[z];
+        a.bad += q[pis::XS_LIMBS];
     }
+    pis::xacc_block_store<256>(a, tot, shx);
+    __syncthreads();
+    if (threadIdx.x == 0) *pe_out = *s.status ? __longlong_as_double(0x7ff8000000000000ll) : 0.5 * pis::xacc_value(tot);
 }
 
 // Per-device address of the scratch array, looked up once per device with that device current.
+// The address belongs to the device's primary context: it stays valid for the life of that context
+// (cudaDeviceReset ends it; calls after a reset are not supported).
 std::mutex g_na_mutex;
 void* g_na_addr[NA_MAX_DEVICES] = {nullptr};
 
@@ -308,11 +324,19 @@ extern "C" pis_status pis_gpu_compute_potential_noalloc(const pis_lj_pair* table
     unsigned char* b = (unsigned char*)base;
     cudaStream_t st = (cudaStream_t)stream;
     const int nblk = (int)((n + NA_THREADS - 1) / NA_THREADS);
+    // an error the caller's earlier work left pending is not this call's: it is neither reported
+    // nor cleared here
+    const cudaError_t pending = cudaPeekAtLastError();
     na_clear<<<64, 256, 0, st>>>(b, (int)ncells);
     na_bin<<<nblk, NA_THREADS, 0, st>>>(b, P, d_pos);
     na_scan<<<1, 1024, 0, st>>>(b, (int)ncells);
     na_scatter<<<nblk, NA_THREADS, 0, st>>>(b, (int)n);
     na_force<<<nblk, NA_THREADS, 0, st>>>(b, P, d_pos, d_type_ids, d_forces);
     na_finish<<<1, 256, 0, st>>>(b, nblk, d_pe);
-    return cudaGetLastError() == cudaSuccess ? PIS_OK : PIS_ERR_CUDA;
+    const cudaError_t now = cudaPeekAtLastError();
+    if (now != cudaSuccess && now != pending) {
+        if (pending == cudaSuccess) cudaGetLastError();  // this call's own launch error
+        return PIS_ERR_CUDA;
+    }
+    return PIS_OK;
 }

@@ -29,6 +29,8 @@ struct pis_gpu_ctx {
     bool plain_graphs = false;
     bool unfused = false;
     bool ref_order = false;
+    int list_cap_req = 0;   // per-atom list capacity asked for (0 = from the density)
+    bool auto_grow = true;  // grow the list and run again when it overflows
     std::unique_ptr<pis::Engine> eng;
     pis::PoolOptions pool;  // options the current engine was created with
     int slot = -1;
@@ -75,6 +77,38 @@ pis_status flags_to_status(pis_gpu_ctx* ctx, const pis::SysState& ss) {
     if (ss.flags & pis::FLAG_TIMEOUT)
         return fail(ctx, PIS_ERR_TIMEOUT, "a device-side wait expired; results are invalid");
     return PIS_OK;
+}
+
+// After a list overflow: a capacity that holds the longest list the build asked for, with room.
+int64_t grown_capacity(const pis::Engine& e, const pis::SysState& ss) {
+    const int64_t cap = e.list_cap();
+    const int64_t need = (int64_t)ss.need_nn + ss.need_nn / 8 + 8;
+    return std::max(cap + cap / 4, need);
+}
+
+bool overflowed(const pis::SysState& ss) { return (ss.flags & pis::FLAG_LIST_OVERFLOW) != 0; }
+
+constexpr int MAX_GROWTH = 6;  // list growths per call before the overflow is returned
+
+pis_status compute_with_growth(pis_gpu_ctx* ctx, pis::SysState& ss, std::string& err) {
+    pis::Engine& e = *ctx->eng;
+    const bool grow = ctx->auto_grow && e.per_atom_list();
+    for (int attempt = 0;; ++attempt) {
+        pis_status st = PIS_OK;
+        if (grow) {
+            st = e.save_state(ctx->slot, err);
+            if (st) return st;
+        }
+        st = e.compute_potential(err);
+        if (st) return st;
+        st = e.read_state(ctx->slot, ss, err);
+        if (st) return st;
+        if (!grow || !overflowed(ss) || attempt >= MAX_GROWTH) return PIS_OK;
+        st = e.grow_list(grown_capacity(e, ss), err);
+        if (st) return st;
+        st = e.restore_state(ctx->slot, err);
+        if (st) return st;
+    }
 }
 
 }  // namespace
@@ -208,7 +242,7 @@ pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_id
     }
     opt.max_cells = ncell + 1;
     opt.max_types_total = ctx->n_types * ctx->n_types;
-    opt.list_cap = list_capacity(n, d.h, rlist);
+    opt.list_cap = ctx->list_cap_req > 0 ? ctx->list_cap_req : list_capacity(n, d.h, rlist);
     std::string err;
     if (ctx->eng && ctx->slot >= 0 && same_pool(ctx->pool, opt)) {
         // same pool shape: replace the system in place
@@ -236,13 +270,19 @@ pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_id
     return PIS_OK;
 }
 
+pis_status pis_gpu_set_list_capacity(pis_gpu_ctx* ctx, int32_t per_atom, int32_t auto_grow) {
+    if (!ctx) return PIS_ERR_INVALID_ARGUMENT;
+    if (per_atom < 0 || per_atom > 65536) return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "list capacity out of range");
+    ctx->list_cap_req = per_atom;
+    ctx->auto_grow = auto_grow != 0;
+    return PIS_OK;
+}
+
 pis_status pis_gpu_compute_potential(pis_gpu_ctx* ctx, double* pe_out, double* forces) {
     if (!have_state(ctx)) return fail(ctx, PIS_ERR_STATE, "no atoms uploaded");
     std::string err;
-    pis_status st = ctx->eng->compute_potential(err);
-    if (st) return fail(ctx, st, err);
     pis::SysState ss;
-    st = ctx->eng->read_state(ctx->slot, ss, err);
+    pis_status st = compute_with_growth(ctx, ss, err);
     if (st) return fail(ctx, st, err);
     if (pe_out) *pe_out = ss.pe;
     if (forces) {
@@ -253,32 +293,64 @@ pis_status pis_gpu_compute_potential(pis_gpu_ctx* ctx, double* pe_out, double* f
 }
 
 pis_status pis_gpu_verlet_step_nve(pis_gpu_ctx* ctx, double dt, int64_t n_steps, double* pe_out) {
+    return pis_gpu_verlet_step_nve_thermo(ctx, dt, n_steps, pe_out, nullptr, nullptr);
+}
+
+pis_status pis_gpu_verlet_step_nve_thermo(pis_gpu_ctx* ctx, double dt, int64_t n_steps, double* pe_out, double* ke_out,
+                                          double* virial_trace_out) {
     if (!have_state(ctx)) return fail(ctx, PIS_ERR_STATE, "no atoms uploaded");
     if (n_steps < 0 || !(dt == dt)) return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "bad step count or dt");
     std::string err;
     pis_status st = ctx->eng->set_dt(ctx->slot, dt, err);
     if (st) return fail(ctx, st, err);
     ctx->dt = dt;
-    const int64_t chunk = 1000;
+    const int64_t chunk = 1000;  // within the 1024-step history rings
     int64_t done = 0;
+    pis::Engine& e = *ctx->eng;
+    const bool grow = ctx->auto_grow && e.per_atom_list();
+    const bool thermo = virial_trace_out != nullptr;
+    if (thermo) {
+        st = e.set_thermo(ctx->slot, true, err);
+        if (st) return fail(ctx, st, err);
+    }
+    auto finish = [&](pis_status r) {
+        if (thermo) {
+            std::string e2;
+            e.set_thermo(ctx->slot, false, e2);
+        }
+        return r;
+    };
     while (done < n_steps) {
         int64_t k = std::min(chunk, n_steps - done);
-        st = ctx->eng->set_steps(ctx->slot, k, err);
-        if (st) return fail(ctx, st, err);
-        st = ctx->eng->run(k, err);
-        if (st) return fail(ctx, st, err);
         pis::SysState ss;
-        st = ctx->eng->read_state(ctx->slot, ss, err);
-        if (st) return fail(ctx, st, err);
-        if (pe_out) {
-            st = ctx->eng->read_pe_history(ctx->slot, k, pe_out + done, err);
-            if (st) return fail(ctx, st, err);
+        // a chunk whose list overflowed is run again from its checkpoint with a larger list
+        for (int attempt = 0;; ++attempt) {
+            if (grow) {
+                st = e.save_state(ctx->slot, err);
+                if (st) return finish(fail(ctx, st, err));
+            }
+            st = e.set_steps(ctx->slot, k, err);
+            if (st) return finish(fail(ctx, st, err));
+            st = e.run(k, err);
+            if (st) return finish(fail(ctx, st, err));
+            st = e.read_state(ctx->slot, ss, err);
+            if (st) return finish(fail(ctx, st, err));
+            if (!grow || !overflowed(ss) || attempt >= MAX_GROWTH) break;
+            st = e.grow_list(grown_capacity(e, ss), err);
+            if (st) return finish(fail(ctx, st, err));
+            st = e.restore_state(ctx->slot, err);
+            if (st) return finish(fail(ctx, st, err));
+        }
+        if (pe_out || ke_out || virial_trace_out) {
+            st = e.read_history(ctx->slot, k, pe_out ? pe_out + done : nullptr, ke_out ? ke_out + done : nullptr,
+                                virial_trace_out ? virial_trace_out + done : nullptr, err);
+            if (st) return finish(fail(ctx, st, err));
         }
         st = flags_to_status(ctx, ss);
-        if (st) return st;
+        if (st) return finish(st);
         done += k;
     }
-    return PIS_OK;
+    return finish(PIS_OK);
 }
 
 pis_status pis_gpu_run_timed(pis_gpu_ctx* ctx, double dt, int64_t n_steps, double* device_ms, double* stage_ms) {

@@ -26,7 +26,7 @@ class GpuContext:
 
     def __init__(self, table, n_types, skin=0.3, precision="fp64", list_kind="default", shift=True,
                  fp64_fast=False, mixed_kahan=False, lanes=0, batch=0, tma=False, cluster=0, scan=0, tiles=False,
-                 plain_graphs=False, unfused=False, ref_order=False):
+                 plain_graphs=False, unfused=False, ref_order=False, list_capacity=0, auto_grow=True):
         self._lib = _ffi.lib()
         self.n_types = int(n_types)
         pairs = (_ffi.LJPair * len(table))()
@@ -44,6 +44,8 @@ class GpuContext:
                                   plain_graphs, unfused, ref_order)
         if list_kind != "default" or flags:
             self._check(self._lib.pis_gpu_set_options(self._h, _ffi.LIST_KIND[list_kind], flags))
+        if list_capacity or not auto_grow:
+            self._check(self._lib.pis_gpu_set_list_capacity(self._h, int(list_capacity), int(bool(auto_grow))))
 
     def _check(self, st):
         if st != 0:
@@ -75,6 +77,14 @@ class GpuContext:
         pe = np.zeros(n_steps) if want_pe else None
         self._check(self._lib.pis_gpu_verlet_step_nve(self._h, float(dt), int(n_steps), _dp(pe)))
         return pe
+
+    def verlet_step_nve_thermo(self, dt, n_steps):
+        """n_steps NVE steps with every step's (PE, KE, virial trace) recorded on the device and
+        read back once: three arrays of n_steps values."""
+        pe, ke, tr = np.zeros(n_steps), np.zeros(n_steps), np.zeros(n_steps)
+        self._check(self._lib.pis_gpu_verlet_step_nve_thermo(self._h, float(dt), int(n_steps), _dp(pe), _dp(ke),
+                                                             _dp(tr)))
+        return pe, ke, tr
 
     def run_timed(self, dt, n_steps, stages=False):
         """Measurement hook: (device milliseconds, per-stage milliseconds or None)."""
