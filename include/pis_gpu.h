@@ -45,7 +45,7 @@ typedef enum {
     PIS_ERR_LIST_OVERFLOW = 23,    /* a neighbour or cell list outgrew its capacity */
     PIS_ERR_CUDA = 24,             /* any CUDA runtime error */
     PIS_ERR_STATE = 25,            /* call out of order (e.g. no atoms uploaded yet) */
-    PIS_ERR_UNSUPPORTED = 26,      /* e.g. non-orthorhombic box */
+    PIS_ERR_UNSUPPORTED = 26,      /* e.g. a triclinic box in mixed precision */
     PIS_ERR_TIMEOUT = 27           /* a bounded device-side wait expired (the kernel stopped early) */
 } pis_status;
 
@@ -140,6 +140,14 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
  * effect at the next set_state, auto_grow at once. */
 pis_status pis_gpu_set_list_capacity(pis_gpu_ctx* ctx, int32_t per_atom, int32_t auto_grow);
 
+/* Poll budget of the bounded waits in the bulk-copy (TMA) force variants (PIS_OPT_LIST_TMA,
+ * PIS_OPT_TILE; no counterpart in the reference): polls < 0 restores the default (2^22 polls).
+ * A wait that runs out stops the block's pipeline, waits (with the full budget) for the block's own
+ * copies in flight and returns PIS_ERR_TIMEOUT from the call; a budget of 0 makes every such wait
+ * run out at once, so tests can exercise that path on a correct kernel. Takes effect at the next
+ * set_state. */
+pis_status pis_gpu_set_wait_limit(pis_gpu_ctx* ctx, int64_t polls);
+
 /* Upload the Atoms state (src/atoms/new.rs:9-17). force may be NULL (zero forces, as the
  * data-file reader leaves them, src/readers/input_file/commands.rs:367). The only
  * AoS <-> device-layout transpose happens here and in pis_gpu_get_state. */
@@ -186,9 +194,18 @@ pis_status pis_gpu_neighbour_list(pis_gpu_ctx* ctx, int64_t* offsets, int32_t* i
 
 /* Ensemble hooks (src/potentials/potential.rs:45-50, 119-134): v <- M v for every atom, and
  * Atoms::scale_box (src/atoms/transformations.rs:5-16): r <- (M h) h^-1 r with h <- M h. Both
- * take row-major 3x3 M. scale_box forces a neighbour-list rebuild at the next evaluation. */
+ * take row-major 3x3 M. scale_box forces a neighbour-list rebuild at the next evaluation. A matrix
+ * M with off-diagonal elements makes the box triclinic, which the FP64 path with exact arithmetic
+ * and one thread per atom supports (the MTK barostat's box update, src/ensemble/npt.rs:49-56); the
+ * cell grid keeps its counts, so the box may not shrink below one list radius per cell. */
 pis_status pis_gpu_scale_velocities(pis_gpu_ctx* ctx, const double* m_rowmajor);
 pis_status pis_gpu_scale_box(pis_gpu_ctx* ctx, const double* m_rowmajor);
+
+/* Atoms::pressure_tensor (src/atoms/properties.rs:53-59): (sum_i v_i v_i^T + sum_i r_i F_i^T) /
+ * volume, row-major, the kinetic tensor without masses as in the reference; and the current box
+ * (3x3 column-major, nalgebra storage). */
+pis_status pis_gpu_pressure_tensor(pis_gpu_ctx* ctx, double* p_rowmajor);
+pis_status pis_gpu_get_box(pis_gpu_ctx* ctx, double* h_colmajor);
 
 pis_status pis_gpu_get_stats(pis_gpu_ctx* ctx, pis_gpu_stats* out);
 const char* pis_gpu_last_error(const pis_gpu_ctx* ctx);

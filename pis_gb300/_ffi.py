@@ -83,6 +83,7 @@ SIGNATURES = [
     ("pis_gpu_create", C.c_int, [C.POINTER(LJPair), C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(_VP)]),
     ("pis_gpu_set_options", C.c_int, [_VP, C.c_int32, C.c_int32]),
     ("pis_gpu_set_list_capacity", C.c_int, [_VP, C.c_int32, C.c_int32]),
+    ("pis_gpu_set_wait_limit", C.c_int, [_VP, C.c_int64]),
     ("pis_gpu_set_state", C.c_int, [_VP, C.c_int64, C.POINTER(C.c_int32), _DP, _DP, _DP, _DP, _DP,
                                     C.POINTER(C.c_uint8)]),
     ("pis_gpu_compute_potential", C.c_int, [_VP, _DP, _DP]),
@@ -94,6 +95,8 @@ SIGNATURES = [
                                          C.POINTER(C.c_int64)]),
     ("pis_gpu_scale_velocities", C.c_int, [_VP, _DP]),
     ("pis_gpu_scale_box", C.c_int, [_VP, _DP]),
+    ("pis_gpu_pressure_tensor", C.c_int, [_VP, _DP]),
+    ("pis_gpu_get_box", C.c_int, [_VP, _DP]),
     ("pis_gpu_get_stats", C.c_int, [_VP, C.POINTER(Stats)]),
     ("pis_gpu_last_error", C.c_char_p, [_VP]),
     ("pis_gpu_destroy", None, [_VP]),

@@ -56,6 +56,9 @@ struct Engine::DevPtrs {
     double* tr_hist;      // and the virial trace of every step run with the slot's thermo flag set
     double* tr_part;      // chunk partials of the virial trace
     long long* xtr_part;  // FP64 pools: the same as exact-sum partials
+    double* kt_part;      // chunk partials of the kinetic tensor sum_i v_i v_i^T (9 per chunk)
+    long long* xkt_part;  // FP64 pools: the same as exact-sum partials
+    uint32_t wait_limit;  // polls of a bulk-copy pipeline wait before it expires
     int64_t npad;
     int32_t cap;
     int32_t hist;
@@ -122,6 +125,35 @@ __device__ __forceinline__ double wrap_axis(double r, double h, double hinv) {
 }
 __device__ __forceinline__ double norm2_ref(double x, double y, double z) {
     return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+}
+
+// General (triclinic) boxes, FP64 path: the reference's own 3x3 arithmetic. A matrix-vector
+// product sums each row left to right without fused multiply-adds (nalgebra, as the reference's
+// SimulationBox uses it); m is row-major.
+__device__ __forceinline__ void matvec_ref(const double* m, double x, double y, double z, double& a, double& b,
+                                           double& c) {
+    a = __dadd_rn(__dadd_rn(__dmul_rn(m[0], x), __dmul_rn(m[1], y)), __dmul_rn(m[2], z));
+    b = __dadd_rn(__dadd_rn(__dmul_rn(m[3], x), __dmul_rn(m[4], y)), __dmul_rn(m[5], z));
+    c = __dadd_rn(__dadd_rn(__dmul_rn(m[6], x), __dmul_rn(m[7], y)), __dmul_rn(m[8], z));
+}
+// SimulationBox::apply_boundary_conditions_dis (src/simulation_box.rs:17-27): s = h^-1 r,
+// s -= round(s), r = h s (rint for round: they differ only at |s| = 1/2, beyond every cutoff).
+__device__ __forceinline__ void min_image_full(const double* H, const double* HI, double& x, double& y, double& z) {
+    double s0, s1, s2;
+    matvec_ref(HI, x, y, z, s0, s1, s2);
+    s0 = __dsub_rn(s0, rint(s0));
+    s1 = __dsub_rn(s1, rint(s1));
+    s2 = __dsub_rn(s2, rint(s2));
+    matvec_ref(H, s0, s1, s2, x, y, z);
+}
+// SimulationBox::apply_boundary_conditions_pos (src/simulation_box.rs:29-42): s -= floor(s).
+__device__ __forceinline__ void wrap_full(const double* H, const double* HI, double& x, double& y, double& z) {
+    double s0, s1, s2;
+    matvec_ref(HI, x, y, z, s0, s1, s2);
+    s0 = __dsub_rn(s0, floor(s0));
+    s1 = __dsub_rn(s1, floor(s1));
+    s2 = __dsub_rn(s2, floor(s2));
+    matvec_ref(H, s0, s1, s2, x, y, z);
 }
 
 // LennardJones::compute_potential (src/potentials/lennard_jones.rs:33-55) behind the
@@ -195,6 +227,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // Bounded wait for the phase of the given parity: false after `limit` unsuccessful polls (each
 // poll may suspend the warp for a short hardware-defined time), so a wait can never hang.
 constexpr uint32_t MBAR_WAIT_LIMIT = 1u << 22;
+// The same with a caller-given poll budget: the pipelines' waits take the pool's budget
+// (DevPtrs::wait_limit, MBAR_WAIT_LIMIT unless a test lowers it to make the expiry path run on a
+// correct kernel); the final wait for a block's own copies in flight always takes the full one.
+__device__ __forceinline__ bool mbar_wait_n(uint64_t* bar, uint32_t parity, uint32_t limit) {
+    for (uint32_t it = 0; it < limit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     for (uint32_t it = 0; it < MBAR_WAIT_LIMIT; ++it)
         if (mbar_try_wait(bar, parity)) return true;
@@ -289,10 +329,22 @@ __device__ __forceinline__ bool slot_runs(const DP& P, int s, int step_mode) {
     return step_mode ? P.st[s].steps_left > 0 : P.st[s].eval != 0;
 }
 
+// TRIC = false: the instantiation for pools without triclinic slots (the general branch costs the
+// cell sort registers).
+template <bool TRIC = true>
 __device__ __forceinline__ float4 cell_relative(const SysParams& sp, double4_32a p, int lc, int type) {
     int cx = lc % sp.nc[0];
     int cy = (lc / sp.nc[0]) % sp.nc[1];
     int cz = lc / (sp.nc[0] * sp.nc[1]);
+    if (TRIC && sp.tric) {  // position relative to the cell centre H ((c + 1/2) / n), minimum image
+        double x, y, z;
+        matvec_ref(sp.H, (cx + 0.5) / sp.nc[0], (cy + 0.5) / sp.nc[1], (cz + 0.5) / sp.nc[2], x, y, z);
+        x = p.x - x;
+        y = p.y - y;
+        z = p.z - z;
+        min_image_full(sp.H, sp.HI, x, y, z);
+        return make_float4((float)x, (float)y, (float)z, __int_as_float(type));
+    }
     double dx = p.x - (cx + 0.5) * sp.cs[0];
     double dy = p.y - (cy + 0.5) * sp.cs[1];
     double dz = p.z - (cz + 0.5) * sp.cs[2];

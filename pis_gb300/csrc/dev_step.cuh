@@ -36,9 +36,13 @@ __device__ __forceinline__ void skin_test(const DP& P, const SysParams& sp, SysS
     // d2 >= 0, so comparing bit patterns as integers orders it like the doubles (a NaN with
     // either sign fails the test too: its magnitude bits exceed every finite value's)
     if ((__double_as_longlong(d2) & 0x7fffffffffffffffll) > __double_as_longlong(sp.half_skin2)) {
-        dx = min_image_axis(dx, sp.h[0], sp.hinv[0]);
-        dy = min_image_axis(dy, sp.h[1], sp.hinv[1]);
-        dz = min_image_axis(dz, sp.h[2], sp.hinv[2]);
+        if (sp.tric) {
+            min_image_full(sp.H, sp.HI, dx, dy, dz);
+        } else {
+            dx = min_image_axis(dx, sp.h[0], sp.hinv[0]);
+            dy = min_image_axis(dy, sp.h[1], sp.hinv[1]);
+            dz = min_image_axis(dz, sp.h[2], sp.hinv[2]);
+        }
         d2 = fma(dx, dx, fma(dy, dy, dz * dz));
         if (!(d2 <= sp.half_skin2)) {  // NaN also requests a rebuild
             st.rebuild = 1;
@@ -71,9 +75,13 @@ __global__ void k_integrate1(const DP P) {
         x = __dadd_rn(p.x, __dadd_rn(__dmul_rn(v.x, sp.dt), __dmul_rn(__dmul_rn(a.x, 0.5), sp.dt2)));
         y = __dadd_rn(p.y, __dadd_rn(__dmul_rn(v.y, sp.dt), __dmul_rn(__dmul_rn(a.y, 0.5), sp.dt2)));
         z = __dadd_rn(p.z, __dadd_rn(__dmul_rn(v.z, sp.dt), __dmul_rn(__dmul_rn(a.z, 0.5), sp.dt2)));
-        x = wrap_axis(x, sp.h[0], sp.hinv[0]);
-        y = wrap_axis(y, sp.h[1], sp.hinv[1]);
-        z = wrap_axis(z, sp.h[2], sp.hinv[2]);
+        if (sp.tric) {
+            wrap_full(sp.H, sp.HI, x, y, z);
+        } else {
+            x = wrap_axis(x, sp.h[0], sp.hinv[0]);
+            y = wrap_axis(y, sp.h[1], sp.hinv[1]);
+            z = wrap_axis(z, sp.h[2], sp.hinv[2]);
+        }
     } else {
         drift_mixed(sp, p, v, a.x, a.y, a.z, x, y, z);
     }
@@ -97,10 +105,16 @@ __device__ __forceinline__ void bin_chunk(const DP& P, int blk, int respect_step
     double4_32a p = P.pos[st.cur][i];
     int c[3];
     double q[3] = {p.x, p.y, p.z};
+    if (sp.tric) {  // fractional coordinates s = H^-1 r; the cell grid divides them
+        matvec_ref(sp.HI, p.x, p.y, p.z, q[0], q[1], q[2]);
+    } else {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) q[d] = __dmul_rn(sp.hinv[d], q[d]);
+    }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         // floor and conversion in one saturating instruction
-        long long k = __double2ll_rd(__dmul_rn(__dmul_rn(sp.hinv[d], q[d]), (double)sp.nc[d]));
+        long long k = __double2ll_rd(__dmul_rn(q[d], (double)sp.nc[d]));
         k %= sp.nc[d];
         if (k < 0) k += sp.nc[d];
         c[d] = (int)k;
@@ -245,6 +259,7 @@ __device__ __forceinline__ uint32_t cell_order_key(const SysParams& sp, const fl
 // the new buffer set and record the build snapshot and cell-relative coordinates.
 constexpr int GATHER_SMEM_KEYS = 256;  // per warp: order keys of cells of 65..256 atoms
 
+template <bool TRIC>
 __device__ __forceinline__ void gather_cell(const DP& P, int64_t g, int respect_steps, uint32_t* kb) {
     int lane = threadIdx.x & 31;
     int s = P.cell_sys[g];
@@ -264,7 +279,7 @@ __device__ __forceinline__ void gather_cell(const DP& P, int64_t g, int respect_
     // cells recompute keys
     auto key_of = [&](int src) {
         const double4_32a p = P.pos[src_set][src];
-        return cell_order_key(sp, cell_relative(sp, p, lc, 0), (uint32_t)P.id[src_set][src]);
+        return cell_order_key(sp, cell_relative<TRIC>(sp, p, lc, 0), (uint32_t)P.id[src_set][src]);
     };
     int rk[2] = {0, 0}, srcs[2] = {-1, -1};
     uint32_t keys[2] = {0xffffffffu, 0xffffffffu};
@@ -276,7 +291,7 @@ __device__ __forceinline__ void gather_cell(const DP& P, int64_t g, int respect_
             if (k < cnt) {
                 srcs[h] = P.perm[beg + k];
                 const double4_32a p = P.pos[src_set][srcs[h]];
-                qs[h] = cell_relative(sp, p, lc, type_of(p.w));
+                qs[h] = cell_relative<TRIC>(sp, p, lc, type_of(p.w));
                 keys[h] = cell_order_key(sp, qs[h], (uint32_t)P.id[src_set][srcs[h]]);
             }
         }
@@ -310,13 +325,13 @@ __device__ __forceinline__ void gather_cell(const DP& P, int64_t g, int respect_
             const uint32_t mine = kb[k];
             for (int r = 0; r < cnt; ++r) rank += kb[r] < mine;
             p = P.pos[src_set][src];
-            q = cell_relative(sp, p, lc, type_of(p.w));
+            q = cell_relative<TRIC>(sp, p, lc, type_of(p.w));
         } else {
             src = P.perm[beg + k];
             const uint32_t mine = key_of(src);
             for (int r = 0; r < cnt; ++r) rank += key_of(P.perm[beg + r]) < mine;
             p = P.pos[src_set][src];
-            q = cell_relative(sp, p, lc, type_of(p.w));
+            q = cell_relative<TRIC>(sp, p, lc, type_of(p.w));
         }
         int dst = beg + rank;
         P.pos[dst_set][dst] = p;
@@ -339,10 +354,11 @@ __device__ __forceinline__ void gather_cell(const DP& P, int64_t g, int respect_
         }
     }
 }
+template <bool TRIC>
 __global__ void k_gather(const DP P, int64_t max_cells, int respect_steps) {
     __shared__ uint32_t keybuf[256 / 32][GATHER_SMEM_KEYS];
     const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (g < max_cells && rebuild_block(P, P.cell_sys, g)) gather_cell(P, g, respect_steps, keybuf[threadIdx.x >> 5]);
+    if (g < max_cells && rebuild_block(P, P.cell_sys, g)) gather_cell<TRIC>(P, g, respect_steps, keybuf[threadIdx.x >> 5]);
 }
 
 // Neighbour-list build at rcut + skin. LPA lanes share one home atom (atoms in cell order, so
@@ -500,7 +516,7 @@ __device__ __forceinline__ void scan_cell(const float4* __restrict__ pp, int j, 
         }
     }
 }
-template <bool HALF>
+template <bool HALF, bool TRIC>
 __device__ __forceinline__ void build1_chunk(const DP& P, int blk, int step_mode) {
     int s, i;
     if (!atom_of_blk(P, blk, s, i)) return;
@@ -523,9 +539,13 @@ __device__ __forceinline__ void build1_chunk(const DP& P, int blk, int step_mode
     const int qmask = P.lq - 1;
     const int64_t jump = npad * P.lq - qmask;
     int cnt = 0;
-    const float gxm = fmaxf(pi.x + 0.5f * csx, 0.f), gxp = fmaxf(0.5f * csx - pi.x, 0.f);
-    const float gym = fmaxf(pi.y + 0.5f * csy, 0.f), gyp = fmaxf(0.5f * csy - pi.y, 0.f);
-    const float gzm = fmaxf(pi.z + 0.5f * csz, 0.f), gzp = fmaxf(0.5f * csz - pi.z, 0.f);
+    // squared distance to the faces of neighbouring cells (orthorhombic cells: skip the cells out of
+    // range for this atom; the parallelepiped cells of a triclinic box are all scanned)
+    const bool tric = TRIC && sp.tric;
+    const bool prune = !tric;
+    const float gxm = prune ? fmaxf(pi.x + 0.5f * csx, 0.f) : 0.f, gxp = prune ? fmaxf(0.5f * csx - pi.x, 0.f) : 0.f;
+    const float gym = prune ? fmaxf(pi.y + 0.5f * csy, 0.f) : 0.f, gyp = prune ? fmaxf(0.5f * csy - pi.y, 0.f) : 0.f;
+    const float gzm = prune ? fmaxf(pi.z + 0.5f * csz, 0.f) : 0.f, gzp = prune ? fmaxf(0.5f * csz - pi.z, 0.f) : 0.f;
     for (int oz = -1; oz <= 1; ++oz) {
         const int z2 = wrapc(cz + oz, nz);
         const float ez = oz < 0 ? gzm : (oz > 0 ? gzp : 0.f);
@@ -543,8 +563,14 @@ __device__ __forceinline__ void build1_chunk(const DP& P, int blk, int step_mode
                                            ((uint32_t)(oz < 0 ? 2 : oz) << 4))
                                           << JBITS;
                 const bool home = ox == 0 && oy == 0 && oz == 0;
-                scan_cell<HALF>(prel + b0, b0, b1, ox * csx - pi.x, oy * csy - pi.y, oz * csz - pi.z, rl2, codebits,
-                                i, home, out, cnt, jump, qmask, cap);
+                float shx = ox * csx, shy = oy * csy, shz = oz * csz;
+                if (tric) {  // image shift ox C0 + oy C1 + oz C2 of the cell edge vectors
+                    shx = (float)ox * sp.fcv[0] + (float)oy * sp.fcv[3] + (float)oz * sp.fcv[6];
+                    shy = (float)ox * sp.fcv[1] + (float)oy * sp.fcv[4] + (float)oz * sp.fcv[7];
+                    shz = (float)ox * sp.fcv[2] + (float)oy * sp.fcv[5] + (float)oz * sp.fcv[8];
+                }
+                scan_cell<HALF>(prel + b0, b0, b1, shx - pi.x, shy - pi.y, shz - pi.z, rl2, codebits, i, home, out,
+                                cnt, jump, qmask, cap);
             }
         }
     }
@@ -555,14 +581,14 @@ __device__ __forceinline__ void build1_chunk(const DP& P, int blk, int step_mode
     P.nn[i] = cnt > cap ? cap : cnt;
 }
 // only_two_cell: just the slots with a two-cell axis (the two-stage build covers the others).
-template <bool HALF>
+template <bool HALF, bool TRIC>
 __global__ void __launch_bounds__(256) k_build1(const DP P, int step_mode, int only_two_cell) {
     if (!rebuild_block(P, P.blk_sys, blockIdx.x)) return;
     if (only_two_cell) {
         const SysParams& sp = P.sp[P.blk_sys[blockIdx.x]];
         if (sp.nc[0] >= 3 && sp.nc[1] >= 3 && sp.nc[2] >= 3) return;
     }
-    build1_chunk<HALF>(P, blockIdx.x, step_mode);
+    build1_chunk<HALF, TRIC>(P, blockIdx.x, step_mode);
 }
 
 // Slots the 27-cell walk does not serve (flagged !walk27: a two-cell axis within 1e-5 of twice
@@ -620,6 +646,7 @@ __global__ void __launch_bounds__(256) k_force_fp64(const DP P, int respect_step
         const LJ64 P0 = lj64_load(tab[0]);
         const double hx = sp.h[0], hy = sp.h[1], hz = sp.h[2];
         const double ix = sp.hinv[0], iy = sp.hinv[1], iz = sp.hinv[2];
+        const bool tric = sp.tric != 0;
         const int nn = P.nn[i];
         const int64_t npad = P.npad;
         for (int k = gl; k < nn; k += LPA) {
@@ -633,9 +660,16 @@ __global__ void __launch_bounds__(256) k_force_fp64(const DP P, int respect_step
             }
             double rx, ry, rz, u, c;
             if (!FAST) {
-                rx = min_image_axis(__dsub_rn(pj.x, pi.x), hx, ix);
-                ry = min_image_axis(__dsub_rn(pj.y, pi.y), hy, iy);
-                rz = min_image_axis(__dsub_rn(pj.z, pi.z), hz, iz);
+                rx = __dsub_rn(pj.x, pi.x);
+                ry = __dsub_rn(pj.y, pi.y);
+                rz = __dsub_rn(pj.z, pi.z);
+                if (tric) {
+                    min_image_full(sp.H, sp.HI, rx, ry, rz);
+                } else {
+                    rx = min_image_axis(rx, hx, ix);
+                    ry = min_image_axis(ry, hy, iy);
+                    rz = min_image_axis(rz, hz, iz);
+                }
                 if (!lj_fp64(L, norm2_ref(rx, ry, rz), u, c)) continue;
             } else {
                 rx = pj.x - pi.x;
@@ -725,10 +759,32 @@ __device__ __forceinline__ int ref_fwd_index(int dx, int dy, int dz) {
 }
 // Reference cell of a wrapped position: floor(s_d n_d) with s = h^-1 r, saturated at 0 as Rust's
 // `f64 as usize`, then modulo n_d (src/atoms/neighbour_list.rs:17-33).
-__device__ __forceinline__ int ref_cell_axis(double x, double hinv, int n) {
-    long long c = __double2ll_rd(__dmul_rn(__dmul_rn(hinv, x), (double)n));
+__device__ __forceinline__ int ref_cell_axis(double s, int n) {  // s: fractional coordinate
+    long long c = __double2ll_rd(__dmul_rn(s, (double)n));
     if (c < 0) c = 0;
     return (int)(c % n);
+}
+__device__ __forceinline__ void ref_cell(const SysParams& sp, const double4_32a& p, int& a, int& b, int& c) {
+    double s0, s1, s2;
+    if (sp.tric) {
+        matvec_ref(sp.HI, p.x, p.y, p.z, s0, s1, s2);
+    } else {
+        s0 = __dmul_rn(sp.hinv[0], p.x);
+        s1 = __dmul_rn(sp.hinv[1], p.y);
+        s2 = __dmul_rn(sp.hinv[2], p.z);
+    }
+    a = ref_cell_axis(s0, sp.rnc[0]);
+    b = ref_cell_axis(s1, sp.rnc[1]);
+    c = ref_cell_axis(s2, sp.rnc[2]);
+}
+__device__ __forceinline__ void ref_min_image(const SysParams& sp, double& x, double& y, double& z) {
+    if (sp.tric) {
+        min_image_full(sp.H, sp.HI, x, y, z);
+    } else {
+        x = min_image_axis(x, sp.h[0], sp.hinv[0]);
+        y = min_image_axis(y, sp.h[1], sp.hinv[1]);
+        z = min_image_axis(z, sp.h[2], sp.hinv[2]);
+    }
 }
 __device__ __forceinline__ int ref_wrap_delta(int d, int n) {
     if (d > 1) d -= n;
@@ -753,10 +809,9 @@ __global__ void __launch_bounds__(256) k_force_fp64_ref(const DP P, int respect_
         const int32_t* __restrict__ oid = P.id[cur];
         const double4_32a pi = pos[i];
         const LJDev* tab = P.tab + sp.tab0 + type_of(pi.w) * sp.nt;
-        const double hx = sp.h[0], hy = sp.h[1], hz = sp.h[2];
-        const double ix = sp.hinv[0], iy = sp.hinv[1], iz = sp.hinv[2];
         const int nx = sp.rnc[0], ny = sp.rnc[1], nz = sp.rnc[2];
-        const int ax = ref_cell_axis(pi.x, ix, nx), ay = ref_cell_axis(pi.y, iy, ny), az = ref_cell_axis(pi.z, iz, nz);
+        int ax, ay, az;
+        ref_cell(sp, pi, ax, ay, az);
         const uint64_t rank_a = (uint64_t)((ax * ny + ay) * nz + az);
         const int nn = P.nn[i];
         const int64_t npad = P.npad;
@@ -766,12 +821,12 @@ __global__ void __launch_bounds__(256) k_force_fp64_ref(const DP P, int respect_
             const double4_32a pj = pos[j];
             const LJDev& T = tab[type_of(pj.w)];
             if (!T.present) continue;
-            const double rx = min_image_axis(__dsub_rn(pj.x, pi.x), hx, ix);
-            const double ry = min_image_axis(__dsub_rn(pj.y, pi.y), hy, iy);
-            const double rz = min_image_axis(__dsub_rn(pj.z, pi.z), hz, iz);
+            double rx = __dsub_rn(pj.x, pi.x), ry = __dsub_rn(pj.y, pi.y), rz = __dsub_rn(pj.z, pi.z);
+            ref_min_image(sp, rx, ry, rz);
             const double r2 = norm2_ref(rx, ry, rz);
             if (r2 > T.rc2_hi || (r2 >= T.rc2_lo && sqrt(r2) > T.rcut)) continue;
-            const int bx = ref_cell_axis(pj.x, ix, nx), by = ref_cell_axis(pj.y, iy, ny), bz = ref_cell_axis(pj.z, iz, nz);
+            int bx, by, bz;
+            ref_cell(sp, pj, bx, by, bz);
             const int dx = ref_wrap_delta(bx - ax, nx), dy = ref_wrap_delta(by - ay, ny), dz = ref_wrap_delta(bz - az, nz);
             int o = ref_fwd_index(dx, dy, dz);
             uint64_t rank = rank_a;
@@ -802,9 +857,8 @@ __global__ void __launch_bounds__(256) k_force_fp64_ref(const DP P, int respect_
             const int j = (int)(P.nbr[(int64_t)k * npad + i] & JMASK);
             const double4_32a pj = pos[j];
             const LJ64 L = lj64_load(tab[type_of(pj.w)]);
-            const double rx = min_image_axis(__dsub_rn(pj.x, pi.x), hx, ix);
-            const double ry = min_image_axis(__dsub_rn(pj.y, pi.y), hy, iy);
-            const double rz = min_image_axis(__dsub_rn(pj.z, pi.z), hz, iz);
+            double rx = __dsub_rn(pj.x, pi.x), ry = __dsub_rn(pj.y, pi.y), rz = __dsub_rn(pj.z, pi.z);
+            ref_min_image(sp, rx, ry, rz);
             double u, c;
             lj_fp64(L, norm2_ref(rx, ry, rz), u, c);
             fx = __dsub_rn(fx, __dmul_rn(c, rx));
@@ -1168,7 +1222,7 @@ __global__ void __launch_bounds__(256, KB <= 8 ? 4 : 2) k_force_mixed_tma(const 
     for (int r = 0; r < R; ++r) {
         const int q0 = r % S;
         const uint32_t par = (uint32_t)(r / S) & 1u;
-        if (!failed && !mbar_wait(&full[q0], par)) failed = true;
+        if (!failed && !mbar_wait_n(&full[q0], par, P.wait_limit)) failed = true;
         if (!failed) {
             done = r + 1;
             const int k0 = r * KB;
@@ -1185,7 +1239,7 @@ __global__ void __launch_bounds__(256, KB <= 8 ? 4 : 2) k_force_mixed_tma(const 
         if (lane == 0) mbar_arrive(&empty[q0]);
         if (t == 0 && !failed && issued < R) {
             // refill this stage with batch r + S once every warp has released batch r
-            if (mbar_wait(&empty[q0], par))
+            if (mbar_wait_n(&empty[q0], par, P.wait_limit))
                 issue(issued++);
             else
                 failed = true;
@@ -1302,7 +1356,7 @@ __global__ void __launch_bounds__(256) k_force_mixed_tile(const DP P, int step_m
                      : make_float4(ox * sp.fcs[0], oy * sp.fcs[1], oz * sp.fcs[2], __int_as_float(delta));
     }
     __syncthreads();
-    bool got = tiled && mbar_wait(&bar, 0u);
+    bool got = tiled && mbar_wait_n(&bar, 0u, P.wait_limit);
     if (tiled && !got) atomicOr(&st.flags, FLAG_TIMEOUT);
     // every thread uses the tile only if the whole block saw it arrive
     got = __syncthreads_and(got ? 1 : 0) != 0;

@@ -93,13 +93,23 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
             if (live) xacc_add(x, virial_trace(p, f));
             xacc_block_store<256>(x, P.xtr_part + (int64_t)blockIdx.x * XS_WORDS, shx);
         }
-        if (st.want_virial) {
+        if (st.want_virial & 1) {
             const double r[3] = {p.x, p.y, p.z}, g[3] = {f.x, f.y, f.z};
             for (int a = 0; a < 3; ++a)
                 for (int b = 0; b < 3; ++b) {
                     xacc_zero(x);
                     if (live) xacc_add(x, __dmul_rn(r[a], g[b]));
                     xacc_block_store<256>(x, P.xvir_part + ((int64_t)blockIdx.x * 9 + a * 3 + b) * XS_WORDS, shx);
+                }
+        }
+        if (!UPDATE && (st.want_virial & 2)) {  // kinetic tensor sum_i v_i v_i^T
+            const double4_32a v = live ? P.vel[cur][i] : make_double4_32a(0.0, 0.0, 0.0, 0.0);
+            const double u[3] = {v.x, v.y, v.z};
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    xacc_zero(x);
+                    if (live) xacc_add(x, __dmul_rn(u[a], u[b]));
+                    xacc_block_store<256>(x, P.xkt_part + ((int64_t)blockIdx.x * 9 + a * 3 + b) * XS_WORDS, shx);
                 }
         }
         return;
@@ -110,7 +120,7 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
         const double t = block_sum<256>(live ? virial_trace(p, f) : 0.0, sh);
         if (threadIdx.x == 0) P.tr_part[blockIdx.x] = t;
     }
-    if (st.want_virial) {
+    if (st.want_virial & 1) {
         double r[3] = {p.x, p.y, p.z}, g[3] = {f.x, f.y, f.z};
 #pragma unroll
         for (int a = 0; a < 3; ++a)
@@ -118,6 +128,15 @@ __global__ void k_integrate2(const DP P, int respect_steps) {
             for (int b = 0; b < 3; ++b) {
                 double t = block_sum<256>(live ? r[a] * g[b] : 0.0, sh);
                 if (threadIdx.x == 0) P.vir_part[(int64_t)blockIdx.x * 9 + a * 3 + b] = t;
+            }
+    }
+    if (!UPDATE && (st.want_virial & 2)) {  // kinetic tensor sum_i v_i v_i^T
+        const double4_32a v = live ? P.vel[cur][i] : make_double4_32a(0.0, 0.0, 0.0, 0.0);
+        const double u[3] = {v.x, v.y, v.z};
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                const double t = block_sum<256>(__dmul_rn(u[a], u[b]), sh);
+                if (threadIdx.x == 0) P.kt_part[(int64_t)blockIdx.x * 9 + a * 3 + b] = t;
             }
     }
 }
@@ -149,7 +168,9 @@ template <int MIX_BATCH>
 __host__ __device__ constexpr int step_list_prefetch() {
     return MIX_BATCH == 4 ? 1 : 4;
 }
-template <int ACC, bool ONE, int MIX_BATCH, bool DRIFT>
+// TRACE: the instantiation launched while some slot records its thermo (the virial trace of every
+// step); the default one carries no trace code (with it the pair loop was measured 6 % slower).
+template <int ACC, bool ONE, int MIX_BATCH, bool DRIFT, bool TRACE>
 __global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixed(const DP P) {
     __shared__ double sh[32];
     __shared__ float shift[12];
@@ -165,8 +186,8 @@ __global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixe
     if (live)
         mixed_atom_forces<ACC, 1, ONE, MIX_BATCH, step_list_prefetch<MIX_BATCH>(), FUSED_LQ>(P, sp, i, 0, shift, acc);
     const bool drift = DRIFT && st.steps_left > 1;
-    const bool want_virial = st.want_virial != 0;
-    const bool want_trace = st.thermo != 0;
+    const bool want_virial = (st.want_virial & 1) != 0;
+    const bool want_trace = TRACE && st.thermo != 0;
     double ke = 0.0;
     double4_32a p = make_double4_32a(0.0, 0.0, 0.0, 0.0), f = p;
     if (live) {
@@ -199,7 +220,7 @@ __global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixe
     if (threadIdx.x == 0) P.pe_part[blockIdx.x] = pe_tot;
     const double ke_tot = block_sum<256>(ke, sh);
     if (threadIdx.x == 0) P.ke_part[blockIdx.x] = 0.5 * ke_tot;
-    if (want_trace) {
+    if (TRACE && want_trace) {
         const double t = block_sum<256>(live ? virial_trace(p, f) : 0.0, sh);
         if (threadIdx.x == 0) P.tr_part[blockIdx.x] = t;
     }
@@ -239,9 +260,11 @@ __device__ __forceinline__ double xacc_slot_value(const long long* part, int64_t
     return v;
 }
 
+// EXACT: an FP64 pool (exact-sum partials); the mixed path's pools sum doubles.
+template <bool EXACT>
 __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) {
     __shared__ double sh[32];
-    __shared__ long long shx[XS_WORDS * (END_THREADS / 32)];
+    __shared__ long long shx[EXACT ? XS_WORDS * (END_THREADS / 32) : 1];
     int s = blockIdx.x;
     const SysParams& sp = P.sp[s];
     if (!sp.active) return;
@@ -250,17 +273,21 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
     if (mode != 0 && !st.eval) return;
     double pe = 0.0, ke = 0.0;
     const int F = P.pe_stride;
-    if (P.exact_sums) {
+    if (EXACT) {
         // FP64 pools: exact sums (PE over the force kernel's blocks, m |v|^2 and r_i F_i per chunk)
         double w[9];
-        const bool vir = st.want_virial && mode != 1;
+        const bool vir = (st.want_virial & 1) && mode != 1;
         if (mode != 2) pe = xacc_slot_value(P.xpe_part, (int64_t)sp.ch0 * F, (int64_t)sp.nch * F, XS_WORDS, shx);
         if (mode != 1) ke = 0.5 * xacc_slot_value(P.xke_part, sp.ch0, sp.nch, XS_WORDS, shx);
         if (vir)
             for (int q = 0; q < 9; ++q)
                 w[q] = xacc_slot_value(P.xvir_part + (int64_t)q * XS_WORDS, sp.ch0, sp.nch, 9 * XS_WORDS, shx);
-        double tr = 0.0;
+        double tr = 0.0, kt[9];
         if (mode == 0 && st.thermo) tr = xacc_slot_value(P.xtr_part, sp.ch0, sp.nch, XS_WORDS, shx);
+        const bool ktn = mode == 2 && (st.want_virial & 2);
+        if (ktn)
+            for (int q = 0; q < 9; ++q)
+                kt[q] = xacc_slot_value(P.xkt_part + (int64_t)q * XS_WORDS, sp.ch0, sp.nch, 9 * XS_WORDS, shx);
         if (threadIdx.x == 0) {
             if (mode != 2) {
                 if (P.full_list) pe *= 0.5;
@@ -269,6 +296,8 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
             if (mode != 1) st.ke = ke;
             if (vir)
                 for (int q = 0; q < 9; ++q) st.virial[q] = w[q];
+            if (ktn)
+                for (int q = 0; q < 9; ++q) st.ktensor[q] = kt[q];
             if ((mode != 2 && pe != pe) || (mode != 1 && ke != ke)) st.flags |= FLAG_NAN;
             if (mode == 2) {
                 st.eval = 0;
@@ -298,7 +327,7 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
     pe = block_sum<END_THREADS>(pe, sh);
     ke = block_sum<END_THREADS>(ke, sh);
     double w[9];
-    const bool vir = st.want_virial && mode != 1;
+    const bool vir = (st.want_virial & 1) && mode != 1;
     if (vir) {
         for (int q = 0; q < 9; ++q) {
             double a = 0.0;
@@ -311,6 +340,15 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
         for (int c = threadIdx.x; c < sp.nch; c += END_THREADS) tr += P.tr_part[sp.ch0 + c];
         tr = block_sum<END_THREADS>(tr, sh);
     }
+    double kt[9];
+    const bool ktn = mode == 2 && (st.want_virial & 2);
+    if (ktn) {
+        for (int q = 0; q < 9; ++q) {
+            double a = 0.0;
+            for (int c = threadIdx.x; c < sp.nch; c += END_THREADS) a += P.kt_part[(int64_t)(sp.ch0 + c) * 9 + q];
+            kt[q] = block_sum<END_THREADS>(a, sh);
+        }
+    }
     if (threadIdx.x == 0) {
         if (mode != 2) {
             if (P.full_list) pe *= 0.5;
@@ -319,6 +357,8 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
         if (mode != 1) st.ke = ke;
         if (vir)
             for (int q = 0; q < 9; ++q) st.virial[q] = w[q];
+        if (ktn)
+            for (int q = 0; q < 9; ++q) st.ktensor[q] = kt[q];
         if ((mode != 2 && pe != pe) || (mode != 1 && ke != ke)) st.flags |= FLAG_NAN;
         if (mode == 2) {
             st.eval = 0;
@@ -385,38 +425,52 @@ __global__ void k_keep(const DP P, int slot) {
         const int64_t q = (int64_t)(k / L) * (P.npad * L) + (int64_t)i * L + k % L;
         int j = (int)(P.nbr[q] & JMASK);
         double4_32a pj = P.pos[cur][j];
-        double rx = min_image_axis(__dsub_rn(pj.x, pi.x), sp.h[0], sp.hinv[0]);
-        double ry = min_image_axis(__dsub_rn(pj.y, pi.y), sp.h[1], sp.hinv[1]);
-        double rz = min_image_axis(__dsub_rn(pj.z, pi.z), sp.h[2], sp.hinv[2]);
+        double rx = __dsub_rn(pj.x, pi.x), ry = __dsub_rn(pj.y, pi.y), rz = __dsub_rn(pj.z, pi.z);
+        if (sp.tric) {
+            min_image_full(sp.H, sp.HI, rx, ry, rz);
+        } else {
+            rx = min_image_axis(rx, sp.h[0], sp.hinv[0]);
+            ry = min_image_axis(ry, sp.h[1], sp.hinv[1]);
+            rz = min_image_axis(rz, sp.h[2], sp.hinv[2]);
+        }
         const LJDev& L = tab[type_of(pj.w)];
         P.keep[q] = (uint8_t)(L.present && !(sqrt(norm2_ref(rx, ry, rz)) > L.rcut));
     }
 }
 
-// v <- M v (row-major M) for one slot (ensemble velocity scaling).
-__global__ void k_scale_vel(const DP P, int slot, double m0, double m1, double m2, double m3, double m4,
-                            double m5, double m6, double m7, double m8) {
+struct Mat3Arg {
+    double m[9];  // row-major
+};
+
+// v <- M v (row-major M) for one slot (ensemble velocity scaling, `&scale * &atoms.velocities`,
+// src/potentials/potential.rs:45-50,119-134), each row summed left to right without fused
+// multiply-adds.
+__global__ void k_scale_vel(const DP P, int slot, const Mat3Arg M) {
     int s, i;
     if (!atom_of(P, s, i) || s != slot) return;
     const int cur = P.st[s].cur;
     double4_32a v = P.vel[cur][i];
-    double x = m0 * v.x + m1 * v.y + m2 * v.z;
-    double y = m3 * v.x + m4 * v.y + m5 * v.z;
-    double z = m6 * v.x + m7 * v.y + m8 * v.z;
+    double x, y, z;
+    matvec_ref(M.m, v.x, v.y, v.z, x, y, z);
     P.vel[cur][i] = make_double4_32a(x, y, z, v.w);
 }
 
-// Atoms::scale_box (src/atoms/transformations.rs:5-16) for a diagonal box and diagonal M:
-// s = h^-1 r (old box), r = h' s (new box).
-__global__ void k_scale_pos(const DP P, int slot, double oh0, double oh1, double oh2, double nh0, double nh1,
-                            double nh2) {
+// Atoms::scale_box (src/atoms/transformations.rs:5-16): s = h^-1 r with the old inverse, r = h' s
+// with the new box. Diagonal boxes use their diagonals (the same products as the full form).
+__global__ void k_scale_pos(const DP P, int slot, const Mat3Arg HI_old, const Mat3Arg H_new, int tric) {
     int s, i;
     if (!atom_of(P, s, i) || s != slot) return;
     const int cur = P.st[s].cur;
     double4_32a p = P.pos[cur][i];
-    p.x = nh0 * (oh0 * p.x);
-    p.y = nh1 * (oh1 * p.y);
-    p.z = nh2 * (oh2 * p.z);
+    if (tric) {
+        double s0, s1, s2;
+        matvec_ref(HI_old.m, p.x, p.y, p.z, s0, s1, s2);
+        matvec_ref(H_new.m, s0, s1, s2, p.x, p.y, p.z);
+    } else {
+        p.x = __dmul_rn(H_new.m[0], __dmul_rn(HI_old.m[0], p.x));
+        p.y = __dmul_rn(H_new.m[4], __dmul_rn(HI_old.m[4], p.y));
+        p.z = __dmul_rn(H_new.m[8], __dmul_rn(HI_old.m[8], p.z));
+    }
     P.pos[cur][i] = p;
 }
 

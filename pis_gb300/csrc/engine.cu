@@ -220,7 +220,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         {(void**)&d_->pe_part, 8 * std::max(NCH * 32, NCC * 4)}, {(void**)&d_->ke_part, 8 * NCH},
         {(void**)&d_->vir_part, 72 * NCH}, {(void**)&d_->pe_hist, 8 * NS * (size_t)opt.hist},
         {(void**)&d_->ke_hist, 8 * NS * (size_t)opt.hist}, {(void**)&d_->tr_hist, 8 * NS * (size_t)opt.hist},
-        {(void**)&d_->tr_part, 8 * NCH},
+        {(void**)&d_->tr_part, 8 * NCH}, {(void**)&d_->kt_part, 72 * NCH},
         {(void**)&d_->ctl, 256},
     };
     if (fused_) items.push_back({&prel_buf_[1], 16 * NA});
@@ -230,6 +230,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         items.push_back({(void**)&d_->xke_part, 8 * XS_WORDS * NCH});
         items.push_back({(void**)&d_->xvir_part, 8 * XS_WORDS * 9 * NCH});
         items.push_back({(void**)&d_->xtr_part, 8 * XS_WORDS * NCH});
+        items.push_back({(void**)&d_->xkt_part, 8 * XS_WORDS * 9 * NCH});
     }
     if (clm_) {
         items.push_back({(void**)&d_->cl_atom, 4 * NCL});
@@ -253,6 +254,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     }
     d_->keep = nullptr;
     d_->exact_sums = exact ? 1 : 0;
+    d_->wait_limit = opt.wait_limit < 0 ? MBAR_WAIT_LIMIT : (uint32_t)std::min<int64_t>(opt.wait_limit, MBAR_WAIT_LIMIT);
     d_->npad = npad_;
     d_->cap = (int32_t)cap_;
     d_->hist = opt.hist;
@@ -324,12 +326,79 @@ static void give_range(std::map<int64_t, int64_t>& fr, int64_t at, int64_t len) 
 
 // Cell grid at rcut + skin: n_d = floor(L_d / rlist) (Atoms::divide_into_cells,
 // src/atoms/neighbour_list.rs:45-57, evaluated at the list radius).
+static bool diagonal_box(const double* h) {
+    return h[1] == 0.0 && h[2] == 0.0 && h[3] == 0.0 && h[5] == 0.0 && h[6] == 0.0 && h[7] == 0.0;
+}
+// nalgebra's 3x3 inverse, as the reference inverts its box (src/simulation_box.rs:13,
+// src/atoms/transformations.rs:12): the adjugate over the determinant by first-row cofactors.
+// m and out are row-major. Returns false for a singular matrix.
+static bool inverse3_ref(const double* m, double* out) {
+    const double c00 = m[4] * m[8] - m[7] * m[5];
+    const double c10 = m[3] * m[8] - m[6] * m[5];
+    const double c20 = m[3] * m[7] - m[6] * m[4];
+    const double det = m[0] * c00 - m[1] * c10 + m[2] * c20;
+    if (det == 0.0) return false;
+    out[0] = c00 / det;
+    out[1] = (m[2] * m[7] - m[8] * m[1]) / det;
+    out[2] = (m[1] * m[5] - m[4] * m[2]) / det;
+    out[3] = -c10 / det;
+    out[4] = (m[0] * m[8] - m[6] * m[2]) / det;
+    out[5] = (m[2] * m[3] - m[5] * m[0]) / det;
+    out[6] = c20 / det;
+    out[7] = (m[1] * m[6] - m[7] * m[0]) / det;
+    out[8] = (m[0] * m[4] - m[3] * m[1]) / det;
+    return true;
+}
+// Widths of the box across each pair of faces: the edges of a diagonal box; for a general box
+// |det h| / |a_e x a_f| with a_d the columns (box vectors). A cell grid of n_d cells along a_d with
+// width_d / n_d >= the list radius keeps every pair within that radius in neighbouring cells.
+static void box_widths(const double* h, double w[3]) {
+    if (diagonal_box(h)) {
+        for (int a = 0; a < 3; ++a) w[a] = h[4 * a];
+        return;
+    }
+    double col[3][3];
+    for (int d = 0; d < 3; ++d)
+        for (int r = 0; r < 3; ++r) col[d][r] = h[3 * r + d];
+    const double vol = std::fabs(col[0][0] * (col[1][1] * col[2][2] - col[1][2] * col[2][1]) -
+                                 col[1][0] * (col[0][1] * col[2][2] - col[0][2] * col[2][1]) +
+                                 col[2][0] * (col[0][1] * col[1][2] - col[0][2] * col[1][1]));
+    for (int d = 0; d < 3; ++d) {
+        const double* e = col[(d + 1) % 3];
+        const double* f = col[(d + 2) % 3];
+        const double cx = e[1] * f[2] - e[2] * f[1], cy = e[2] * f[0] - e[0] * f[2], cz = e[0] * f[1] - e[1] * f[0];
+        w[d] = vol / std::sqrt(cx * cx + cy * cy + cz * cz);
+    }
+}
+
 static void cell_grid(const SlotDesc& d, double rlist, int nc[3]) {
+    double w[3];
+    box_widths(d.h, w);
     for (int a = 0; a < 3; ++a) {
-        double L = d.h[4 * a];
-        double q = std::floor(L / rlist);
+        double q = std::floor(w[a] / rlist);
         nc[a] = q < 1.0 ? 1 : (q > 2000.0 ? 2000 : (int)q);
     }
+}
+
+// Box fields of a slot from a row-major h and its inverse (p.nc set): diagonals (h, hinv) for the
+// orthorhombic kernels, the full matrices and cell edge vectors for a triclinic box, cell widths.
+static void set_box(SysParams& p, const double* h, const double* hi) {
+    double w[3];
+    box_widths(h, w);
+    p.tric = diagonal_box(h) ? 0 : 1;
+    for (int k = 0; k < 9; ++k) {
+        p.H[k] = h[k];
+        p.HI[k] = hi[k];
+    }
+    for (int a = 0; a < 3; ++a) {
+        p.h[a] = h[4 * a];
+        p.hinv[a] = hi[4 * a];
+        p.cs[a] = w[a] / p.nc[a];
+        p.fcs[a] = (float)p.cs[a];
+        p.fsub[a] = (float)(4.0 / p.cs[a]);
+    }
+    for (int d = 0; d < 3; ++d)
+        for (int r = 0; r < 3; ++r) p.fcv[3 * d + r] = (float)(h[3 * r + d] / p.nc[d]);
 }
 
 // The reference's own cell grid at the largest cutoff (Atoms::divide_into_cells,
@@ -354,6 +423,12 @@ static double slot_rlist(const SlotDesc& d) {
     for (auto& e : d.table)
         if (e.present && e.rcut > rc) rc = e.rcut;
     return rc + d.skin;
+}
+
+int64_t Engine::cells_for(const SlotDesc& d) {
+    int nc[3];
+    cell_grid(d, slot_rlist(d), nc);
+    return (int64_t)nc[0] * nc[1] * nc[2];
 }
 
 bool Engine::fits(const SlotDesc& d) const {
@@ -385,12 +460,15 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
         err = "no atoms defined";
         return -PIS_ERR_NO_ATOMS;
     }
-    for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b)
-            if (a != b && d.h[3 * a + b] != 0.0) {
-                err = "only orthorhombic boxes are supported (tilt factors must be zero)";
-                return -PIS_ERR_UNSUPPORTED;
-            }
+    if (!diagonal_box(d.h) && !triclinic_capable()) {
+        err = "general (triclinic) boxes run on the FP64 path with exact arithmetic, one thread per atom";
+        return -PIS_ERR_UNSUPPORTED;
+    }
+    double hinv_full[9];
+    if (!inverse3_ref(d.h, hinv_full)) {
+        err = "box matrix is singular";
+        return -PIS_ERR_INVALID_ARGUMENT;
+    }
     for (int a = 0; a < 3; ++a)
         if (!d.pbc[a]) {
             err = "only fully periodic boxes are supported";
@@ -406,12 +484,20 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
         err = "no pair potential defined";
         return -PIS_ERR_MISSING_POTENTIAL;
     }
-    for (int a = 0; a < 3; ++a) {
-        double L = d.h[4 * a];
-        if (!(L > 2.0 * rlist)) {
-            err = "box edge " + std::to_string(L) + " is not longer than 2 (rcut + skin) = " +
-                  std::to_string(2.0 * rlist);
-            return -PIS_ERR_BOX_TOO_SMALL;
+    {
+        double w[3];
+        box_widths(d.h, w);
+        for (int a = 0; a < 3; ++a) {
+            const double L = w[a];
+            if (!(L > 2.0 * rlist)) {
+                err = "box width " + std::to_string(L) + " is not longer than 2 (rcut + skin) = " +
+                      std::to_string(2.0 * rlist);
+                return -PIS_ERR_BOX_TOO_SMALL;
+            }
+            if (!diagonal_box(d.h) && !(L >= 3.0 * rlist)) {
+                err = "a triclinic box needs at least 3 cells of the list radius across each pair of faces";
+                return -PIS_ERR_BOX_TOO_SMALL;
+            }
         }
     }
     for (int64_t k = 0; k < d.n; ++k)
@@ -521,22 +607,9 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     for (int a = 0; a < 3; ++a) {
         p.nc[a] = nc[a];
         p.pbc[a] = 1;
-        p.h[a] = d.h[4 * a];
     }
     // h^-1 by adjugate / determinant, the reference's 3x3 inverse (src/simulation_box.rs:13)
-    {
-        const double* m = d.h;
-        double m11 = m[4] * m[8] - m[7] * m[5];
-        double det = m[0] * m11 - m[1] * (m[3] * m[8] - m[6] * m[5]) + m[2] * (m[3] * m[7] - m[6] * m[4]);
-        p.hinv[0] = m11 / det;
-        p.hinv[1] = (m[0] * m[8] - m[6] * m[2]) / det;
-        p.hinv[2] = (m[0] * m[4] - m[3] * m[1]) / det;
-    }
-    for (int a = 0; a < 3; ++a) {
-        p.cs[a] = p.h[a] / nc[a];
-        p.fcs[a] = (float)p.cs[a];
-        p.fsub[a] = (float)(4.0 / p.cs[a]);
-    }
+    set_box(p, d.h, hinv_full);
     p.half_skin2 = 0.25 * d.skin * d.skin;
     p.dt = d.dt;
     p.dt2 = d.dt * d.dt;
@@ -623,6 +696,10 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
 
 void Engine::remove_slot(int slot) {
     if (slot < 0 || slot >= opt_.max_slots || !hp_[slot].active) return;
+    if ((int)slot_thermo_.size() > slot && slot_thermo_[slot]) {
+        slot_thermo_[slot] = 0;
+        thermo_slots_ -= 1;
+    }
     SysParams& p = hp_[slot];
     int64_t ncell = (int64_t)p.nc[0] * p.nc[1] * p.nc[2];
     give_range(free_atoms_, p.a0, p.n);
@@ -706,11 +783,14 @@ pis_status Engine::rebuild_block_map(std::string& err) {
     dirty_map_ = false;
     // the force kernel variant depends on whether every slot is single-type; captured graphs
     // bake that choice in, so they are dropped when it flips
-    bool one = true;
-    for (int s = 0; s < opt_.max_slots; ++s)
+    bool one = true, tric = false;
+    for (int s = 0; s < opt_.max_slots; ++s) {
         if (hp_[s].active && hp_[s].nt != 1) one = false;
-    if (one != single_type_) {
+        if (hp_[s].active && hp_[s].tric) tric = true;
+    }
+    if (one != single_type_ || tric != any_tric_) {
         single_type_ = one;
+        any_tric_ = tric;
         for (auto& kv : graphs_) {
             cudaGraphExecDestroy(kv.second.exec);
             for (auto e : kv.second.ev) cudaEventDestroy(e);
@@ -754,7 +834,10 @@ void Engine::enqueue_rebuild(bool respect) {
     LAUNCH(k_scan, (unsigned)opt_.max_slots, SCAN_THREADS, P, r);
     LAUNCH(k_scatter, ga, opt_.blk, P, r);
     unsigned gcells = (unsigned)((opt_.max_cells * 32 + 255) / 256);
-    LAUNCH(k_gather, gcells, 256, P, (int64_t)opt_.max_cells, r);
+    if (any_tric_)
+        LAUNCH(k_gather<true>, gcells, 256, P, (int64_t)opt_.max_cells, r);
+    else
+        LAUNCH(k_gather<false>, gcells, 256, P, (int64_t)opt_.max_cells, r);
     launch_build(r);
     LAUNCH(k_rebuild_done, (unsigned)((opt_.max_slots + 127) / 128), 128, P, r);
 }
@@ -762,16 +845,24 @@ void Engine::enqueue_rebuild(bool respect) {
 // Lanes-per-atom kernels are templates; these dispatch on the pool's runtime choice. Their grid
 // has lpa blocks per chunk.
 // List build over `chunks` (L blocks per chunk for lanes-per-atom layouts).
+template <bool HALF>
+static void launch_build1(const DP& P, bool tric, unsigned g, cudaStream_t st, int r, int only_two_cell) {
+    if (tric)
+        k_build1<HALF, true><<<g, 256, 0, st>>>(P, r, only_two_cell);
+    else
+        k_build1<HALF, false><<<g, 256, 0, st>>>(P, r, only_two_cell);
+}
+
 template <int L>
-static void launch_build_t(const DP& P, bool half, unsigned chunks, cudaStream_t st, int r) {
+static void launch_build_t(const DP& P, bool half, bool tric, unsigned chunks, cudaStream_t st, int r) {
     const unsigned g = chunks * L;
     if (L == 1) {
         // lean kernel for slots with >= 3 cells per axis, generic kernel for the rest
         if (half) {
-            k_build1<true><<<g, 256, 0, st>>>(P, r, 0);
+            launch_build1<true>(P, tric, g, st, r, 0);
             k_build1_generic<true><<<g, 256, 0, st>>>(P, r);
         } else {
-            k_build1<false><<<g, 256, 0, st>>>(P, r, 0);
+            launch_build1<false>(P, tric, g, st, r, 0);
             k_build1_generic<false><<<g, 256, 0, st>>>(P, r);
         }
         g_launches.fetch_add(2);
@@ -913,16 +1004,16 @@ void Engine::launch_build(int r) {
                 k_filter_cl<false, 4><<<gc * 4, CL_THREADS, 0, ls_>>>(*d_, r);
         }
         if (half_) {
-            k_build1<true><<<ga, 256, 0, ls_>>>(*d_, r, 1);
+            launch_build1<true>(*d_, any_tric_, ga, ls_, r, 1);
             k_build1_generic<true><<<ga, 256, 0, ls_>>>(*d_, r);
         } else {
-            k_build1<false><<<ga, 256, 0, ls_>>>(*d_, r, 1);
+            launch_build1<false>(*d_, any_tric_, ga, ls_, r, 1);
             k_build1_generic<false><<<ga, 256, 0, ls_>>>(*d_, r);
         }
         g_launches.fetch_add(4);
         return;
     }
-#define PIS_CALL(L) launch_build_t<L>(*d_, half_, ch, ls_, r)
+#define PIS_CALL(L) launch_build_t<L>(*d_, half_, any_tric_, ch, ls_, r)
     PIS_LPA_DISPATCH(opt_.lpa, PIS_CALL)
 #undef PIS_CALL
 }
@@ -1047,7 +1138,7 @@ void Engine::enqueue_step(bool respect, cudaEvent_t* ev, int64_t q, int64_t g) {
             LAUNCH((k_integrate2<true, true>), (unsigned)max_chunks_, opt_.blk, P, r);
     }
     if (ev) cudaEventRecordWithFlags(ev[4], stream_, cudaEventRecordExternal);
-    LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 0);
+    launch_step_end(0);
     if (ev) cudaEventRecordWithFlags(ev[5], stream_, cudaEventRecordExternal);
     if (fused) {
         d_->prel = (float4*)prel_buf_[0];
@@ -1055,31 +1146,46 @@ void Engine::enqueue_step(bool respect, cudaEvent_t* ev, int64_t q, int64_t g) {
     }
 }
 
-template <int ACC, bool ONE, int B>
-static void launch_step_mixed_t(const DP& P, bool drift, unsigned chunks, cudaStream_t st) {
+template <int ACC, bool ONE, int B, bool TRACE>
+static void launch_step_mixed_tt(const DP& P, bool drift, unsigned chunks, cudaStream_t st) {
     if (drift)
-        k_step_mixed<ACC, ONE, B, true><<<chunks, 256, 0, st>>>(P);
+        k_step_mixed<ACC, ONE, B, true, TRACE><<<chunks, 256, 0, st>>>(P);
     else
-        k_step_mixed<ACC, ONE, B, false><<<chunks, 256, 0, st>>>(P);
+        k_step_mixed<ACC, ONE, B, false, TRACE><<<chunks, 256, 0, st>>>(P);
+}
+template <int ACC, bool ONE, int B>
+static void launch_step_mixed_t(const DP& P, bool drift, bool trace, unsigned chunks, cudaStream_t st) {
+    if (trace)
+        launch_step_mixed_tt<ACC, ONE, B, true>(P, drift, chunks, st);
+    else
+        launch_step_mixed_tt<ACC, ONE, B, false>(P, drift, chunks, st);
+}
+
+void Engine::launch_step_end(int mode) {
+    if (d_->exact_sums)
+        LAUNCH(k_step_end<true>, (unsigned)opt_.max_slots, END_THREADS, *d_, mode);
+    else
+        LAUNCH(k_step_end<false>, (unsigned)opt_.max_slots, END_THREADS, *d_, mode);
 }
 
 void Engine::launch_step_mixed(bool drift) {
     const unsigned ch = (unsigned)max_chunks_;
     const bool b8 = opt_.mix_batch == 8;
+    const bool tr = thermo_slots_ > 0;
     if (opt_.mixed_kahan) {
         if (single_type_)
-            b8 ? launch_step_mixed_t<1, true, 8>(*d_, drift, ch, stream_)
-               : launch_step_mixed_t<1, true, 4>(*d_, drift, ch, stream_);
+            b8 ? launch_step_mixed_t<1, true, 8>(*d_, drift, tr, ch, stream_)
+               : launch_step_mixed_t<1, true, 4>(*d_, drift, tr, ch, stream_);
         else
-            b8 ? launch_step_mixed_t<1, false, 8>(*d_, drift, ch, stream_)
-               : launch_step_mixed_t<1, false, 4>(*d_, drift, ch, stream_);
+            b8 ? launch_step_mixed_t<1, false, 8>(*d_, drift, tr, ch, stream_)
+               : launch_step_mixed_t<1, false, 4>(*d_, drift, tr, ch, stream_);
     } else {
         if (single_type_)
-            b8 ? launch_step_mixed_t<0, true, 8>(*d_, drift, ch, stream_)
-               : launch_step_mixed_t<0, true, 4>(*d_, drift, ch, stream_);
+            b8 ? launch_step_mixed_t<0, true, 8>(*d_, drift, tr, ch, stream_)
+               : launch_step_mixed_t<0, true, 4>(*d_, drift, tr, ch, stream_);
         else
-            b8 ? launch_step_mixed_t<0, false, 8>(*d_, drift, ch, stream_)
-               : launch_step_mixed_t<0, false, 4>(*d_, drift, ch, stream_);
+            b8 ? launch_step_mixed_t<0, false, 8>(*d_, drift, tr, ch, stream_)
+               : launch_step_mixed_t<0, false, 4>(*d_, drift, tr, ch, stream_);
     }
     g_launches.fetch_add(1);
 }
@@ -1094,7 +1200,7 @@ void Engine::enqueue_potential(int only) {
         launch_force_mixed(0);
     else
         launch_force_fp64(0);
-    LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 1);
+    launch_step_end(1);
 }
 
 // Inside a stream capture of stream_: a 1-thread kernel sets the condition from the rebuild word,
@@ -1176,13 +1282,13 @@ pis_status Engine::compute_potential_slots(const std::vector<int>& slots, std::s
         launch_force_mixed(0);
     else
         launch_force_fp64(0);
-    LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 1);
+    launch_step_end(1);
     for (int s : slots) LAUNCH(k_mark_eval, sg, 128, P, s, 0, 1);
     if (opt_.precision == PIS_PRECISION_MIXED)
         LAUNCH((k_integrate2<false, false>), (unsigned)max_chunks_, opt_.blk, P, 0);
     else
         LAUNCH((k_integrate2<false, true>), (unsigned)max_chunks_, opt_.blk, P, 0);
-    LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 2);
+    launch_step_end(2);
     st = check(cudaGetLastError(), "launch", err);
     if (st) return st;
     return sync(err);
@@ -1190,17 +1296,17 @@ pis_status Engine::compute_potential_slots(const std::vector<int>& slots, std::s
 
 pis_status Engine::reduce_state(bool virial, std::string& err) { return reduce_state_slot(virial, -1, err); }
 
-pis_status Engine::reduce_state_slot(bool virial, int only, std::string& err) {
+pis_status Engine::reduce_state_slot(bool virial, int only, std::string& err, bool ktensor) {
     pis_status st = rebuild_block_map(err);
     if (st) return st;
     const DP& P = *d_;
     const unsigned sg = (unsigned)((opt_.max_slots + 127) / 128);
-    LAUNCH(k_mark_eval, sg, 128, P, only, 0, virial ? 1 : 0);
+    LAUNCH(k_mark_eval, sg, 128, P, only, 0, (virial ? 1 : 0) | (ktensor ? 2 : 0));
     if (opt_.precision == PIS_PRECISION_MIXED)
         LAUNCH((k_integrate2<false, false>), (unsigned)max_chunks_, opt_.blk, P, 0);
     else
         LAUNCH((k_integrate2<false, true>), (unsigned)max_chunks_, opt_.blk, P, 0);
-    LAUNCH(k_step_end, (unsigned)opt_.max_slots, END_THREADS, P, 2);
+    launch_step_end(2);
     st = check(cudaGetLastError(), "launch", err);
     if (st) return st;
     return sync(err);
@@ -1217,7 +1323,8 @@ pis_status Engine::run(int64_t k, std::string& err) {
     const int64_t G = graph_steps_;
     while (k > 0) {
         int64_t g = k >= G ? G : k;
-        int64_t key = 2 * g + (instrument_ ? 1 : 0);
+        // graphs differ by length, instrumentation and whether the fused step records thermo
+        int64_t key = 4 * g + (instrument_ ? 1 : 0) + (thermo_slots_ > 0 ? 2 : 0);
         auto it = graphs_.find(key);
         if (it == graphs_.end()) {
             GraphRec rec;
@@ -1322,6 +1429,11 @@ pis_status Engine::read_states(std::vector<SysState>& out, std::string& err) {
 }
 
 pis_status Engine::set_thermo(int slot, bool on, std::string& err) {
+    if (slot_thermo_.size() != hp_.size()) slot_thermo_.assign(hp_.size(), 0);
+    if (slot_thermo_[slot] != (on ? 1 : 0)) {
+        thermo_slots_ += on ? 1 : -1;
+        slot_thermo_[slot] = on ? 1 : 0;
+    }
     const int32_t v = on ? 1 : 0;
     pis_status st = check(cudaMemcpyAsync(&d_->st[slot].thermo, &v, 4, cudaMemcpyHostToDevice, stream_), "thermo", err);
     if (st) return st;
@@ -1616,56 +1728,67 @@ pis_status Engine::grow_list(int64_t new_cap, std::string& err) {
 }
 
 pis_status Engine::scale_velocities(int slot, const double* m, std::string& err) {
-    LAUNCH(k_scale_vel, (unsigned)max_chunks_, opt_.blk, *d_, slot, m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8]);
+    Mat3Arg M;
+    for (int k = 0; k < 9; ++k) M.m[k] = m[k];
+    LAUNCH(k_scale_vel, (unsigned)max_chunks_, opt_.blk, *d_, slot, M);
     pis_status st = check(cudaGetLastError(), "scale velocities", err);
     if (st) return st;
     return sync(err);
 }
 
+// Atoms::scale_box (src/atoms/transformations.rs:5-16): h <- M h, h^-1 <- inverse(h), positions
+// carried in fractional coordinates. The cell grid keeps its counts (the pool's cell ranges are
+// fixed); the box may not shrink below one list radius per cell. Everything is checked before any
+// state changes.
 pis_status Engine::scale_box(int slot, const double* m, std::string& err) {
-    for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b)
-            if (a != b && m[3 * a + b] != 0.0) {
-                err = "box scaling must keep the box orthorhombic (diagonal matrix)";
-                return PIS_ERR_UNSUPPORTED;
-            }
     SysParams p = hp_[slot];
-    const double oh[3] = {p.hinv[0], p.hinv[1], p.hinv[2]};
-    double nh[3] = {m[0] * p.h[0], m[4] * p.h[1], m[8] * p.h[2]};
-    double rl = slot_rlist_[slot];
-    for (int a = 0; a < 3; ++a)
-        if (!(nh[a] > 2.0 * rl)) {
+    double nh[9], nhi[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c)
+            nh[3 * r + c] = m[3 * r] * p.H[c] + m[3 * r + 1] * p.H[3 + c] + m[3 * r + 2] * p.H[6 + c];
+    if (!inverse3_ref(nh, nhi)) {
+        err = "scaled box matrix is singular";
+        return PIS_ERR_INVALID_ARGUMENT;
+    }
+    if (!diagonal_box(nh) && !triclinic_capable()) {
+        err = "box scaling that tilts the box needs the FP64 path with exact arithmetic, one thread per atom";
+        return PIS_ERR_UNSUPPORTED;
+    }
+    const double rl = slot_rlist_[slot];
+    double w[3];
+    box_widths(nh, w);
+    for (int a = 0; a < 3; ++a) {
+        if (!(w[a] > 2.0 * rl)) {
             err = "scaled box is shorter than 2 (rcut + skin)";
             return PIS_ERR_BOX_TOO_SMALL;
         }
-    // new h and h^-1; the cell grid keeps its counts, the cell edge follows the box
-    for (int a = 0; a < 3; ++a) {
-        p.h[a] = nh[a];
-        p.cs[a] = nh[a] / p.nc[a];
-        p.fcs[a] = (float)p.cs[a];
-        p.fsub[a] = (float)(4.0 / p.cs[a]);
-    }
-    p.hinv[0] = (p.h[1] * p.h[2]) / (p.h[0] * (p.h[1] * p.h[2]));
-    p.hinv[1] = (p.h[0] * p.h[2]) / (p.h[0] * (p.h[1] * p.h[2]));
-    p.hinv[2] = (p.h[0] * p.h[1]) / (p.h[0] * (p.h[1] * p.h[2]));
-    for (int a = 0; a < 3; ++a)
-        if (p.cs[a] < rl) {
+        if (w[a] / p.nc[a] < rl) {
             err = "box shrank below the cell size; re-create the state to re-grid";
             return PIS_ERR_UNSUPPORTED;
         }
-    {
-        const double hm[9] = {p.h[0], 0.0, 0.0, 0.0, p.h[1], 0.0, 0.0, 0.0, p.h[2]};
-        reference_cells(hm, slot_rcmax_[slot], p.rnc);
-        if (opt_.ref_order && !reference_cells_ok(p.rnc)) {
-            err = "reference-order forces need at least 3 cells of the largest cutoff per axis";
-            return PIS_ERR_UNSUPPORTED;
-        }
+    }
+    if (!diagonal_box(nh) && (p.nc[0] < 3 || p.nc[1] < 3 || p.nc[2] < 3)) {
+        err = "a triclinic box needs at least 3 cells of the list radius across each pair of faces";
+        return PIS_ERR_BOX_TOO_SMALL;
+    }
+    Mat3Arg hi_old, h_new;
+    for (int k = 0; k < 9; ++k) {
+        hi_old.m[k] = p.HI[k];
+        h_new.m[k] = nh[k];
+    }
+    const int full = (p.tric || !diagonal_box(nh)) ? 1 : 0;
+    set_box(p, nh, nhi);
+    reference_cells(nh, slot_rcmax_[slot], p.rnc);
+    if (opt_.ref_order && !reference_cells_ok(p.rnc)) {
+        err = "reference-order forces need at least 3 cells of the largest cutoff per axis";
+        return PIS_ERR_UNSUPPORTED;
     }
     // the 27-cell walk's two-cell condition (add_slot) for the new edges
     p.walk27 = 1;
     for (int a = 0; a < 3; ++a)
         if (p.nc[a] < 2 || (p.nc[a] == 2 && !(p.h[a] > 2.0 * std::sqrt((double)p.frlist2) * (1.0 + 1e-5)))) p.walk27 = 0;
-    LAUNCH(k_scale_pos, (unsigned)max_chunks_, opt_.blk, *d_, slot, oh[0], oh[1], oh[2], nh[0], nh[1], nh[2]);
+    LAUNCH(k_scale_pos, (unsigned)max_chunks_, opt_.blk, *d_, slot, hi_old, h_new, full);
+    if (p.tric && !any_tric_) dirty_map_ = true;  // the next launch selects the triclinic kernels
     hp_[slot] = p;
     pis_status st = check(cudaMemcpyAsync(d_->sp + slot, &hp_[slot], sizeof(SysParams), cudaMemcpyHostToDevice, stream_),
                           "params", err);

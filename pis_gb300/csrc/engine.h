@@ -31,7 +31,7 @@ struct SlotDesc {
     int n_types = 1;
     std::vector<LJHost> table;      // n_types * n_types
     std::vector<double> masses;     // per type
-    double h[9] = {0};              // row-major box matrix (must be diagonal)
+    double h[9] = {0};              // row-major box matrix (diagonal, or general on the FP64 path)
     int pbc[3] = {1, 1, 1};
     double skin = 0.3;
     double dt = 0.005;
@@ -61,6 +61,10 @@ struct SysParams {
     float fsub[3];     // 4 / cell edge: sub-cell index scale of the in-cell atom order
     int32_t walk27;    // the 27-cell walk of the thread-per-atom build is valid (see add_slot)
     int32_t rnc[3];    // the reference's own cell grid at the largest cutoff (reference-order forces)
+    int32_t tric;      // the box has off-diagonal elements (FP64 path only): H / HI below are used
+    double H[9];       // row-major box matrix (columns = box vectors) and its inverse (adjugate /
+    double HI[9];      // determinant, as the reference's 3x3 inverse); diagonal boxes use h / hinv
+    float fcv[9];      // triclinic cell edge vectors: column d of H / nc[d] in fcv[3d..3d+2]
 };
 
 // Device-side pair parameters: FP64 quantities computed exactly as the reference does per pair,
@@ -86,6 +90,7 @@ struct SysState {
     int64_t rebuilds;
     double pe, ke;
     double virial[9];
+    double ktensor[9];    // sum_i v_i v_i^T (Atoms::kinetic_tensor, no masses), on request
 };
 
 enum : int32_t { FLAG_NAN = 1, FLAG_LIST_OVERFLOW = 2, FLAG_CELL_OVERFLOW = 4, FLAG_TIMEOUT = 8 };
@@ -114,6 +119,7 @@ struct PoolOptions {
     bool unfused = false;      // mixed, default kernel shape: separate force, kick and drift kernels
                                // (otherwise one fused step kernel does all three)
     bool ref_order = false;    // FP64, full list: forces summed in the reference's own order
+    int64_t wait_limit = -1;   // polls of a bulk-copy pipeline wait (< 0: the default, 2^22)
 };
 
 class Engine {
@@ -130,6 +136,8 @@ class Engine {
     void remove_slot(int slot);
     // Ask whether a system of this shape fits in the free space right now.
     bool fits(const SlotDesc& d) const;
+    // Cells of a system's list grid (at rcut + skin across each pair of box faces).
+    static int64_t cells_for(const SlotDesc& d);
     int64_t list_cap() const { return opt_.cluster ? ccap_ : cap_; }
     int cluster_size() const { return opt_.cluster; }
     int precision() const { return opt_.precision; }
@@ -147,7 +155,7 @@ class Engine {
     pis_status run(int64_t k, std::string& err);
     // KE and virial of every active slot at the current state.
     pis_status reduce_state(bool virial, std::string& err);
-    pis_status reduce_state_slot(bool virial, int slot, std::string& err);
+    pis_status reduce_state_slot(bool virial, int slot, std::string& err, bool ktensor = false);
     pis_status sync(std::string& err);
 
     pis_status download(int slot, double* pos, double* vel, double* force, std::string& err);
@@ -169,6 +177,11 @@ class Engine {
     pis_status restore_state(int slot, std::string& err);
     pis_status grow_list(int64_t new_cap, std::string& err);
     bool per_atom_list() const { return !opt_.cluster; }
+    // General (triclinic) boxes are supported by the FP64 path with exact arithmetic, one thread
+    // per atom and per-atom lists.
+    bool triclinic_capable() const {
+        return opt_.precision == PIS_PRECISION_FP64 && !opt_.fp64_fast && opt_.lpa == 1 && !opt_.cluster && !clm_;
+    }
     pis_status scale_velocities(int slot, const double* m, std::string& err);
     pis_status scale_box(int slot, const double* m, std::string& err);
     const SysParams& params(int slot) const { return hp_[slot]; }
@@ -203,6 +216,7 @@ class Engine {
     void launch_force_fp64(int respect_steps);
     void launch_force_mixed(int respect_steps);
     void launch_step_mixed(bool drift);
+    void launch_step_end(int mode);
     void launch_build(int respect_steps);
     void launch_force_cluster(int respect_steps);
     pis_status check(cudaError_t e, const char* what, std::string& err);
@@ -249,9 +263,12 @@ class Engine {
     int64_t kernels_per_step_ = 0;
     bool dirty_map_ = true;
     bool single_type_ = true;  // every active slot has one atom type (selects the force kernel)
+    bool any_tric_ = false;    // some active slot has a triclinic box (selects the rebuild kernels)
     bool fused_ = false;       // mixed steps run the fused force + kick + drift kernel
     bool list_groups_ = false; // the per-atom list is stored in groups of consecutive entries
     void* prel_buf_[2] = {nullptr, nullptr};  // the two cell-relative coordinate buffers (fused steps)
+    int thermo_slots_ = 0;             // slots whose steps record thermo (selects the fused kernel)
+    std::vector<int> slot_thermo_;
     void* nbr_own_ = nullptr;   // a grown neighbour list (allocated apart from the pool)
     void* save_ = nullptr;      // checkpoint of one slot's per-atom arrays (allocated on first use)
     int save_slot_ = -1;

@@ -3,7 +3,7 @@
 // System::contextualize (:100-175) builds the velocities and the LJ table, Simulation::run
 // (src/simulation.rs:8-88) steps the ensemble, prints thermo lines and writes .lammpstrj dumps
 // (src/writers/dump_traj.rs:18-74). NVE and the Nose-Hoover-chain NVT (src/ensemble/nvt.rs) run;
-// NPT needs a triclinic box update, which the GPU engine does not support.
+// NPT runs on the FP64 path, whose engine supports the triclinic boxes the barostat produces.
 #include <algorithm>
 #include <cerrno>
 #include <cmath>
@@ -83,6 +83,100 @@ struct Nhc {
         t_target = t_start + ((t_end - t_start) / (double)steps) * (double)step;
     }
 };
+
+// ---- 3x3 matrices (row-major) for the MTK barostat ------------------------------------------------
+void m3_mul(const double* a, const double* b, double* c) {
+    for (int r = 0; r < 3; ++r)
+        for (int k = 0; k < 3; ++k) c[3 * r + k] = a[3 * r] * b[k] + a[3 * r + 1] * b[3 + k] + a[3 * r + 2] * b[6 + k];
+}
+// math::symmetrize: (A + A^T) * 0.5
+void m3_sym(const double* a, double* out) {
+    double t[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) t[3 * r + c] = (a[3 * r + c] + a[3 * c + r]) * 0.5;
+    std::memcpy(out, t, sizeof(t));
+}
+// Matrix exponential by scaling and squaring of a Taylor series: A / 2^s with a 1-norm at most 1/4,
+// terms until they fall below 1e-18 (at most 30), then s squarings. The barostat's arguments are
+// symmetric and small (|A| ~ dt / tau_p), where this is exact to rounding.
+void m3_exp(const double* a, double* out) {
+    double norm = 0.0;
+    for (int c = 0; c < 3; ++c) norm = std::max(norm, std::fabs(a[c]) + std::fabs(a[3 + c]) + std::fabs(a[6 + c]));
+    int sq = 0;
+    while (norm > 0.25 && sq < 60) {
+        norm *= 0.5;
+        ++sq;
+    }
+    const double scale = std::ldexp(1.0, -sq);
+    double b[9], term[9], sum[9], tmp[9];
+    for (int k = 0; k < 9; ++k) {
+        b[k] = a[k] * scale;
+        term[k] = (k % 4 == 0) ? 1.0 : 0.0;
+        sum[k] = term[k];
+    }
+    for (int n = 1; n <= 30; ++n) {
+        m3_mul(term, b, tmp);
+        double tn = 0.0;
+        for (int k = 0; k < 9; ++k) {
+            term[k] = tmp[k] / n;
+            sum[k] += term[k];
+            tn = std::max(tn, std::fabs(term[k]));
+        }
+        if (tn < 1e-18) break;
+    }
+    for (int q = 0; q < sq; ++q) {
+        m3_mul(sum, sum, tmp);
+        std::memcpy(sum, tmp, sizeof(tmp));
+    }
+    std::memcpy(out, sum, sizeof(sum));
+}
+
+// MTKBarostat (src/ensemble/npt.rs:11-91): target pressure p_start I, momentum, mass
+// W = 3 N KB T tau^2 with T the thermostat's start temperature.
+struct Mtk {
+    double pt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double mom[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double w = 0.0;
+    void init(double p_start, double tau, int64_t n, double t_target) {
+        for (int k = 0; k < 9; ++k) pt[k] = (k % 4 == 0) ? p_start : 0.0;
+        w = ((double)(3 * n)) * KB * t_target * (tau * tau);
+    }
+    // delta_momentum (:42-47): symmetrize((P - P_target) * (V * 0.5 * dt))
+    void add_delta(const double* p, double vol, double dt) {
+        double d[9];
+        const double f = vol * 0.5 * dt;
+        for (int k = 0; k < 9; ++k) d[k] = (p[k] - pt[k]) * f;
+        m3_sym(d, d);
+        for (int k = 0; k < 9; ++k) mom[k] += d[k];
+    }
+    // scale (:49-56): exp(symmetrize(momentum / W) * factor * dt), factor -0.5 for velocities, 1 for the box
+    void scale(double dt, bool velocity, double* out) const {
+        double e[9];
+        for (int k = 0; k < 9; ++k) e[k] = mom[k] / w;
+        m3_sym(e, e);
+        const double factor = velocity ? -0.5 : 1.0;
+        for (int k = 0; k < 9; ++k) e[k] = e[k] * factor * dt;
+        m3_exp(e, out);
+    }
+    // kinetic_energy (:58-60): tr(M M^T) / (2 W); potential_energy (:62-64): tr(P_target^T h)
+    double kinetic_energy() const {
+        double d[3];
+        for (int r = 0; r < 3; ++r)
+            d[r] = mom[3 * r] * mom[3 * r] + mom[3 * r + 1] * mom[3 * r + 1] + mom[3 * r + 2] * mom[3 * r + 2];
+        return (d[0] + d[1] + d[2]) / (2.0 * w);
+    }
+    double potential_energy(const double* h) const {
+        double d[3];
+        for (int r = 0; r < 3; ++r) d[r] = pt[r] * h[r] + pt[3 + r] * h[3 + r] + pt[6 + r] * h[6 + r];
+        return d[0] + d[1] + d[2];
+    }
+};
+
+// |det h| by first-row cofactors (SimulationBox::volume, src/simulation_box.rs:67-69), row-major h
+double volume3(const double* m) {
+    return std::fabs(m[0] * (m[4] * m[8] - m[7] * m[5]) - m[1] * (m[3] * m[8] - m[6] * m[5]) +
+                     m[2] * (m[3] * m[7] - m[6] * m[4]));
+}
 
 }  // namespace
 
@@ -401,8 +495,8 @@ pis_status pis_system_run(pis_system* s, const char* thermo_path) {
         return sfail(s, PIS_ERR_MISSING_POTENTIAL, "Potential manager not initialized - missing pair_style or pair_coeff commands");
     if (!s->have_atoms) return sfail(s, PIS_ERR_NO_ATOMS, "No atoms defined in input file");
     const int ens = pis_system_ensemble(s);
-    if (ens == 2)
-        return sfail(s, PIS_ERR_UNSUPPORTED, "NPT needs a triclinic box update, which the GPU engine does not support");
+    if (ens == 2 && s->precision != PIS_PRECISION_FP64)
+        return sfail(s, PIS_ERR_UNSUPPORTED, "NPT tilts the box: it runs on the FP64 path");
     FILE* th = thermo_path ? std::fopen(thermo_path, "w") : stdout;
     if (!th) return sfail(s, PIS_ERR_IO, "cannot open thermo output");
     std::unique_ptr<FILE, int (*)(FILE*)> th_guard(thermo_path ? th : nullptr, [](FILE* f) { return f ? std::fclose(f) : 0; });
@@ -429,7 +523,25 @@ pis_status pis_system_run(pis_system* s, const char* thermo_path) {
     if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
     std::fprintf(th, "%d %s\n", 0, format_f64(pe).c_str());
     Nhc nhc;
-    if (ens == 1) nhc.init(s->nhc.t_start, s->nhc.t_end, s->nhc.tau);
+    if (ens >= 1) nhc.init(s->nhc.t_start, s->nhc.t_end, s->nhc.tau);
+    Mtk mtk;
+    if (ens == 2) mtk.init(s->mtk.p_start, s->mtk.tau, n, s->nhc.t_start);
+    // the current box, row-major (NPT changes it every step)
+    auto current_box = [&](double* hr) {
+        double hcm[9];
+        pis_status q = pis_gpu_get_box(s->ctx, hcm);
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) hr[3 * r + c] = hcm[3 * c + r];
+        return q;
+    };
+    // MTKBarostat::delta_momentum on the device's pressure tensor (src/ensemble/npt.rs:42-47)
+    auto barostat_kick = [&](double dtk) {
+        double pt[9], hr[9];
+        pis_status q = pis_gpu_pressure_tensor(s->ctx, pt);
+        if (!q) q = current_box(hr);
+        if (!q) mtk.add_delta(pt, volume3(hr), dtk);
+        return q;
+    };
     const double dt = s->timestep;
     if (ens == 0) {
         // NVE: runs of up to 1000 steps (or up to the next dump) with every step's PE, KE and virial
@@ -472,7 +584,20 @@ pis_status pis_system_run(pis_system* s, const char* thermo_path) {
     }
     for (int64_t i = 0; i < s->steps; ++i) {
         double ke = 0.0, w[9];
-        if (ens == 1) {
+        double sv[9];
+        if (ens == 2) {
+            // verlet_step_npt_mtk (src/potentials/potential.rs:112-135): barostat half kick, velocity
+            // and box scaling, the thermostatted step, velocity scaling, barostat half kick
+            st = barostat_kick(dt);
+            if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
+            double sh[9];
+            mtk.scale(dt, true, sv);
+            mtk.scale(dt, false, sh);
+            st = pis_gpu_scale_velocities(s->ctx, sv);
+            if (!st) st = pis_gpu_scale_box(s->ctx, sh);
+            if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
+        }
+        if (ens >= 1) {
             // verlet_step_nvt_nhc (src/potentials/potential.rs:35-58)
             st = pis_gpu_reductions(s->ctx, &ke, nullptr);
             if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
@@ -487,23 +612,34 @@ pis_status pis_system_run(pis_system* s, const char* thermo_path) {
             if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
             nhc.compute_forces(ke, n);
             nhc.propagate_half_step(dt);
+            if (ens == 2) {
+                st = pis_gpu_scale_velocities(s->ctx, sv);
+                if (!st) st = barostat_kick(dt);
+                if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
+            }
             nhc.target(i, s->steps);
         } else {
             st = pis_gpu_verlet_step_nve(s->ctx, dt, 1, &pe);
             if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
         }
+        double hr[9];
+        st = current_box(hr);
+        if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
+        const double hdiag[3] = {hr[0], hr[4], hr[8]};
         // Simulation::output (src/simulation.rs:66-88)
         if (s->dump_step > 0 && ((i + 1) % s->dump_step) == 0) {
             st = pis_gpu_get_state(s->ctx, pos.data(), nullptr, nullptr);
             if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
-            write_dump(dump, i + 1, n, d.type_ids.data(), pos.data(), h);
+            write_dump(dump, i + 1, n, d.type_ids.data(), pos.data(), hdiag);
         }
         st = pis_gpu_reductions(s->ctx, &ke, w);
         if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
+        // Simulation::compute_hamiltonian (src/simulation.rs:90-115)
         double ham = pe + ke;
-        if (ens == 1) ham += nhc.kinetic_energy() + nhc.potential_energy(n);
+        if (ens >= 1) ham = ham + nhc.kinetic_energy() + nhc.potential_energy(n);
+        if (ens == 2) ham = ham + mtk.kinetic_energy() + mtk.potential_energy(hr);
         const double temp = (2.0 * ke) / ((double)(3 * n) * KB);
-        const double press = (2.0 * ke + (w[0] + w[4] + w[8])) / (3.0 * vol);
+        const double press = (2.0 * ke + (w[0] + w[4] + w[8])) / (3.0 * (ens == 2 ? volume3(hr) : vol));
         std::fprintf(th, "%lld %.3f %.3f %.3f %.3f %.3f\n", (long long)(i + 1), pe, ke, ham, temp, press);
     }
     std::fflush(th);

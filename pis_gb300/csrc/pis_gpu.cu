@@ -31,6 +31,7 @@ struct pis_gpu_ctx {
     bool ref_order = false;
     int list_cap_req = 0;   // per-atom list capacity asked for (0 = from the density)
     bool auto_grow = true;  // grow the list and run again when it overflows
+    int64_t wait_limit = -1;  // polls of a bulk-copy pipeline wait (< 0: the default)
     std::unique_ptr<pis::Engine> eng;
     pis::PoolOptions pool;  // options the current engine was created with
     int slot = -1;
@@ -67,7 +68,7 @@ bool same_pool(const pis::PoolOptions& a, const pis::PoolOptions& b) {
            a.mixed_kahan == b.mixed_kahan && a.lpa == b.lpa && a.mix_batch == b.mix_batch &&
            a.list_tma == b.list_tma && a.cluster == b.cluster && a.build_cluster == b.build_cluster &&
            a.cell_tiles == b.cell_tiles && a.plain_graphs == b.plain_graphs &&
-           a.unfused == b.unfused && a.ref_order == b.ref_order;
+           a.unfused == b.unfused && a.ref_order == b.ref_order && a.wait_limit == b.wait_limit;
 }
 
 pis_status flags_to_status(pis_gpu_ctx* ctx, const pis::SysState& ss) {
@@ -233,14 +234,10 @@ pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_id
     opt.plain_graphs = ctx->plain_graphs;
     opt.unfused = ctx->unfused;
     opt.ref_order = ctx->ref_order;
+    opt.wait_limit = ctx->wait_limit;
     opt.max_atoms = n;
     opt.max_slots = 1;
-    int64_t ncell = 1;
-    for (int a = 0; a < 3; ++a) {
-        double q = std::floor(d.h[4 * a] / rlist);
-        ncell *= (int64_t)(q < 1 ? 1 : (q > 2000 ? 2000 : q));
-    }
-    opt.max_cells = ncell + 1;
+    opt.max_cells = pis::Engine::cells_for(d) + 1;
     opt.max_types_total = ctx->n_types * ctx->n_types;
     opt.list_cap = ctx->list_cap_req > 0 ? ctx->list_cap_req : list_capacity(n, d.h, rlist);
     std::string err;
@@ -267,6 +264,12 @@ pis_status pis_gpu_set_state(pis_gpu_ctx* ctx, int64_t n, const int32_t* type_id
     ctx->pool = opt;
     ctx->slot = slot;
     ctx->n = n;
+    return PIS_OK;
+}
+
+pis_status pis_gpu_set_wait_limit(pis_gpu_ctx* ctx, int64_t polls) {
+    if (!ctx) return PIS_ERR_INVALID_ARGUMENT;
+    ctx->wait_limit = polls;
     return PIS_OK;
 }
 
@@ -445,6 +448,33 @@ pis_status pis_gpu_scale_box(pis_gpu_ctx* ctx, const double* m) {
     std::string err;
     pis_status st = ctx->eng->scale_box(ctx->slot, m, err);
     return st ? fail(ctx, st, err) : PIS_OK;
+}
+
+pis_status pis_gpu_pressure_tensor(pis_gpu_ctx* ctx, double* p) {
+    if (!have_state(ctx)) return fail(ctx, PIS_ERR_STATE, "no atoms uploaded");
+    if (!p) return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "null output");
+    std::string err;
+    pis_status st = ctx->eng->reduce_state_slot(true, ctx->slot, err, true);
+    if (st) return fail(ctx, st, err);
+    pis::SysState ss;
+    st = ctx->eng->read_state(ctx->slot, ss, err);
+    if (st) return fail(ctx, st, err);
+    // SimulationBox::volume (src/simulation_box.rs:67-69): |det h| by first-row cofactors
+    const double* m = ctx->eng->params(ctx->slot).H;
+    const double det = m[0] * (m[4] * m[8] - m[7] * m[5]) - m[1] * (m[3] * m[8] - m[6] * m[5]) +
+                       m[2] * (m[3] * m[7] - m[6] * m[4]);
+    const double vol = std::fabs(det);
+    for (int q = 0; q < 9; ++q) p[q] = (ss.ktensor[q] + ss.virial[q]) / vol;
+    return PIS_OK;
+}
+
+pis_status pis_gpu_get_box(pis_gpu_ctx* ctx, double* h_colmajor) {
+    if (!have_state(ctx)) return fail(ctx, PIS_ERR_STATE, "no atoms uploaded");
+    if (!h_colmajor) return fail(ctx, PIS_ERR_INVALID_ARGUMENT, "null output");
+    const double* m = ctx->eng->params(ctx->slot).H;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) h_colmajor[3 * c + r] = m[3 * r + c];
+    return PIS_OK;
 }
 
 pis_status pis_gpu_get_stats(pis_gpu_ctx* ctx, pis_gpu_stats* out) {

@@ -26,7 +26,8 @@ class GpuContext:
 
     def __init__(self, table, n_types, skin=0.3, precision="fp64", list_kind="default", shift=True,
                  fp64_fast=False, mixed_kahan=False, lanes=0, batch=0, tma=False, cluster=0, scan=0, tiles=False,
-                 plain_graphs=False, unfused=False, ref_order=False, list_capacity=0, auto_grow=True):
+                 plain_graphs=False, unfused=False, ref_order=False, list_capacity=0, auto_grow=True,
+                 wait_limit=None):
         self._lib = _ffi.lib()
         self.n_types = int(n_types)
         pairs = (_ffi.LJPair * len(table))()
@@ -46,6 +47,8 @@ class GpuContext:
             self._check(self._lib.pis_gpu_set_options(self._h, _ffi.LIST_KIND[list_kind], flags))
         if list_capacity or not auto_grow:
             self._check(self._lib.pis_gpu_set_list_capacity(self._h, int(list_capacity), int(bool(auto_grow))))
+        if wait_limit is not None:
+            self._check(self._lib.pis_gpu_set_wait_limit(self._h, int(wait_limit)))
 
     def _check(self, st):
         if st != 0:
@@ -129,6 +132,18 @@ class GpuContext:
     def scale_box(self, m):
         mm = np.ascontiguousarray(m, dtype=np.float64).reshape(9)
         self._check(self._lib.pis_gpu_scale_box(self._h, _dp(mm)))
+
+    def pressure_tensor(self) -> np.ndarray:
+        """Atoms::pressure_tensor: (sum v v^T + sum r F^T) / volume (3x3)."""
+        p = np.zeros(9)
+        self._check(self._lib.pis_gpu_pressure_tensor(self._h, _dp(p)))
+        return p.reshape(3, 3)
+
+    def box(self) -> np.ndarray:
+        """The current box matrix h (3x3, columns = box vectors)."""
+        hc = np.zeros(9)
+        self._check(self._lib.pis_gpu_get_box(self._h, _dp(hc)))
+        return hc.reshape(3, 3).T.copy()
 
     def stats(self) -> dict:
         s = _ffi.Stats()
