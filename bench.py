@@ -75,8 +75,10 @@ def parse():
     p.add_argument("--no-batch", action="store_true", help="skip the 512-replica batched measurement")
     p.add_argument("--batch-steps", type=int, default=200)
     p.add_argument("--no-serve", action="store_true", help="skip the served-stream measurement")
-    p.add_argument("--serve-jobs", type=int, default=32)
+    p.add_argument("--serve-jobs", type=int, default=128)
+    p.add_argument("--serve-fp64-jobs", type=int, default=12)
     p.add_argument("--no-drift", action="store_true", help="skip the 10^4-step energy-drift runs")
+    p.add_argument("--no-driver", action="store_true", help="skip the input-file driver measurement")
     p.add_argument("--drift-steps", type=int, default=10000)
     p.add_argument("--mixed-options", default=None,
                    help='kernel variant of the mixed path as JSON (GpuContext keywords, e.g. '
@@ -198,25 +200,37 @@ def run_reference(args, rank, world):
     """The reference arm: the oracle's restatement of the reference's multithreaded manager
     (LJVParallelManager, src/potentials/lennard_jones.rs:253-336, OpenMP on all host cores) on the
     same workload. The start state is built without the GPU library (the oracle's copies of the
-    lattice order and of this project's velocity generator give the same arrays bit for bit) and
-    melted on the CPU for the same number of unreported steps as the GPU arm's melt (in FP64 here,
-    in mixed precision there: the same liquid statistically, not bit for bit)."""
+    lattice order and of this project's velocity generator) and melted on the CPU for the same
+    number of unreported steps as the GPU arm's melt (in FP64 here, in mixed precision there: the
+    same liquid statistically, not bit for bit). To keep the melt to seconds, a periodic block of
+    base^3 FCC cells (base the largest divisor of the cell count up to 20) is melted and tiled to
+    the full box: a periodic liquid tiled periodically is a liquid of the same density, temperature
+    and neighbour statistics."""
     if rank != 0:
         return
     import oracle
     oracle.build()
     threads = oracle.num_threads_available()
     a = (4.0 / RHO) ** (1.0 / 3.0)
-    pos = oracle.fcc_lattice(a, args.cells, args.cells, args.cells)
-    n = len(pos)
-    L = a * args.cells
-    vel = oracle.maxwell_boltzmann(np.ones(n), TSTAR / oracle.KB, 1)
-    s = oracle.System(pos, np.ones(n, np.int32), [1.0], np.eye(3) * L, TABLE, velocities=vel)
-    s.compute_potential(manager=oracle.PARALLEL, nthreads=threads)
+    base = max([d for d in range(8, 21) if args.cells % d == 0], default=args.cells)
+    pos0 = oracle.fcc_lattice(a, base, base, base)
+    n0 = len(pos0)
+    L0 = a * base
+    vel0 = oracle.maxwell_boltzmann(np.ones(n0), TSTAR / oracle.KB, 1)
+    s0 = oracle.System(pos0, np.ones(n0, np.int32), [1.0], np.eye(3) * L0, TABLE, velocities=vel0)
+    s0.compute_potential(manager=oracle.PARALLEL, nthreads=threads)
     t_melt = time.perf_counter()
     for _ in range(args.equil):
-        s.verlet_step_nve(DT, manager=oracle.PARALLEL, nthreads=threads)
+        s0.verlet_step_nve(DT, manager=oracle.PARALLEL, nthreads=threads)
     t_melt = time.perf_counter() - t_melt
+    rep = args.cells // base
+    shifts = np.array([(x, y, z) for x in range(rep) for y in range(rep) for z in range(rep)], dtype=np.float64) * L0
+    pos = (s0.pos[None, :, :] + shifts[:, None, :]).reshape(-1, 3)
+    vel = np.tile(s0.vel, (rep ** 3, 1))
+    n = len(pos)
+    L = L0 * rep
+    s = oracle.System(pos, np.ones(n, np.int32), [1.0], np.eye(3) * L, TABLE, velocities=vel)
+    s.compute_potential(manager=oracle.PARALLEL, nthreads=threads)
     # bounded sample: each step of the 2M-atom system costs ~0.5 s on 16 cores
     k = max(1, min(args.steps, 5))
     w = max(0, min(args.warmup, 3))
@@ -233,9 +247,9 @@ def run_reference(args, rank, world):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args, n),
         "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{k} NVE steps of the {n}-atom liquid melted on the CPU for {args.equil} steps "
-                                   f"({t_melt:.0f} s, untimed), after {w} warm-up step(s); LJVParallelManager "
-                                   "restated with OpenMP (oracle/pis_oracle.cpp)"},
+                         "sample": f"{k} NVE steps of the {n}-atom liquid ({base}^3-cell block melted on the CPU "
+                                   f"for {args.equil} steps in {t_melt:.1f} s and tiled {rep}^3, untimed), after {w} "
+                                   "warm-up step(s); LJVParallelManager restated with OpenMP (oracle/pis_oracle.cpp)"},
         "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -378,7 +392,8 @@ def main():
     drift = None if args.no_drift else run_drift(args, melt_pos, melt_vel, types, h, tuned)
     batched = None if args.no_batch else run_batched(args, rank, world)
     mix_errors = None if (args.no_batch or args.no_drift) else run_batch_errors(args, tuned)
-    served = None if (args.no_serve or rank != 0) else run_served(args)
+    served = None if (args.no_serve or rank != 0) else run_served(args, tuned)
+    driver = None if (args.no_driver or rank != 0) else run_driver(args, tuned)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -415,6 +430,7 @@ def main():
             "precision": "mixed",
             # details first; the figures the summary keys below restate come last on the line
             "served": served,
+            "driver": driver,
             "drift": drift,
             "batched_detail": batched,
             "batched_errors_vs_fp64": mix_errors,
@@ -485,14 +501,9 @@ def run_batched(args, rank, world):
     return out
 
 
-def run_batch_errors(args, tuned, count=6):
-    """Error of the mixed path against FP64 on representative replicas of the 512-replica mix (the
-    smallest and largest systems, the median one, and the hottest, coldest and densest of the rest):
-    each replica is admitted to an FP64 pool and to a mixed pool from the same seed; force RMS and
-    energy error at step 0, then 10^4 NVE steps in each with the total energy every 500 steps and its
-    drift per atom per 10^4 steps."""
-    from pis_gb300.batch import Batch, lj_pool_cells
-    jobs = batch_jobs(seed=2024)
+def representative(jobs, count=6):
+    """Indices of the smallest and largest systems, the median one, and the hottest, coldest and
+    densest of the rest."""
     order = sorted(range(len(jobs)), key=lambda r: jobs[r].k)
     pick = [order[0], order[-1], order[len(order) // 2]]
     for key in (lambda r: jobs[r].t_star, lambda r: -jobs[r].t_star, lambda r: jobs[r].rho):
@@ -500,19 +511,34 @@ def run_batch_errors(args, tuned, count=6):
             if r not in pick:
                 pick.append(r)
                 break
-    pick = pick[:count]
-    steps, chunk = args.drift_steps, 500
+    return pick[:count]
+
+
+def job_errors(jobs, pick, steps, tuned, chunk=500, melt=300):
+    """Error of the mixed path against FP64 on the jobs `pick`: each job's lattice start is melted
+    for `melt` steps in an FP64 pool (a perfect lattice has forces of ~1e-14, so errors relative to
+    them mean nothing); the melted state is admitted to an FP64 pool and to a mixed pool; force RMS
+    and energy error of their first evaluations, then `steps` NVE steps in each with the total
+    energy every `chunk` steps and its drift per atom per 10^4 steps."""
+    from pis_gb300.batch import Batch, lj_pool_cells
     sel = [jobs[r] for r in pick]
     atoms = sum(4 * j.k ** 3 for j in sel)
     cells = sum(lj_pool_cells(j.k, j.rho) for j in sel)
+    b = Batch(atoms + 1024, len(sel), cells + 1024, precision="fp64")
+    slots = [b.admit_lj(type(j)(j.k, j.rho, j.t_star, j.rcut, j.skin, j.dt, melt, j.seed)) for j in sel]
+    b.advance(melt)
+    melted = [b.result(sl, 4 * j.k ** 3) for sl, j in zip(slots, sel)]
+    b.close()
     res = {}
     for prec in ("fp64", "mixed"):
         kw = tuned if prec == "mixed" else {}
         b = Batch(atoms + 1024, len(sel), cells + 1024, precision=prec, **kw)
         slots = []
-        for j in sel:
-            j2 = type(j)(j.k, j.rho, j.t_star, j.rcut, j.skin, j.dt, steps, j.seed)
-            slots.append(b.admit_lj(j2))
+        for j, m in zip(sel, melted):
+            n = 4 * j.k ** 3
+            L = np.cbrt(4.0 / j.rho) * j.k
+            slots.append(b.admit(m["pos"], np.ones(n, np.int32), [1.0], np.eye(3) * L, {(1, 1): (1.0, 1.0, j.rcut)},
+                                 steps, velocities=m["vel"], skin=j.skin, dt=j.dt))
         first = [b.result(sl, 4 * j.k ** 3) for sl, j in zip(slots, sel)]
         series = [[f["pe"] + f["ke"]] for f in first]
         for _ in range(steps // chunk):
@@ -528,16 +554,22 @@ def run_batch_errors(args, tuned, count=6):
         f64, fm = res["fp64"][0][q], res["mixed"][0][q]
         d64 = drift_stats(np.array(res["fp64"][1][q]), n, chunk)["drift_per_atom_per_1e4_steps"]
         dm = drift_stats(np.array(res["mixed"][1][q]), n, chunk)["drift_per_atom_per_1e4_steps"]
-        reps.append({"replica": r, "atoms": n, "rho": j.rho, "t_star": j.t_star,
+        reps.append({"job": r, "atoms": n, "rho": j.rho, "t_star": j.t_star,
                      "force_rms_rel": float(np.sqrt(np.sum((fm["force"] - f64["force"]) ** 2) / np.sum(f64["force"] ** 2))),
                      "pe_rel": abs(fm["pe"] - f64["pe"]) / abs(f64["pe"]),
                      "drift_fp64": d64, "drift_mixed": dm})
-    summary = {"replicas": len(reps), "steps": steps,
+    summary = {"jobs": len(reps), "steps": steps, "melt_steps": melt,
                "max_force_rms_rel": max(x["force_rms_rel"] for x in reps),
                "max_pe_rel": max(x["pe_rel"] for x in reps),
                "max_abs_drift_mixed": max(abs(x["drift_mixed"]) for x in reps),
                "max_abs_drift_fp64": max(abs(x["drift_fp64"]) for x in reps)}
-    return {"per_replica": reps, "summary": summary}
+    return {"per_job": reps, "summary": summary}
+
+
+def run_batch_errors(args, tuned, count=6):
+    """Mixed against FP64 on representative replicas of the 512-replica mix, 10^4 NVE steps."""
+    jobs = batch_jobs(seed=2024)
+    return job_errors(jobs, representative(jobs, count), args.drift_steps, tuned)
 
 
 def energy_series(ctx, steps, chunk):
@@ -603,9 +635,9 @@ def run_drift(args, melt_pos, melt_vel, types, h, tuned):
     return out
 
 
-def serve_requests(count, seed=77, rate=200.0, step_scale=0.2):
+def serve_requests(count, seed=77, rate=200.0, step_scale=1.0):
     """Poisson arrivals (rate jobs/s) of LJ jobs: N log-uniform in [1000, 256000] rounded to 4 k^3,
-    rho* in U[0.70, 0.95], T* in U[0.5, 1.5], steps U[100, 5000] scaled by step_scale."""
+    rho* in U[0.70, 0.95], T* in U[0.5, 1.5], steps U[100, 5000] (times step_scale)."""
     import math
     from pis_gb300.batch import lj_job
     rng = np.random.default_rng(seed)
@@ -620,39 +652,102 @@ def serve_requests(count, seed=77, rate=200.0, step_scale=0.2):
     return reqs
 
 
-def run_served(args):
-    """Served stream with continuous batching (mixed precision, one pool) against the plain FP64
-    path serving the same requests one at a time."""
+def serve_stats(reqs, res, wall):
+    work = sum(4 * j.k ** 3 * j.steps for _, j in reqs)
+    lat = np.array([r["finished_s"] - r["arrival_s"] for r in res])
+    wait = np.array([r["admitted_s"] - r["arrival_s"] for r in res])
+    return {"jobs": len(reqs), "atom_steps": work, "atom_steps_per_s": work / wall, "wall_s": wall,
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "p50_queue_wait_s": float(np.percentile(wait, 50)), "p99_queue_wait_s": float(np.percentile(wait, 99)),
+            "all_ok": all(r["status"] == 0 for r in res)}
+
+
+def run_served(args, tuned):
+    """The served stream as stated: Poisson arrivals at 200 jobs/s, steps U[100, 5000], a fixed job
+    count; continuous batching on one mixed-precision pool (50-step graphs). The plain FP64 path
+    serves the first jobs of the same stream one at a time (a subset: one at a time it would take
+    minutes). An arrival-rate sweep runs a lighter stream (steps x 0.2) below and above saturation.
+    Mixed-precision error against FP64 on representative jobs of the stream, 10^4 steps each."""
     from pis_gb300.batch import Batch, lj_pool_cells
     reqs = serve_requests(args.serve_jobs)
     work = sum(4 * j.k ** 3 * j.steps for _, j in reqs)
-    offered = sum(4 * j.k ** 3 * j.steps for _, j in reqs) / max(reqs[-1][0], 1e-9)
-    out = {"jobs": len(reqs), "arrival_rate_per_s": 200.0, "step_scale": 0.2, "atom_steps": work,
-           "offered_atom_steps_per_s": offered}
+    out = {"jobs": len(reqs), "arrival_rate_per_s": 200.0, "step_scale": 1.0, "atom_steps": work,
+           "offered_atom_steps_per_s": work / max(reqs[-1][0], 1e-9), "graph_steps": 50}
     max_atoms = 4 * 40 ** 3 * 8
     max_cells = max(lj_pool_cells(j.k, j.rho) for _, j in reqs) * 16
-    for name, precision, slots in (("mixed_batched", "mixed", 64), ("fp64_one_at_a_time", "fp64", 1)):
-        b = Batch(max_atoms, slots, max_cells, precision=precision)
-        res, wall = b.serve(reqs, graph_steps=50)
-        b.close()
-        lat = np.array([r["finished_s"] - r["arrival_s"] for r in res])
-        ok = all(r["status"] == 0 for r in res)
-        out[name] = {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
-                     "atom_steps_per_s": work / wall, "wall_s": wall, "all_ok": ok}
-    # arrival-rate sweep of the continuous-batching path (a longer stream per rate)
+    b = Batch(max_atoms, 64, max_cells, precision="mixed")
+    res, wall = b.serve(reqs, graph_steps=50)
+    b.close()
+    out["mixed_batched"] = serve_stats(reqs, res, wall)
+    sub = reqs[:args.serve_fp64_jobs]
+    b = Batch(max_atoms, 1, max_cells, precision="fp64")
+    res, wall = b.serve(sub, graph_steps=50)
+    b.close()
+    out["fp64_one_at_a_time"] = serve_stats(sub, res, wall)
+    out["fp64_one_at_a_time"]["subset"] = f"the first {len(sub)} jobs of the stream"
+    # arrival-rate sweep of the continuous-batching path
     sweep = []
     for rate in (100.0, 200.0, 400.0, 800.0):
-        rq = serve_requests(4 * args.serve_jobs, seed=78, rate=rate)
+        rq = serve_requests(128, seed=78, rate=rate, step_scale=0.2)
         w = sum(4 * j.k ** 3 * j.steps for _, j in rq)
         cells = max(lj_pool_cells(j.k, j.rho) for _, j in rq) * 16
         b = Batch(max_atoms, 64, cells, precision="mixed")
         res, wall = b.serve(rq, graph_steps=50)
         b.close()
-        lat = np.array([r["finished_s"] - r["arrival_s"] for r in res])
-        sweep.append({"rate_per_s": rate, "jobs": len(rq), "offered_atom_steps_per_s": w / max(rq[-1][0], 1e-9),
-                      "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
-                      "atom_steps_per_s": w / wall, "all_ok": all(r["status"] == 0 for r in res)})
+        st = serve_stats(rq, res, wall)
+        st.update(rate_per_s=rate, step_scale=0.2, offered_atom_steps_per_s=w / max(rq[-1][0], 1e-9))
+        sweep.append(st)
     out["mixed_rate_sweep"] = sweep
+    if not args.no_drift:
+        jobs = [j for _, j in reqs]
+        out["errors_vs_fp64"] = job_errors(jobs, representative(jobs, 4), args.drift_steps, tuned)
+    return out
+
+
+def run_driver(args, tuned, steps=2000, dump_every=1000):
+    """The input-file driver (System::run on the GPU manager: a thermo line i PE KE H T P every step,
+    a LAMMPS dump every dump_every steps) against pis_gpu_verlet_step_nve with every step's energy
+    read back, both on the same melted 256,000-atom liquid, mixed precision, wall clock."""
+    import tempfile
+    from pis_gb300.io import System, write_data
+    from pis_gb300.lattice import lj_liquid
+    from pis_gb300.potentials import GpuContext
+    pos, vel, L = lj_liquid(40, RHO, TSTAR, 7)
+    n = len(pos)
+    types = np.ones(n, np.int32)
+    g = GpuContext(TABLE, 1, skin=SKIN, precision="mixed")
+    g.set_state(pos, types, [1.0], np.eye(3) * L, velocities=vel)
+    g.compute_potential(want_forces=False)
+    g.run_timed(DT, 500)
+    p, v, _ = g.get_state()
+    g.close()
+    out = {"atoms": n, "steps": steps, "thermo_every": 1, "dump_every": dump_every}
+    with tempfile.TemporaryDirectory() as d:
+        data = os.path.join(d, "liquid.txt")
+        write_data(data, p, types, [1.0], [0, L, 0, L, 0, L], TABLE, v)
+        inp = os.path.join(d, "in.pis")
+        with open(inp, "w") as fh:
+            fh.write(f"timestep {DT}\nread_data {data}\ndump d1 all atom {dump_every} {os.path.join(d, 'traj')}\n"
+                     f"run {steps}\n")
+        sysm = System(inp, precision="mixed", skin=SKIN)
+        t0 = time.perf_counter()
+        sysm.run(os.path.join(d, "thermo.txt"))
+        wall = time.perf_counter() - t0
+        with open(os.path.join(d, "thermo.txt")) as fh:
+            lines = sum(1 for _ in fh)
+        sysm.close()
+    out["driver"] = {"atom_steps_per_s": n * steps / wall, "wall_s": wall, "thermo_lines": lines}
+    g = GpuContext(TABLE, 1, skin=SKIN, precision="mixed")
+    g.set_state(p, types, [1.0], np.eye(3) * L, velocities=v)
+    g.compute_potential(want_forces=False)
+    g.verlet_step_nve(DT, 50)
+    t0 = time.perf_counter()
+    g.compute_potential(want_forces=False)
+    g.verlet_step_nve(DT, steps)
+    wall = time.perf_counter() - t0
+    g.close()
+    out["verlet_step_nve"] = {"atom_steps_per_s": n * steps / wall, "wall_s": wall}
+    out["driver_over_verlet_step_nve"] = out["driver"]["atom_steps_per_s"] / out["verlet_step_nve"]["atom_steps_per_s"]
     return out
 
 

@@ -45,7 +45,9 @@ pis_status pis_data_write(const char* path, int64_t n, int32_t n_types, const in
 pis_status pis_maxwell_boltzmann(int64_t n, const double* masses_per_atom, double temperature, uint64_t seed,
                                  double* vel);
 
-/* Format a double like Rust's `{}` (shortest round-trip decimal, no exponent) into buf. */
+/* Format a double like Rust's `{}` (shortest round-trip decimal, no exponent) into buf (at most
+ * buflen - 1 characters and a terminator); returns the full length (up to 342), so a call with
+ * buf = NULL sizes the buffer. */
 int32_t pis_format_f64(double v, char* buf, int32_t buflen);
 
 /* System::new(infile).read().contextualize() (src/system.rs:41-175), with the GPU manager in place

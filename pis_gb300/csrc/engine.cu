@@ -455,7 +455,7 @@ bool Engine::fits(const SlotDesc& d) const {
 }
 
 int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* pos, const double* vel,
-                     const double* force, std::string& err) {
+                     const double* force, std::string& err, bool defer_map) {
     if (d.n <= 0) {
         err = "no atoms defined";
         return -PIS_ERR_NO_ATOMS;
@@ -591,8 +591,10 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
         t.frc2 = (float)rc2;
         t.fucut = (float)ucut;
     }
-    pis_status st = check(cudaMemcpyAsync(d_->tab + tab0, tab.data(), sizeof(LJDev) * tab.size(),
-                                          cudaMemcpyHostToDevice, stream_),
+    // deferred placement: nothing waits for these copies, so their sources are held
+    auto src = [&](const void* q, size_t bytes) { return defer_map ? hold(q, bytes) : q; };
+    pis_status st = check(cudaMemcpyAsync(d_->tab + tab0, src(tab.data(), sizeof(LJDev) * tab.size()),
+                                          sizeof(LJDev) * tab.size(), cudaMemcpyHostToDevice, stream_),
                           "table upload", err);
     if (st) return -st;
 
@@ -664,10 +666,12 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     std::memset(&ss, 0, sizeof(ss));
     ss.cur = 0;
     ss.rebuild = 1;
+    ss.steps_left = d.steps > 0 ? d.steps : 0;
     std::vector<int32_t> csys(ncell + 1, slot);
-#define CP(dst, src, bytes)                                                                             \
+#define CP(dst, from, bytes)                                                                            \
     do {                                                                                                \
-        st = check(cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyHostToDevice, stream_), "upload", err); \
+        st = check(cudaMemcpyAsync((dst), src((from), (bytes)), (bytes), cudaMemcpyHostToDevice, stream_), \
+                   "upload", err);                                                                      \
         if (st) return -st;                                                                             \
     } while (0)
     CP(d_->pos[1] + a0, pos, 24 * d.n);
@@ -687,6 +691,7 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     CP(d_->st + slot, &ss, sizeof(ss));
 #undef CP
     dirty_map_ = true;
+    if (defer_map) return slot;
     st = rebuild_block_map(err);
     if (st) return -st;
     st = sync(err);
@@ -694,7 +699,7 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
     return slot;
 }
 
-void Engine::remove_slot(int slot) {
+void Engine::remove_slot(int slot, bool defer_map) {
     if (slot < 0 || slot >= opt_.max_slots || !hp_[slot].active) return;
     if ((int)slot_thermo_.size() > slot && slot_thermo_[slot]) {
         slot_thermo_[slot] = 0;
@@ -707,9 +712,11 @@ void Engine::remove_slot(int slot) {
     if (clm_) give_range(free_clusters_, p.cl0, p.clcap);
     for (int k = 0; k < slot_tab_size_[slot]; ++k) free_tab_[p.tab0 + k] = 1;
     std::vector<int32_t> csys(ncell + 1, -1);
-    cudaMemcpyAsync(d_->cell_sys + p.c0, csys.data(), 4 * (ncell + 1), cudaMemcpyHostToDevice, stream_);
+    cudaMemcpyAsync(d_->cell_sys + p.c0, defer_map ? hold(csys.data(), 4 * (ncell + 1)) : csys.data(),
+                    4 * (ncell + 1), cudaMemcpyHostToDevice, stream_);
     p.active = 0;
     dirty_map_ = true;
+    if (defer_map) return;
     std::string err;
     rebuild_block_map(err);
     cudaStreamSynchronize(stream_);
@@ -747,10 +754,10 @@ pis_status Engine::rebuild_block_map(std::string& err) {
             bf[c] = (int32_t)(p.a0 + (int64_t)k * opt_.blk);
         }
     }
-    pis_status st = check(cudaMemcpyAsync(d_->blk_sys, bs.data(), 4 * max_chunks_, cudaMemcpyHostToDevice, stream_),
+    pis_status st = check(cudaMemcpyAsync(d_->blk_sys, hold(bs.data(), 4 * max_chunks_), 4 * max_chunks_, cudaMemcpyHostToDevice, stream_),
                           "block map", err);
     if (st) return st;
-    st = check(cudaMemcpyAsync(d_->blk_first, bf.data(), 4 * max_chunks_, cudaMemcpyHostToDevice, stream_),
+    st = check(cudaMemcpyAsync(d_->blk_first, hold(bf.data(), 4 * max_chunks_), 4 * max_chunks_, cudaMemcpyHostToDevice, stream_),
                "block map", err);
     if (st) return st;
     // cluster kernels: every active slot gets ceil(cluster capacity / CL_THREADS) chunks
@@ -768,27 +775,29 @@ pis_status Engine::rebuild_block_map(std::string& err) {
                 cbf[q] = p.cl0 + k * CL_THREADS;
             }
         }
-        st = check(cudaMemcpyAsync(d_->cblk_sys, cbs.data(), 4 * max_cchunks_, cudaMemcpyHostToDevice, stream_),
+        st = check(cudaMemcpyAsync(d_->cblk_sys, hold(cbs.data(), 4 * max_cchunks_), 4 * max_cchunks_, cudaMemcpyHostToDevice, stream_),
                    "block map", err);
         if (st) return st;
-        st = check(cudaMemcpyAsync(d_->cblk_first, cbf.data(), 4 * max_cchunks_, cudaMemcpyHostToDevice, stream_),
+        st = check(cudaMemcpyAsync(d_->cblk_first, hold(cbf.data(), 4 * max_cchunks_), 4 * max_cchunks_, cudaMemcpyHostToDevice, stream_),
                    "block map", err);
         if (st) return st;
     }
-    st = check(cudaMemcpyAsync(d_->sp, hp_.data(), sizeof(SysParams) * hp_.size(), cudaMemcpyHostToDevice, stream_),
+    st = check(cudaMemcpyAsync(d_->sp, hold(hp_.data(), sizeof(SysParams) * hp_.size()), sizeof(SysParams) * hp_.size(), cudaMemcpyHostToDevice, stream_),
                "params", err);
     if (st) return st;
-    // host staging vectors must outlive the async copies
-    st = check(cudaStreamSynchronize(stream_), "block map", err);
+    // No synchronisation here (the sources are held), so a host loop can change the map while
+    // earlier graphs still run: the copies are ordered after them on the stream.
     dirty_map_ = false;
     // the force kernel variant depends on whether every slot is single-type; captured graphs
-    // bake that choice in, so they are dropped when it flips
+    // bake that choice in, so they are dropped when it flips (after the stream has drained)
     bool one = true, tric = false;
     for (int s = 0; s < opt_.max_slots; ++s) {
         if (hp_[s].active && hp_[s].nt != 1) one = false;
         if (hp_[s].active && hp_[s].tric) tric = true;
     }
     if (one != single_type_ || tric != any_tric_) {
+        st = check(cudaStreamSynchronize(stream_), "block map", err);
+        if (st) return st;
         single_type_ = one;
         any_tric_ = tric;
         for (auto& kv : graphs_) {
@@ -802,8 +811,26 @@ pis_status Engine::rebuild_block_map(std::string& err) {
 
 pis_status Engine::sync(std::string& err) {
     pis_status st = check(cudaStreamSynchronize(stream_), "stream sync", err);
-    if (!st) account_body_launches();
+    if (!st) {
+        account_body_launches();
+        held_.clear();
+    }
     return st;
+}
+
+const void* Engine::hold(const void* src, size_t bytes) {
+    if (!src || bytes == 0) return src;
+    held_.push_back(Held{held_seq_, std::vector<unsigned char>((const unsigned char*)src,
+                                                                (const unsigned char*)src + bytes)});
+    return held_.back().buf.data();
+}
+
+pis_status Engine::wait_event(cudaEvent_t e, std::string& err) {
+    return check(cudaEventSynchronize(e), "event wait", err);
+}
+
+void Engine::retire_staging(uint64_t mark) {
+    while (!held_.empty() && held_.front().seq < mark) held_.pop_front();
 }
 
 pis_status Engine::set_dt(int slot, double dt, std::string& err) {
@@ -1269,7 +1296,7 @@ pis_status Engine::compute_potential_slot(int only, std::string& err) {
 // Force evaluation and reductions for a set of slots (each marked, then one kernel sequence for
 // all): the serving loop evaluates the jobs it admits between two graphs together. Every slot's
 // results are those of compute_potential_slot on it alone.
-pis_status Engine::compute_potential_slots(const std::vector<int>& slots, std::string& err) {
+pis_status Engine::compute_potential_slots(const std::vector<int>& slots, std::string& err, bool wait) {
     if (slots.empty()) return PIS_OK;
     pis_status st = rebuild_block_map(err);
     if (st) return st;
@@ -1291,7 +1318,7 @@ pis_status Engine::compute_potential_slots(const std::vector<int>& slots, std::s
     launch_step_end(2);
     st = check(cudaGetLastError(), "launch", err);
     if (st) return st;
-    return sync(err);
+    return wait ? sync(err) : PIS_OK;
 }
 
 pis_status Engine::reduce_state(bool virial, std::string& err) { return reduce_state_slot(virial, -1, err); }
@@ -1418,6 +1445,13 @@ pis_status Engine::read_state(int slot, SysState& ss, std::string& err) {
     pis_status st = check(cudaMemcpyAsync(&ss, d_->st + slot, sizeof(SysState), cudaMemcpyDeviceToHost, stream_), "state", err);
     if (st) return st;
     return sync(err);
+}
+
+pis_status Engine::snapshot_states(SysState* host, cudaEvent_t done, std::string& err) {
+    pis_status st = check(cudaMemcpyAsync(host, d_->st, sizeof(SysState) * opt_.max_slots, cudaMemcpyDeviceToHost,
+                                          stream_), "state", err);
+    if (st) return st;
+    return check(cudaEventRecord(done, stream_), "state", err);
 }
 
 pis_status Engine::read_states(std::vector<SysState>& out, std::string& err) {

@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 #include <map>
+#include <deque>
 
 #include "pis_gpu.h"
 
@@ -35,6 +36,7 @@ struct SlotDesc {
     int pbc[3] = {1, 1, 1};
     double skin = 0.3;
     double dt = 0.005;
+    int64_t steps = 0;              // steps the slot takes in the following runs
 };
 
 // Device-side per-slot parameters (read-only inside kernels).
@@ -131,9 +133,12 @@ class Engine {
 
     pis_status init(const PoolOptions& opt, std::string& err);
     // Place a system in the pool. Returns the slot id (>= 0) or a negative pis_status.
+    // defer_map: leave the chunk map and the stream unsynchronised (the next evaluation or run
+    // rebuilds the map once for every slot placed or removed since), so a host loop can place and
+    // remove many slots between two graphs with one synchronisation.
     int add_slot(const SlotDesc& d, const int32_t* type_ids, const double* pos, const double* vel,
-                 const double* force, std::string& err);
-    void remove_slot(int slot);
+                 const double* force, std::string& err, bool defer_map = false);
+    void remove_slot(int slot, bool defer_map = false);
     // Ask whether a system of this shape fits in the free space right now.
     bool fits(const SlotDesc& d) const;
     // Cells of a system's list grid (at rcut + skin across each pair of box faces).
@@ -150,7 +155,18 @@ class Engine {
     // The same for one slot only (the others keep their state untouched).
     pis_status compute_potential_slot(int slot, std::string& err);
     // The same for several slots at once (one kernel sequence; each slot's results as alone).
-    pis_status compute_potential_slots(const std::vector<int>& slots, std::string& err);
+    // wait = false leaves the stream running (the caller's next launch or synchronisation follows)
+    // every slot's SysState copied to `host` (pinned, max_slots entries) after the work queued so
+    // far, then `done` recorded; nothing waits
+    pis_status snapshot_states(SysState* host, cudaEvent_t done, std::string& err);
+    // Host sources of uploads that no synchronisation follows (the map rebuild, deferred slot
+    // placement and removal) are copied here and kept until the stream has passed them: until the
+    // next sync(), or retire_staging(mark) once an event recorded after staging_mark() returned
+    // `mark` has completed.
+    uint64_t staging_mark() { return ++held_seq_; }
+    pis_status wait_event(cudaEvent_t e, std::string& err);
+    void retire_staging(uint64_t mark);
+    pis_status compute_potential_slots(const std::vector<int>& slots, std::string& err, bool wait = true);
     // Run k velocity-Verlet steps on every active slot with steps_left > 0 (graph chunks).
     pis_status run(int64_t k, std::string& err);
     // KE and virial of every active slot at the current state.
@@ -262,6 +278,13 @@ class Engine {
     int64_t stage_steps_ = 0;
     int64_t kernels_per_step_ = 0;
     bool dirty_map_ = true;
+    struct Held {
+        uint64_t seq;
+        std::vector<unsigned char> buf;
+    };
+    std::deque<Held> held_;  // upload sources kept until the stream has passed them
+    uint64_t held_seq_ = 0;
+    const void* hold(const void* src, size_t bytes);
     bool single_type_ = true;  // every active slot has one atom type (selects the force kernel)
     bool any_tric_ = false;    // some active slot has a triclinic box (selects the rebuild kernels)
     bool fused_ = false;       // mixed steps run the fused force + kick + drift kernel

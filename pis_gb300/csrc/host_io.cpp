@@ -1,6 +1,7 @@
 // host_io.cpp - data-file reader and writer, number parsing and formatting with the reference's
 // rules, and the Maxwell-Boltzmann velocity generator (include/pis_host.h).
 #include <cctype>
+#include <charconv>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -80,37 +81,62 @@ std::string trim(const std::string& s) {
 
 // Rust `{}` for f64: the shortest decimal that reads back to the same value, written without an
 // exponent ("1", "0.1", "-0", "123456789000000000000", "0.000001").
-std::string format_f64(double v) {
-    if (std::isnan(v)) return "NaN";
-    if (std::isinf(v)) return v > 0 ? "inf" : "-inf";
-    if (v == 0.0) return std::signbit(v) ? "-0" : "0";
-    char buf[64];
-    int prec = 1;
-    for (; prec <= 17; ++prec) {
-        std::snprintf(buf, sizeof buf, "%.*e", prec - 1, v);
-        if (std::strtod(buf, nullptr) == v) break;
+// Rust's `{}` for f64: the shortest digit string that parses back to the same value (among those,
+// the one nearest the value), written in positional notation without an exponent. The digits come
+// from std::to_chars in scientific form without a precision (a shortest round-trip conversion);
+// they are then placed around the decimal point. out holds at least 400 characters (the longest
+// case is a subnormal: "0.", 323 zeros and 17 digits); returns the length written.
+int format_f64_buf(double v, char* out) {
+    if (std::isnan(v)) return (int)(std::memcpy(out, "NaN", 3), 3);
+    if (std::isinf(v)) {
+        if (v > 0) return (int)(std::memcpy(out, "inf", 3), 3);
+        return (int)(std::memcpy(out, "-inf", 4), 4);
     }
-    // buf = [-]d.ddddde[+-]xx : digits and decimal exponent
-    std::string s(buf);
-    bool neg = s[0] == '-';
-    if (neg) s = s.substr(1);
-    size_t e = s.find('e');
-    int exp10 = std::atoi(s.c_str() + e + 1);
-    std::string digits;
-    for (size_t q = 0; q < e; ++q)
-        if (s[q] != '.') digits += s[q];
-    while (digits.size() > 1 && digits.back() == '0') digits.pop_back();
-    std::string out;
-    const int nd = (int)digits.size();
+    if (v == 0.0) {
+        if (std::signbit(v)) return (int)(std::memcpy(out, "-0", 2), 2);
+        out[0] = '0';
+        return 1;
+    }
+    char sci[40];
+    const auto r = std::to_chars(sci, sci + sizeof sci, v, std::chars_format::scientific);
+    const char* p = sci;
+    int len = 0;
+    if (*p == '-') {
+        out[len++] = '-';
+        ++p;
+    }
+    // p = d[.ddd]e[+-]xx
+    char digits[24];
+    int nd = 0;
+    const char* q = p;
+    for (; q < r.ptr && *q != 'e'; ++q)
+        if (*q != '.') digits[nd++] = *q;
+    // exponent: sign and digits up to r.ptr (to_chars writes no terminator)
+    int exp10 = 0;
+    const bool eneg = q + 1 < r.ptr && q[1] == '-';
+    for (const char* e = q + 2; e < r.ptr; ++e) exp10 = 10 * exp10 + (*e - '0');
+    if (eneg) exp10 = -exp10;
+    while (nd > 1 && digits[nd - 1] == '0') --nd;
     const int point = exp10 + 1;  // digits before the decimal point
     if (point <= 0) {
-        out = "0." + std::string(-point, '0') + digits;
+        out[len++] = '0';
+        out[len++] = '.';
+        for (int z = 0; z < -point; ++z) out[len++] = '0';
+        for (int z = 0; z < nd; ++z) out[len++] = digits[z];
     } else if (point >= nd) {
-        out = digits + std::string(point - nd, '0');
+        for (int z = 0; z < nd; ++z) out[len++] = digits[z];
+        for (int z = nd; z < point; ++z) out[len++] = '0';
     } else {
-        out = digits.substr(0, point) + "." + digits.substr(point);
+        for (int z = 0; z < point; ++z) out[len++] = digits[z];
+        out[len++] = '.';
+        for (int z = point; z < nd; ++z) out[len++] = digits[z];
     }
-    return neg ? "-" + out : out;
+    return len;
+}
+
+std::string format_f64(double v) {
+    char buf[400];
+    return std::string(buf, (size_t)format_f64_buf(v, buf));
 }
 
 std::string int_parse_message(const std::string& t) {

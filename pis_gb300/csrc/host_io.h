@@ -32,6 +32,7 @@ std::string open_error_message(const std::string& path, int os_errno);
 std::vector<std::string> split_ws(const std::string& line);
 std::string trim(const std::string& s);
 std::string format_f64(double v);
+int format_f64_buf(double v, char* out);  // out: >= 400 chars; returns the length
 pis_status read_data_file(const std::string& path, DataFile& d, std::string& err);
 void maxwell_boltzmann(int64_t n, const double* m, double temperature, uint64_t seed, double* v);
 

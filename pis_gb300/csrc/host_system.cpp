@@ -4,6 +4,7 @@
 // (src/simulation.rs:8-88) steps the ensemble, prints thermo lines and writes .lammpstrj dumps
 // (src/writers/dump_traj.rs:18-74). NVE and the Nose-Hoover-chain NVT (src/ensemble/nvt.rs) run;
 // NPT runs on the FP64 path, whose engine supports the triclinic boxes the barostat produces.
+#include <charconv>
 #include <algorithm>
 #include <cerrno>
 #include <cmath>
@@ -401,13 +402,31 @@ pis_status contextualize(pis_system* s) {
     return PIS_OK;
 }
 
+// DumpTraj::write_step (src/writers/dump_traj.rs:68-74): lines formatted into a buffer and written
+// in blocks of about 1 MB.
 void write_dump(std::ofstream& o, int64_t step, int64_t n, const int32_t* types, const double* pos, const double h[3]) {
     o << "ITEM: TIMESTEP\n" << step << "\nITEM: NUMBER OF ATOMS\n" << n << "\nITEM: BOX BOUNDS pp pp pp\n";
     for (int a = 0; a < 3; ++a) o << "0 " << format_f64(h[a]) << "\n";
     o << "ITEM: ATOMS id type x y z\n";
-    for (int64_t i = 0; i < n; ++i)
-        o << (i + 1) << " " << types[i] << " " << format_f64(pos[3 * i]) << " " << format_f64(pos[3 * i + 1]) << " "
-          << format_f64(pos[3 * i + 2]) << "\n";
+    std::vector<char> buf((size_t)1 << 21);
+    size_t len = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        if (len + 1300 > buf.size()) {  // room for a line of three maximal numbers
+            o.write(buf.data(), (std::streamsize)len);
+            len = 0;
+        }
+        char* p = buf.data() + len;
+        p = std::to_chars(p, p + 24, (long long)(i + 1)).ptr;
+        *p++ = ' ';
+        p = std::to_chars(p, p + 16, types[i]).ptr;
+        for (int a = 0; a < 3; ++a) {
+            *p++ = ' ';
+            p += pis::format_f64_buf(pos[3 * i + a], p);
+        }
+        *p++ = '\n';
+        len = (size_t)(p - buf.data());
+    }
+    o.write(buf.data(), (std::streamsize)len);
 }
 
 }  // namespace
@@ -517,7 +536,14 @@ pis_status pis_system_run(pis_system* s, const char* thermo_path) {
     if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
     const double vol = std::fabs(h[0] * (h[1] * h[2]));
     std::vector<double> pos(3 * n);
-    write_dump(dump, 0, n, d.type_ids.data(), d.pos.data(), h);
+    // the step-0 dump (the input's positions) is written while the first steps run
+    std::thread writer0([&dump, n, &d, h] { write_dump(dump, 0, n, d.type_ids.data(), d.pos.data(), h); });
+    struct Join {
+        std::thread& t;
+        ~Join() {
+            if (t.joinable()) t.join();
+        }
+    } join0{writer0};
     double pe = 0.0;
     st = pis_gpu_compute_potential(s->ctx, &pe, nullptr);
     if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
@@ -561,6 +587,7 @@ pis_status pis_system_run(pis_system* s, const char* thermo_path) {
                 return sfail(s, st, pis_gpu_last_error(s->ctx));
             }
             if (s->dump_step > 0 && ((i + k) % s->dump_step) == 0) {
+                if (writer0.joinable()) writer0.join();  // dumps are written in step order
                 if (writer.joinable()) writer.join();  // the buffer written two dumps ago is free again
                 st = pis_gpu_get_state(s->ctx, dump_pos[buf].data(), nullptr, nullptr);
                 if (st) return sfail(s, st, pis_gpu_last_error(s->ctx));
@@ -578,10 +605,12 @@ pis_status pis_system_run(pis_system* s, const char* thermo_path) {
             }
             i += k;
         }
+        if (writer0.joinable()) writer0.join();
         if (writer.joinable()) writer.join();
         std::fflush(th);
         return dump.good() ? PIS_OK : sfail(s, PIS_ERR_IO, "Failed to write trajectory file");
     }
+    if (writer0.joinable()) writer0.join();  // the thermostatted loop writes its dumps in line
     for (int64_t i = 0; i < s->steps; ++i) {
         double ke = 0.0, w[9];
         double sv[9];

@@ -107,14 +107,17 @@ pis::SlotDesc lj_desc(const pis_lj_job& j, double L) {
 
 // Place a job in the pool and set its step count; `evaluate`: also its first force evaluation
 // (otherwise the caller evaluates the new slots together, Engine::compute_potential_slots).
-pis_status place_desc(pis_batch* b, const pis::SlotDesc& d, const int32_t* types, const double* pos,
+pis_status place_desc(pis_batch* b, const pis::SlotDesc& d0, const int32_t* types, const double* pos,
                       const double* vel, int64_t steps, bool evaluate, int32_t* slot_out) {
     if (steps < 0) return bfail(b, PIS_ERR_INVALID_ARGUMENT, "negative step count");
     std::string err;
-    int slot = b->eng.add_slot(d, types, pos, vel, nullptr, err);
+    pis::SlotDesc d = d0;
+    d.steps = steps;
+    // without the evaluation (the serving loop): placed with the chunk map left for the next
+    // evaluation, which covers every job admitted between two graphs
+    int slot = b->eng.add_slot(d, types, pos, vel, nullptr, err, !evaluate);
     if (slot < 0) return bfail(b, (pis_status)(-slot), err);
     pis_status st = evaluate ? b->eng.compute_potential_slot(slot, err) : PIS_OK;
-    if (!st) st = b->eng.set_steps(slot, steps, err);
     if (st) {
         b->eng.remove_slot(slot);
         return bfail(b, st, err);
@@ -365,6 +368,63 @@ pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64
         const double now = seconds_since(t0);
         while (next < order.size() && reqs[order[next]].arrival_s <= now) queue.push_back(order[next++]);
     };
+    // Pipelined cycle: graph k+1 is queued before the state snapshot taken after graph k is read,
+    // so releases, admissions (host-side state generation, uploads, the map rebuild) and the
+    // evaluation of admitted jobs are prepared on the host while graph k+1 runs, and the work they
+    // queue follows it on the stream. A job is seen finished in the snapshot of the graph it
+    // finished in; slots placed after a graph was queued are not read from its snapshot.
+    const int S = b->opt.max_slots;
+    pis::SysState* snap[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    struct Cleanup {
+        pis::SysState** snap;
+        cudaEvent_t* ev;
+        ~Cleanup() {
+            for (int k = 0; k < 2; ++k) {
+                if (snap[k]) cudaFreeHost(snap[k]);
+                if (ev[k]) cudaEventDestroy(ev[k]);
+            }
+        }
+    } cleanup{snap, ev};
+    for (int k = 0; k < 2; ++k) {
+        if (cudaMallocHost((void**)&snap[k], sizeof(pis::SysState) * S) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            return bfail(b, PIS_ERR_NO_MEMORY, "pinned state snapshot");
+        }
+    }
+    std::vector<int64_t> placed_at(S, 0);  // first graph that steps each slot's current job
+    int64_t graphs = 0;                    // graphs queued so far
+    int inflight = -1;                     // snapshot buffer of the last graph queued and not read
+    uint64_t mark[2] = {0, 0};
+    int64_t snap_graph[2] = {0, 0};
+    auto read_snapshot = [&](int k) -> pis_status {
+        pis_status rs = b->eng.wait_event(ev[k], err);
+        if (rs) return rs;
+        b->eng.retire_staging(mark[k]);
+        const double t_done = seconds_since(t0);
+        const pis::SysState* ss = snap[k];
+        // finished jobs: energies and counters as their last step left them (the step end writes
+        // PE and KE every step); released with the chunk map rebuilt once, before the next graph
+        for (int s = 0; s < S; ++s) {
+            const int32_t q = slot_req[s];
+            if (q < 0 || placed_at[s] > snap_graph[k] || ss[s].steps_left > 0) continue;
+            out[q].finished_s = t_done;
+            out[q].pe = ss[s].pe;
+            out[q].ke = ss[s].ke;
+            out[q].steps = ss[s].steps_done;
+            out[q].status = (ss[s].flags & pis::FLAG_NAN)             ? PIS_ERR_NAN_DETECTED
+                            : (ss[s].flags & pis::FLAG_LIST_OVERFLOW) ? PIS_ERR_LIST_OVERFLOW
+                            : (ss[s].flags & pis::FLAG_TIMEOUT)       ? PIS_ERR_TIMEOUT
+                                                                      : PIS_OK;
+            b->eng.remove_slot(s, true);
+            b->atoms[s] = 0;
+            slot_req[s] = -1;
+            --active;
+            ++finished;
+        }
+        return PIS_OK;
+    };
     while (finished < n) {
         arrivals();
         // admit in arrival order while the head of the queue fits
@@ -390,52 +450,55 @@ pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64
                 continue;
             }
             slot_req[slot] = q;
+            placed_at[slot] = graphs + 1;
             fresh.push_back(slot);
             ++active;
         }
         if (!fresh.empty()) {
-            pis_status st = b->eng.compute_potential_slots(fresh, err);
+            // no synchronisation: the graph follows on the same stream
+            pis_status st = b->eng.compute_potential_slots(fresh, err, false);
             if (st) return bfail(b, st, err);
         }
-        if (active == 0) {
-            if (next < order.size()) {
-                const double wait = reqs[order[next]].arrival_s - seconds_since(t0);
-                if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
-            }
-            continue;
+        int queued = -1;
+        if (active > 0) {
+            pis_status st = b->eng.run(graph_steps, err);
+            if (st) return bfail(b, st, err);
+            queued = inflight == 0 ? 1 : 0;
+            ++graphs;
+            snap_graph[queued] = graphs;
+            mark[queued] = b->eng.staging_mark();
+            st = b->eng.snapshot_states(snap[queued], ev[queued], err);
+            if (st) return bfail(b, st, err);
         }
-        pis_status st = b->eng.run(graph_steps, err);
-        if (st) return bfail(b, st, err);
-        // while the graph runs: the initial states of the next queued jobs
-        arrivals();
-        {
+        if (inflight >= 0) {
+            pis_status st = read_snapshot(inflight);
+            if (st) return bfail(b, st, err);
+            inflight = -1;
+        }
+        if (queued >= 0) {
+            inflight = queued;
+            // while the graph runs: the initial states of the next queued jobs
+            arrivals();
             int k = 0;
             for (int32_t q : queue) {
                 if (k++ >= 8) break;
                 prepare(q);
             }
+            continue;
         }
-        std::vector<pis::SysState> ss;
-        st = b->eng.read_states(ss, err);  // synchronises with the graph
-        if (st) return bfail(b, st, err);
-        const double t_done = seconds_since(t0);
-        for (int s = 0; s < (int)ss.size(); ++s) {
-            const int32_t q = slot_req[s];
-            if (q < 0 || ss[s].steps_left > 0) continue;
-            double pe = 0, ke = 0;
-            int64_t steps = 0;
-            pis_status rs = pis_batch_result(b, s, nullptr, nullptr, nullptr, &pe, &ke, &steps);
-            out[q].finished_s = t_done;
-            out[q].pe = pe;
-            out[q].ke = ke;
-            out[q].steps = steps;
-            out[q].status = rs;
-            pis_batch_release(b, s);
-            slot_req[s] = -1;
-            --active;
-            ++finished;
+        // nothing running and nothing admitted: wait for the next arrival
+        if (next < order.size()) {
+            const double wait = reqs[order[next]].arrival_s - seconds_since(t0);
+            if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
         }
     }
+    if (inflight >= 0) {  // a last graph queued after every job had finished (it steps nothing)
+        pis_status st = read_snapshot(inflight);
+        if (st) return bfail(b, st, err);
+    }
+    std::string serr;
+    pis_status st = b->eng.sync(serr);
+    if (st) return bfail(b, st, serr);
     if (wall_s) *wall_s = seconds_since(t0);
     return PIS_OK;
 }

@@ -63,8 +63,9 @@ def write_data(path, positions, type_ids, masses, bounds, table=None, velocities
 
 
 def format_f64(v: float) -> str:
-    buf = C.create_string_buffer(64)
-    _ffi.lib().pis_format_f64(float(v), buf, 64)
+    n = _ffi.lib().pis_format_f64(float(v), None, 0)
+    buf = C.create_string_buffer(n + 1)
+    _ffi.lib().pis_format_f64(float(v), buf, n + 1)
     return buf.value.decode()
 
 

@@ -35,12 +35,13 @@ def to_oracle(sysd):
 
 def to_gpu(sysd, precision="fp64", skin=0.3, list_kind="default", fp64_fast=False, mixed_kahan=False, lanes=0,
            batch=0, tma=False, cluster=0, scan=0, tiles=False, plain_graphs=False,
-           unfused=False, ref_order=False, list_capacity=0, auto_grow=True):
+           unfused=False, ref_order=False, list_capacity=0, auto_grow=True, wait_limit=None):
     from pis_gb300.potentials import GpuContext
     ctx = GpuContext(sysd["table"], len(sysd["masses"]), skin=skin, precision=precision, list_kind=list_kind,
                      fp64_fast=fp64_fast, mixed_kahan=mixed_kahan, lanes=lanes, batch=batch, tma=tma,
                      cluster=cluster, scan=scan, tiles=tiles, plain_graphs=plain_graphs,
-                     unfused=unfused, ref_order=ref_order, list_capacity=list_capacity, auto_grow=auto_grow)
+                     unfused=unfused, ref_order=ref_order, list_capacity=list_capacity, auto_grow=auto_grow,
+                     wait_limit=wait_limit)
     ctx.set_state(sysd["pos"], sysd["types"], sysd["masses"], sysd["h"], velocities=sysd["vel"])
     return ctx
 

@@ -139,3 +139,41 @@ def test_nan_replica_fails_alone(cuda_lib):
     ref.advance(50)
     r2 = ref.result(s2, len(good["pos"]))
     assert np.array_equal(r["pos"], r2["pos"])
+
+
+@pytest.mark.parametrize("precision,opts", [("fp64", {}), ("mixed", {}),
+                                            ("mixed", dict(lanes=1, batch=4, mixed_kahan=True))])
+def test_slot_forces_equal_a_single_context(cuda_lib, precision, opts):
+    # the forces a slot returns after a run are the evaluation of its state: the same state in a
+    # single context gives the same forces, in every slot of a pool (after 50 steps from the
+    # lattice start, whose forces vanish by symmetry)
+    from pis_gb300.batch import Batch, lj_job
+    from pis_gb300.potentials import GpuContext
+    table = {(1, 1): (1.0, 1.0, 2.5)}
+    jobs = [lj_job(5, 0.88, 0.95, 50, 61), lj_job(9, 0.71, 1.5, 50, 62), lj_job(7, 0.94, 0.5, 50, 63)]
+    b = Batch(8000, 4, 0, precision=precision, **opts)
+    slots = [b.admit_lj(j) for j in jobs]
+    b.advance(50)
+    for j, sl in zip(jobs, slots):
+        n = 4 * j.k ** 3
+        r = b.result(sl, n)
+        L = np.cbrt(4.0 / j.rho) * j.k
+        g = GpuContext(table, 1, precision=precision, **opts)
+        g.set_state(r["pos"], np.ones(n, np.int32), [1.0], np.eye(3) * L, velocities=r["vel"])
+        pe, f = g.compute_potential()
+        g.close()
+        assert np.all(np.isfinite(r["force"]))
+        # FP64: the same pair terms (the half list's atomics add them in another order). Mixed:
+        # the pool's FP32 cell-relative coordinates are the build's plus the FP32 displacement
+        # since, a fresh context's are rounded from the FP64 positions, so the two are two mixed
+        # evaluations of one state, each within the mixed path's error of the FP64 forces
+        tol = 1e-12 if precision == "fp64" else 1e-5
+        assert np.linalg.norm(r["force"] - f) <= tol * np.linalg.norm(f), (j.k, precision)
+        assert abs(r["pe"] - pe) <= tol * abs(pe)
+        if precision == "mixed":
+            g64 = GpuContext(table, 1, precision="fp64")
+            g64.set_state(r["pos"], np.ones(n, np.int32), [1.0], np.eye(3) * L, velocities=r["vel"])
+            _, f64 = g64.compute_potential()
+            g64.close()
+            assert np.sqrt(np.sum((r["force"] - f64) ** 2) / np.sum(f64 ** 2)) <= 1e-5
+    b.close()

@@ -60,6 +60,16 @@ def test_format_round_trips(io):
         assert float(io.format_f64(v)) == v
 
 
+def test_format_is_the_shortest_positional(io):
+    # the shortest round-trip digits, nearest the value, positional: numpy's Dragon4 in unique mode
+    # gives the same string over the whole range (subnormals and the largest values included)
+    rng = np.random.default_rng(1)
+    vals = np.concatenate([rng.normal(0, 10, 300), 10.0 ** rng.uniform(-320, 308, 300) * rng.choice([-1, 1], 300),
+                           [5e-324, 2.2250738585072014e-308, 1.7976931348623157e308, 0.1, 0.3, 1 / 3]])
+    for v in vals:
+        assert io.format_f64(float(v)) == np.format_float_positional(v, unique=True, trim="-")
+
+
 def test_restart_round_trip(io, tmp_path):
     rng = np.random.default_rng(3)
     n = 50
