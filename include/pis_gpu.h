@@ -329,6 +329,18 @@ typedef struct {
 pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64_t graph_steps,
                          pis_request_result* out, double* wall_s);
 
+/* Accounting of the last pis_serve_run on a batch, per graph: atom-steps done (sum over slots of
+ * atoms x steps taken in the graph) and device seconds from the end of the previous graph to the
+ * end of this one (CUDA events; admissions, evaluations and any wait for the host included).
+ * "Saturated" graphs are those queued while a request was waiting for pool space: their rate is
+ * the served throughput at saturation, free of the stream's ramp-up and drain. */
+typedef struct {
+    int64_t graphs, saturated_graphs;
+    double atom_steps, device_s;
+    double saturated_atom_steps, saturated_device_s;
+} pis_serve_stats;
+pis_status pis_serve_last_stats(const pis_batch* b, pis_serve_stats* out);
+
 /* Number of kernel launches this library issued on the calling thread's contexts since load
  * (every kernel of this library, graph launches counted per contained kernel). */
 int64_t pis_gpu_kernel_launches(void);

@@ -74,6 +74,11 @@ class RequestResult(C.Structure):
                 ("pe", C.c_double), ("ke", C.c_double), ("status", C.c_int32)]
 
 
+class ServeStats(C.Structure):
+    _fields_ = [("graphs", C.c_int64), ("saturated_graphs", C.c_int64), ("atom_steps", C.c_double),
+                ("device_s", C.c_double), ("saturated_atom_steps", C.c_double), ("saturated_device_s", C.c_double)]
+
+
 _lib = None
 
 # (name, restype, argtypes) of every C-ABI entry point declared in include/pis_gpu.h
@@ -118,6 +123,7 @@ SIGNATURES = [
     ("pis_batch_last_error", C.c_char_p, [_VP]),
     ("pis_batch_destroy", None, [_VP]),
     ("pis_serve_run", C.c_int, [_VP, C.POINTER(Request), C.c_int32, C.c_int64, C.POINTER(RequestResult), _DP]),
+    ("pis_serve_last_stats", C.c_int, [_VP, C.POINTER(ServeStats)]),
     ("pis_gpu_kernel_launches", C.c_int64, []),
     ("pis_gpu_version", C.c_char_p, []),
 ]

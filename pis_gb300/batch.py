@@ -122,6 +122,17 @@ class Batch:
                 "status": out[q].status} for q in range(n)]
         return res, wall.value
 
+    def serve_stats(self) -> dict:
+        """Per-graph accounting of the last serve(): atom-steps and device seconds, over all graphs
+        and over the saturated ones (queued while a request waited for pool space)."""
+        st = _ffi.ServeStats()
+        self._check(self._lib.pis_serve_last_stats(self._h, C.byref(st)))
+        out = {f: getattr(st, f) for f, _ in _ffi.ServeStats._fields_}
+        out["atom_steps_per_device_s"] = st.atom_steps / st.device_s if st.device_s > 0 else None
+        out["saturated_atom_steps_per_device_s"] = (st.saturated_atom_steps / st.saturated_device_s
+                                                    if st.saturated_device_s > 0 else None)
+        return out
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.pis_batch_destroy(self._h)

@@ -402,20 +402,13 @@ pis_status contextualize(pis_system* s) {
     return PIS_OK;
 }
 
-// DumpTraj::write_step (src/writers/dump_traj.rs:68-74): lines formatted into a buffer and written
-// in blocks of about 1 MB.
-void write_dump(std::ofstream& o, int64_t step, int64_t n, const int32_t* types, const double* pos, const double h[3]) {
-    o << "ITEM: TIMESTEP\n" << step << "\nITEM: NUMBER OF ATOMS\n" << n << "\nITEM: BOX BOUNDS pp pp pp\n";
-    for (int a = 0; a < 3; ++a) o << "0 " << format_f64(h[a]) << "\n";
-    o << "ITEM: ATOMS id type x y z\n";
-    std::vector<char> buf((size_t)1 << 21);
+// Atom lines [i0, i1) of a dump ("id type x y z"), appended to out.
+void format_dump_lines(std::vector<char>& out, int64_t i0, int64_t i1, const int32_t* types, const double* pos) {
+    out.resize((size_t)(i1 - i0) * 80 + 2048);
     size_t len = 0;
-    for (int64_t i = 0; i < n; ++i) {
-        if (len + 1300 > buf.size()) {  // room for a line of three maximal numbers
-            o.write(buf.data(), (std::streamsize)len);
-            len = 0;
-        }
-        char* p = buf.data() + len;
+    for (int64_t i = i0; i < i1; ++i) {
+        if (len + 1300 > out.size()) out.resize(out.size() * 2);  // room for a line of three maximal numbers
+        char* p = out.data() + len;
         p = std::to_chars(p, p + 24, (long long)(i + 1)).ptr;
         *p++ = ' ';
         p = std::to_chars(p, p + 16, types[i]).ptr;
@@ -424,9 +417,26 @@ void write_dump(std::ofstream& o, int64_t step, int64_t n, const int32_t* types,
             p += pis::format_f64_buf(pos[3 * i + a], p);
         }
         *p++ = '\n';
-        len = (size_t)(p - buf.data());
+        len = (size_t)(p - out.data());
     }
-    o.write(buf.data(), (std::streamsize)len);
+    out.resize(len);
+}
+
+// DumpTraj::write_step (src/writers/dump_traj.rs:68-74). Large frames are formatted by up to 8
+// threads, each over a contiguous range of atoms, and written in order.
+void write_dump(std::ofstream& o, int64_t step, int64_t n, const int32_t* types, const double* pos, const double h[3]) {
+    o << "ITEM: TIMESTEP\n" << step << "\nITEM: NUMBER OF ATOMS\n" << n << "\nITEM: BOX BOUNDS pp pp pp\n";
+    for (int a = 0; a < 3; ++a) o << "0 " << format_f64(h[a]) << "\n";
+    o << "ITEM: ATOMS id type x y z\n";
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int T = n < 65536 ? 1 : (int)std::min<unsigned>(8, hw > 1 ? hw : 1);
+    std::vector<std::vector<char>> parts((size_t)T);
+    std::vector<std::thread> workers;
+    for (int t = 1; t < T; ++t)
+        workers.emplace_back([&, t] { format_dump_lines(parts[t], n * t / T, n * (t + 1) / T, types, pos); });
+    format_dump_lines(parts[0], 0, n / T, types, pos);
+    for (auto& w : workers) w.join();
+    for (auto& q : parts) o.write(q.data(), (std::streamsize)q.size());
 }
 
 }  // namespace

@@ -24,6 +24,7 @@ struct pis_batch {
     pis::PoolOptions opt;
     std::string err;
     std::vector<int64_t> atoms;  // per slot, 0 when free
+    pis_serve_stats serve{};     // the last pis_serve_run's accounting
 };
 
 namespace {
@@ -308,6 +309,12 @@ pis_status pis_batch_release(pis_batch* b, int32_t slot) {
     return PIS_OK;
 }
 
+pis_status pis_serve_last_stats(const pis_batch* b, pis_serve_stats* out) {
+    if (!b || !out) return PIS_ERR_INVALID_ARGUMENT;
+    *out = b->serve;
+    return PIS_OK;
+}
+
 int64_t pis_batch_atoms(const pis_batch* b) {
     if (!b) return 0;
     int64_t t = 0;
@@ -374,41 +381,74 @@ pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64
     // queue follows it on the stream. A job is seen finished in the snapshot of the graph it
     // finished in; slots placed after a graph was queued are not read from its snapshot.
     const int S = b->opt.max_slots;
+    // snapshot buffers alternate between the graph in flight and the one being read; the events
+    // that close each graph form a ring of 4 (a graph's interval starts at its predecessor's)
+    constexpr int RING = 4;
     pis::SysState* snap[2] = {nullptr, nullptr};
-    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaEvent_t ev[RING] = {nullptr, nullptr, nullptr, nullptr};
     struct Cleanup {
         pis::SysState** snap;
         cudaEvent_t* ev;
         ~Cleanup() {
-            for (int k = 0; k < 2; ++k) {
+            for (int k = 0; k < 2; ++k)
                 if (snap[k]) cudaFreeHost(snap[k]);
+            for (int k = 0; k < RING; ++k)
                 if (ev[k]) cudaEventDestroy(ev[k]);
-            }
         }
     } cleanup{snap, ev};
-    for (int k = 0; k < 2; ++k) {
-        if (cudaMallocHost((void**)&snap[k], sizeof(pis::SysState) * S) != cudaSuccess ||
-            cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming) != cudaSuccess) {
+    for (int k = 0; k < 2; ++k)
+        if (cudaMallocHost((void**)&snap[k], sizeof(pis::SysState) * S) != cudaSuccess) {
             cudaGetLastError();
             return bfail(b, PIS_ERR_NO_MEMORY, "pinned state snapshot");
         }
+    for (int k = 0; k < RING; ++k)
+        if (cudaEventCreate(&ev[k]) != cudaSuccess) {
+            cudaGetLastError();
+            return bfail(b, PIS_ERR_CUDA, "event");
+        }
+    // graph g (from 1) ends at ev[g % RING]; ev[0] is recorded now as the start of graph 1
+    if (cudaEventRecord(ev[0], b->eng.stream()) != cudaSuccess) {
+        cudaGetLastError();
+        return bfail(b, PIS_ERR_CUDA, "event");
     }
     std::vector<int64_t> placed_at(S, 0);  // first graph that steps each slot's current job
+    std::vector<int64_t> seen_steps(S, 0);  // steps_done of each slot's job at the last snapshot read
+    std::vector<char> saturated(1, 0);      // per graph: queued while a request waited for space
+    pis_serve_stats stats{};
     int64_t graphs = 0;                    // graphs queued so far
     int inflight = -1;                     // snapshot buffer of the last graph queued and not read
     uint64_t mark[2] = {0, 0};
     int64_t snap_graph[2] = {0, 0};
     auto read_snapshot = [&](int k) -> pis_status {
-        pis_status rs = b->eng.wait_event(ev[k], err);
+        const int64_t g = snap_graph[k];
+        pis_status rs = b->eng.wait_event(ev[g % RING], err);
         if (rs) return rs;
         b->eng.retire_staging(mark[k]);
         const double t_done = seconds_since(t0);
         const pis::SysState* ss = snap[k];
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, ev[(g - 1) % RING], ev[g % RING]) != cudaSuccess) {
+            cudaGetLastError();
+            ms = 0.f;
+        }
+        double done = 0.0;  // atom-steps of graph g
+        for (int s = 0; s < S; ++s) {
+            if (slot_req[s] < 0 || placed_at[s] > g) continue;
+            done += (double)b->atoms[s] * (double)(ss[s].steps_done - seen_steps[s]);
+            seen_steps[s] = ss[s].steps_done;
+        }
+        stats.atom_steps += done;
+        stats.device_s += 1e-3 * ms;
+        if (saturated[g]) {
+            stats.saturated_graphs += 1;
+            stats.saturated_atom_steps += done;
+            stats.saturated_device_s += 1e-3 * ms;
+        }
         // finished jobs: energies and counters as their last step left them (the step end writes
         // PE and KE every step); released with the chunk map rebuilt once, before the next graph
         for (int s = 0; s < S; ++s) {
             const int32_t q = slot_req[s];
-            if (q < 0 || placed_at[s] > snap_graph[k] || ss[s].steps_left > 0) continue;
+            if (q < 0 || placed_at[s] > g || ss[s].steps_left > 0) continue;
             out[q].finished_s = t_done;
             out[q].pe = ss[s].pe;
             out[q].ke = ss[s].ke;
@@ -451,9 +491,11 @@ pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64
             }
             slot_req[slot] = q;
             placed_at[slot] = graphs + 1;
+            seen_steps[slot] = 0;
             fresh.push_back(slot);
             ++active;
         }
+        const bool waiting = !queue.empty();  // the head did not fit: the pool is the limit
         if (!fresh.empty()) {
             // no synchronisation: the graph follows on the same stream
             pis_status st = b->eng.compute_potential_slots(fresh, err, false);
@@ -465,9 +507,10 @@ pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64
             if (st) return bfail(b, st, err);
             queued = inflight == 0 ? 1 : 0;
             ++graphs;
+            saturated.push_back(waiting ? 1 : 0);
             snap_graph[queued] = graphs;
             mark[queued] = b->eng.staging_mark();
-            st = b->eng.snapshot_states(snap[queued], ev[queued], err);
+            st = b->eng.snapshot_states(snap[queued], ev[graphs % RING], err);
             if (st) return bfail(b, st, err);
         }
         if (inflight >= 0) {
@@ -499,6 +542,8 @@ pis_status pis_serve_run(pis_batch* b, const pis_request* reqs, int32_t n, int64
     std::string serr;
     pis_status st = b->eng.sync(serr);
     if (st) return bfail(b, st, serr);
+    stats.graphs = graphs;
+    b->serve = stats;
     if (wall_s) *wall_s = seconds_since(t0);
     return PIS_OK;
 }

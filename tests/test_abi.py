@@ -126,3 +126,14 @@ def test_stats_struct_matches_header():
         assert n in body, n
     assert names[-2:] == ["fused_step", "reserved_"]
     assert ctypes.sizeof(_ffi.Stats) == 8 * 4 + 4 * 4 + 8 * 11 + 8
+
+
+def test_serve_stats_struct_matches_header():
+    import ctypes
+    from pis_gb300 import _ffi
+    text = open(os.path.join(ROOT, "include", "pis_gpu.h")).read()
+    body = text[text.rindex("typedef struct {", 0, text.index("} pis_serve_stats;")):text.index("} pis_serve_stats;")]
+    fields = re.findall(r"(int64_t|double)\s+([^;]+);", body)
+    names = [n.strip() for _, group in fields for n in group.split(",")]
+    assert names == [f[0] for f in _ffi.ServeStats._fields_]
+    assert ctypes.sizeof(_ffi.ServeStats) == 6 * 8

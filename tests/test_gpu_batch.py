@@ -95,6 +95,12 @@ def test_served_stream_results_match_alone(cuda_lib):
     b = _batch(atoms=4500, slots=3)  # too small for all at once: later requests wait for releases
     res, wall = b.serve(reqs, graph_steps=25)
     assert wall > 0
+    # the per-graph accounting adds up to every job's atoms x steps; some graphs ran while a
+    # request waited for space
+    st = b.serve_stats()
+    assert st["atom_steps"] == sum(4 * job.k ** 3 * job.steps for _, job in reqs)
+    assert st["graphs"] >= max(job.steps for _, job in reqs) // 25
+    assert 0 < st["saturated_graphs"] < st["graphs"] and 0 < st["saturated_device_s"] < st["device_s"]
     for (t, job), r in zip(reqs, res):
         assert r["status"] == 0
         assert r["steps"] == job.steps
