@@ -199,12 +199,12 @@ __global__ void __launch_bounds__(CL_THREADS) k_filter_cl(const DP P, int step_m
 template <int ACC, bool ONE, int M, int NB>
 __global__ void __launch_bounds__(CL_THREADS) k_force_cl(const DP P, int step_mode) {
     __shared__ double sh[32];
-    __shared__ ShiftTab4 shift;
+    __shared__ float4 shift[64];
     const int s = P.cblk_sys[blockIdx.x];
     if (s < 0) return;
     if (!slot_runs(P, s, step_mode)) return;
     const SysParams& sp = P.sp[s];
-    fill_shift_table(&shift, sp);
+    fill_shift_table(shift, sp);
     __syncthreads();
     const int c = P.cblk_first[blockIdx.x] + (int)threadIdx.x;
     const bool live = c < sp.cl0 + P.st[s].ncl;
@@ -260,9 +260,8 @@ __global__ void __launch_bounds__(CL_THREADS) k_force_cl(const DP P, int step_mo
             for (int b = 0; b < NB; ++b) pj[b] = __ldg(prel + (ent[b] & JMASK));
 #pragma unroll
             for (int b = 0; b < NB; ++b) {
-                const Shift3 sv = shift_of(&shift, ent[b] >> JBITS);
-                const float jx = (pj[b].x + sv.hi.x) + sv.lo.x, jy = (pj[b].y + sv.hi.y) + sv.lo.y,
-                            jz = (pj[b].z + sv.hi.z) + sv.lo.z;
+                const float4 sv = shift[ent[b] >> JBITS];
+                const float jx = pj[b].x + sv.x, jy = pj[b].y + sv.y, jz = pj[b].z + sv.z;
                 const int tj = __float_as_int(pj[b].w);
 #pragma unroll
                 for (int m = 0; m < M; ++m) {
@@ -317,13 +316,13 @@ __global__ void __launch_bounds__(CL_THREADS) k_force_cl(const DP P, int step_mo
 template <int ACC, bool ONE, int M, int NB>
 __global__ void __launch_bounds__(CL_THREADS) k_force_cl_lane(const DP P, int step_mode) {
     __shared__ double sh[32];
-    __shared__ ShiftTab4 shift;
+    __shared__ float4 shift[64];
     const int chunk = blockIdx.x / M, sub = blockIdx.x % M;
     const int s = P.cblk_sys[chunk];
     if (s < 0) return;
     if (!slot_runs(P, s, step_mode)) return;
     const SysParams& sp = P.sp[s];
-    fill_shift_table(&shift, sp);
+    fill_shift_table(shift, sp);
     __syncthreads();
     const int c = P.cblk_first[chunk] + sub * (CL_THREADS / M) + (int)threadIdx.x / M;
     const int m = (int)threadIdx.x % M;
@@ -351,7 +350,7 @@ __global__ void __launch_bounds__(CL_THREADS) k_force_cl_lane(const DP P, int st
 #pragma unroll
                 for (int b = 0; b < NB; ++b) ent[b] = (k0 + b < nn) ? load_list_word(nbp + q + (uint32_t)b * row) : pad;
             }
-            mixed_pairs<ONE, NB, ACC, true>(ent, prel, pi, &shift, tab, P0, acc);
+            mixed_pairs<ONE, NB, ACC, true>(ent, prel, pi, shift, tab, P0, acc);
             since += NB;
             if (since >= MIX_FLUSH) {
                 acc.fold();

@@ -351,7 +351,8 @@ __device__ __forceinline__ float4 cell_relative(const SysParams& sp, double4_32a
     dx -= sp.h[0] * rint(dx * sp.hinv[0]);
     dy -= sp.h[1] * rint(dy * sp.hinv[1]);
     dz -= sp.h[2] * rint(dz * sp.hinv[2]);
-    return make_float4((float)dx, (float)dy, (float)dz, __int_as_float(type));
+    // in units of the x cell edge (SysParams::sc)
+    return make_float4((float)(dx * sp.isc), (float)(dy * sp.isc), (float)(dz * sp.isc), __int_as_float(type));
 }
 
 }  // namespace pis

@@ -51,10 +51,17 @@ __device__ __forceinline__ void skin_test(const DP& P, const SysParams& sp, SysS
         if (x != x || y != y || z != z) atomicOr(&st.flags, FLAG_NAN);
     }
 }
-// cell-relative FP32 coordinates = build-time ones + displacement since the build
-__device__ __forceinline__ float4 cell_relative_moved(const DP& P, int i, double dx, double dy, double dz) {
+// cell-relative FP32 coordinates = build-time ones + displacement since the build, in units of
+// the slot's x cell edge (SysParams::sc); the displacement (below the skin) is scaled in FP32 by
+// 1/sc as the sum of two floats, so the scale carries no FP32 rounding of its own
+__device__ __forceinline__ float scaled_step(float d, const SysParams& sp) {
+    return fmaf(d, sp.fisc_lo, d * sp.fisc_hi);
+}
+__device__ __forceinline__ float4 cell_relative_moved(const DP& P, const SysParams& sp, int i, double dx, double dy,
+                                                      double dz) {
     const float4 q = P.prelb[i];
-    return make_float4(q.x + (float)dx, q.y + (float)dy, q.z + (float)dz, q.w);
+    return make_float4(q.x + scaled_step((float)dx, sp), q.y + scaled_step((float)dy, sp),
+                       q.z + scaled_step((float)dz, sp), q.w);
 }
 
 template <bool MIXED>
@@ -89,7 +96,7 @@ __global__ void k_integrate1(const DP P) {
     if (P.zero_forces) P.frc[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
     double dx, dy, dz;
     skin_test(P, sp, st, i, x, y, z, dx, dy, dz);
-    if (MIXED) P.prel[i] = cell_relative_moved(P, i, dx, dy, dz);
+    if (MIXED) P.prel[i] = cell_relative_moved(P, sp, i, dx, dy, dz);
 }
 
 // Counting sort, pass 1: cell of every atom (reference binning of src/atoms/neighbour_list.rs:
@@ -881,26 +888,7 @@ __global__ void __launch_bounds__(256) k_force_fp64_ref(const DP P, int respect_
 // PE = sum_i sum_j u_ij, halved at the reduction.
 // Image-shift table of the mixed kernels: code -> cell offset * cell edge; a 3 in any field marks
 // a padding entry and sends it out of range.
-// Image shifts of the mixed pair loop. A list entry's code (2 bits per axis: 0, +1, -1, padding)
-// selects the shift of the neighbour cell, ox * cell edge per axis. The cell edge is not an FP32
-// number, so every shift is carried as hi = the nearest float and lo = the float nearest the rest,
-// and a displacement is formed as ((x_j - x_i) + hi) + lo. With hi alone, every pair across a
-// cell face is displaced by the same ~1e-7 (the rounding of the edge, a fixed sign per face), a
-// bias rather than noise: it raised the NVE energy drift of the 256,000-atom liquid from
-// 6.5e-6 to 1.4e-5 per atom per 10^4 steps (six states each; FP64: 5.6e-6).
-struct Shift3 {
-    float3 hi, lo;
-};
-__device__ __forceinline__ void shift_parts(const SysParams& sp, int a, float& hi, float& lo) {
-    hi = sp.fcs[a];
-    lo = (float)(sp.cs[a] - (double)sp.fcs[a]);
-}
-// 64-entry tables (code -> shift), hi parts with w free for the caller, lo parts in xyz
-struct ShiftTab4 {
-    float4 hi[64];
-    float4 lo[64];
-};
-__device__ __forceinline__ void fill_shift_table(ShiftTab4* t, const SysParams& sp) {
+__device__ __forceinline__ void fill_shift_table(float4* shift, const SysParams& sp) {
     if (threadIdx.x < 64) {
         const int c = threadIdx.x;
         const int bx = c & 3, by = (c >> 2) & 3, bz = (c >> 4) & 3;
@@ -908,33 +896,27 @@ __device__ __forceinline__ void fill_shift_table(ShiftTab4* t, const SysParams& 
         const float fy = by == 1 ? 1.f : (by == 2 ? -1.f : 0.f);
         const float fz = bz == 1 ? 1.f : (bz == 2 ? -1.f : 0.f);
         const bool pad = bx == 3 || by == 3 || bz == 3;
-        float h[3], l[3];
-        for (int a = 0; a < 3; ++a) shift_parts(sp, a, h[a], l[a]);
-        t->hi[c] = pad ? make_float4(1e18f, 1e18f, 1e18f, 0.f) : make_float4(fx * h[0], fy * h[1], fz * h[2], 0.f);
-        t->lo[c] = pad ? make_float4(0.f, 0.f, 0.f, 0.f) : make_float4(fx * l[0], fy * l[1], fz * l[2], 0.f);
+        shift[c] = pad ? make_float4(1e18f, 1e18f, 1e18f, 0.f)
+                       : make_float4(fx * sp.fcs[0], fy * sp.fcs[1], fz * sp.fcs[2], 0.f);
     }
 }
 
-// Per-axis image shifts: t[4a + c] = (hi, lo) of (0, +1, -1, pad) x cell edge along axis a for the
-// axis's 2-bit code c. Three 4-entry tables: the lanes of a warp read at most 4 distinct entries per
-// axis, so a lookup is one shared-memory wavefront, where the 64-entry float4 table's scattered
-// 16-byte reads conflict on banks (~7 wavefronts per warp-wide lookup).
-__device__ __forceinline__ void fill_shift_axes(float2* t, const SysParams& sp) {
+// Per-axis image shifts: t[4a + c] = (0, +1, -1, pad) x cell edge along axis a for the axis's
+// 2-bit code c. Three 4-word tables: the lanes of a warp read at most 4 distinct words per axis, so
+// a lookup is one shared-memory wavefront, where the 64-entry float4 table's scattered 16-byte reads
+// conflict on banks (~7 wavefronts per warp-wide lookup).
+__device__ __forceinline__ void fill_shift_axes(float* t, const SysParams& sp) {
     if (threadIdx.x < 12) {
         const int a = threadIdx.x >> 2, c = threadIdx.x & 3;
-        float hi, lo;
-        shift_parts(sp, a, hi, lo);
-        t[threadIdx.x] = c == 3 ? make_float2(1e18f, 0.f)
-                                : (c == 1 ? make_float2(hi, lo) : (c == 2 ? make_float2(-hi, -lo) : make_float2(0.f, 0.f)));
+        t[threadIdx.x] = c == 3 ? 1e18f : (c == 1 ? sp.fcs[a] : (c == 2 ? -sp.fcs[a] : 0.f));
     }
 }
-__device__ __forceinline__ Shift3 shift_of(const ShiftTab4* t, uint32_t code) {
-    const float4 h = t->hi[code], l = t->lo[code];
-    return Shift3{make_float3(h.x, h.y, h.z), make_float3(l.x, l.y, l.z)};
+__device__ __forceinline__ float3 shift_of(const float4* t, uint32_t code) {
+    const float4 v = t[code];
+    return make_float3(v.x, v.y, v.z);
 }
-__device__ __forceinline__ Shift3 shift_of(const float2* t, uint32_t code) {
-    const float2 x = t[code & 3u], y = t[4 + ((code >> 2) & 3u)], z = t[8 + (code >> 4)];
-    return Shift3{make_float3(x.x, y.x, z.x), make_float3(x.y, y.y, z.y)};
+__device__ __forceinline__ float3 shift_of(const float* t, uint32_t code) {
+    return make_float3(t[code & 3u], t[4 + ((code >> 2) & 3u)], t[8 + (code >> 4)]);
 }
 
 // Per-atom accumulator of the mixed kernels: FP32 pair terms summed over a batch, batch sums
@@ -994,10 +976,10 @@ __device__ __forceinline__ void mixed_pairs_math(const uint32_t (&ent)[NB], cons
                                                  MixAcc<ACC>& a) {
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
-        const Shift3 sv = shift_of(shift, ent[b] >> JBITS);
-        const float dx = ((pj[b].x - pi.x) + sv.hi.x) + sv.lo.x;
-        const float dy = ((pj[b].y - pi.y) + sv.hi.y) + sv.lo.y;
-        const float dz = ((pj[b].z - pi.z) + sv.hi.z) + sv.lo.z;
+        const float3 sv = shift_of(shift, ent[b] >> JBITS);
+        const float dx = (pj[b].x - pi.x) + sv.x;
+        const float dy = (pj[b].y - pi.y) + sv.y;
+        const float dz = (pj[b].z - pi.z) + sv.z;
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         float frc2 = P0.frc2, fs2 = P0.fs2, fe24 = P0.fe24, fe4 = P0.fe4, fuc = P0.fuc;
         if (!ONE) {
@@ -1142,7 +1124,7 @@ __device__ __forceinline__ float4 mixed_atom_forces(const DP& P, const SysParams
 template <int ACC, int LPA, bool ONE, int MIX_BATCH, int Q = 1>
 __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) {
     __shared__ double sh[32];
-    __shared__ float2 shift[12];
+    __shared__ float shift[12];
     auto tile = cg::tiled_partition<LPA>(cg::this_thread_block());
     int s, i;
     const bool live = group_atom_of<LPA>(P, s, i);
@@ -1189,7 +1171,7 @@ __global__ void __launch_bounds__(256, KB <= 8 ? 4 : 2) k_force_mixed_tma(const 
     constexpr int S = MIX_TMA_STAGES;
     extern __shared__ __align__(128) uint32_t ring[];  // S * KB * MIX_TMA_ROW words
     __shared__ double sh[32];
-    __shared__ ShiftTab4 shift;
+    __shared__ float4 shift[64];
     __shared__ __align__(8) uint64_t full[S];
     __shared__ __align__(8) uint64_t empty[S];
     __shared__ int wmax[8];
@@ -1200,7 +1182,7 @@ __global__ void __launch_bounds__(256, KB <= 8 ? 4 : 2) k_force_mixed_tma(const 
     const SysParams& sp = P.sp[s];
     SysState& st = P.st[s];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    fill_shift_table(&shift, sp);
+    fill_shift_table(shift, sp);
     const int first = P.blk_first[blockIdx.x];
     const int cnt = min(256, (int)(sp.a0 + sp.n) - first);
     const int off = first & 3;
@@ -1256,7 +1238,7 @@ __global__ void __launch_bounds__(256, KB <= 8 ? 4 : 2) k_force_mixed_tma(const 
                 const uint32_t* rp = ring + q0 * KB * MIX_TMA_ROW + col;
 #pragma unroll
                 for (int b = 0; b < KB; ++b) ent[b] = (k0 + b < nn) ? rp[b * MIX_TMA_ROW] : pad;
-                mixed_pairs<ONE, KB, ACC>(ent, prel, pi, &shift, tab, P0, acc);
+                mixed_pairs<ONE, KB, ACC>(ent, prel, pi, shift, tab, P0, acc);
                 if (((r + 1) * KB) % MIX_FLUSH == 0) acc.fold();
             }
         }
@@ -1301,7 +1283,7 @@ constexpr int TILE_ATOMS = 3328;  // 52 KB of float4 per block: four blocks per 
 template <int ACC, bool ONE>
 __global__ void __launch_bounds__(256) k_force_mixed_tile(const DP P, int step_mode) {
     extern __shared__ __align__(16) float4 tile[];  // TILE_ATOMS
-    __shared__ ShiftTab4 shd[3];                   // (wrap state, code) -> image shift, delta bits in hi.w
+    __shared__ float4 shd[3 * 64];                 // (wrap state, code) -> image shift, delta bits in w
     __shared__ int psrc[27], plen[27], poff[27];   // pieces: first atom, atoms, shared-memory offset
     __shared__ int use_tile;
     __shared__ __align__(8) uint64_t bar;
@@ -1377,11 +1359,8 @@ __global__ void __launch_bounds__(256) k_force_mixed_tile(const DP P, int step_m
             if (!pad && w == 2 && ox == 1) p = 18 + row;
             delta = poff[p] - psrc[p];
         }
-        float h[3], l[3];
-        for (int a = 0; a < 3; ++a) shift_parts(sp, a, h[a], l[a]);
-        shd[w].hi[c] = pad ? make_float4(1e18f, 1e18f, 1e18f, __int_as_float(delta))
-                           : make_float4(ox * h[0], oy * h[1], oz * h[2], __int_as_float(delta));
-        shd[w].lo[c] = pad ? make_float4(0.f, 0.f, 0.f, 0.f) : make_float4(ox * l[0], oy * l[1], oz * l[2], 0.f);
+        shd[t] = pad ? make_float4(1e18f, 1e18f, 1e18f, __int_as_float(delta))
+                     : make_float4(ox * sp.fcs[0], oy * sp.fcs[1], oz * sp.fcs[2], __int_as_float(delta));
     }
     __syncthreads();
     bool got = tiled && mbar_wait_n(&bar, 0u, P.wait_limit);
@@ -1396,7 +1375,7 @@ __global__ void __launch_bounds__(256) k_force_mixed_tile(const DP P, int step_m
         const LJDev* tab = P.tab + sp.tab0 + ti * sp.nt;
         const MixLJ P0 = mix_lj_load(tab[0]);
         const int cx = P.cellof[i] % nx;
-        const ShiftTab4* shift = shd + (got ? (cx == 0 ? 1 : (cx == nx - 1 ? 2 : 0)) : 0);
+        const float4* shift = shd + (got ? 64 * (cx == 0 ? 1 : (cx == nx - 1 ? 2 : 0)) : 0);
         const int nn = P.nn[i];
         const uint32_t row32 = (uint32_t)P.npad;
         const uint32_t* __restrict__ nbp = P.nbr + i;
@@ -1419,7 +1398,7 @@ __global__ void __launch_bounds__(256) k_force_mixed_tile(const DP P, int step_m
             if (got) {
 #pragma unroll
                 for (int b = 0; b < NB; ++b)
-                    pj[b] = tile[(int)(ent[b] & JMASK) + __float_as_int(shift->hi[ent[b] >> JBITS].w)];
+                    pj[b] = tile[(int)(ent[b] & JMASK) + __float_as_int(shift[ent[b] >> JBITS].w)];
             } else {
 #pragma unroll
                 for (int b = 0; b < NB; ++b) pj[b] = __ldg(prel + (ent[b] & JMASK));

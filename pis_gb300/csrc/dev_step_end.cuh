@@ -173,7 +173,7 @@ __host__ __device__ constexpr int step_list_prefetch() {
 template <int ACC, bool ONE, int MIX_BATCH, bool DRIFT, bool TRACE>
 __global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixed(const DP P) {
     __shared__ double sh[32];
-    __shared__ float2 shift[12];
+    __shared__ float shift[12];
     int s, i;
     const bool live = atom_of(P, s, i);
     if (s < 0) return;
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixe
             P.pos[cur][i] = make_double4_32a(x, y, z, p.w);
             double dx, dy, dz;
             skin_test(P, sp, st, i, x, y, z, dx, dy, dz);
-            P.prel_out[i] = cell_relative_moved(P, i, dx, dy, dz);
+            P.prel_out[i] = cell_relative_moved(P, sp, i, dx, dy, dz);
         }
     }
     const double pe_tot = block_sum<256>(acc.e, sh);

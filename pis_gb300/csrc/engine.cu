@@ -283,6 +283,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     hp_.assign(NS, SysParams{});
     slot_rlist_.assign(NS, 0.0);
     slot_rcmax_.assign(NS, 0.0);
+    slot_tab_host_.assign(NS, std::vector<LJDev>());
     free_atoms_.clear();
     free_cells_.clear();
     free_atoms_[0] = NA;
@@ -382,7 +383,8 @@ static void cell_grid(const SlotDesc& d, double rlist, int nc[3]) {
 
 // Box fields of a slot from a row-major h and its inverse (p.nc set): diagonals (h, hinv) for the
 // orthorhombic kernels, the full matrices and cell edge vectors for a triclinic box, cell widths.
-static void set_box(SysParams& p, const double* h, const double* hi) {
+// rl: the padded list radius (the FP32 list test's radius, in length units)
+static void set_box(SysParams& p, const double* h, const double* hi, double rl) {
     double w[3];
     box_widths(h, w);
     p.tric = diagonal_box(h) ? 0 : 1;
@@ -394,11 +396,42 @@ static void set_box(SysParams& p, const double* h, const double* hi) {
         p.h[a] = h[4 * a];
         p.hinv[a] = hi[4 * a];
         p.cs[a] = w[a] / p.nc[a];
-        p.fcs[a] = (float)p.cs[a];
-        p.fsub[a] = (float)(4.0 / p.cs[a]);
     }
+    p.sc = p.tric ? 1.0 : p.cs[0];
+    p.isc = p.tric ? 1.0 : 1.0 / p.cs[0];
+    p.fisc_hi = (float)p.isc;
+    p.fisc_lo = (float)(p.isc - (double)p.fisc_hi);
+    for (int a = 0; a < 3; ++a) {
+        p.fcs[a] = (float)(p.cs[a] * p.isc);
+        p.fsub[a] = (float)(4.0 * p.sc / p.cs[a]);
+    }
+    p.frlist2 = (float)(rl * rl * (p.isc * p.isc));
     for (int d = 0; d < 3; ++d)
         for (int r = 0; r < 3; ++r) p.fcv[3 * d + r] = (float)(h[3 * r + d] / p.nc[d]);
+}
+
+// FP32 constants of a pair-table entry for FP32 coordinates in units of sc (r' = r / sc):
+// sigma^2 / r^2 and the cutoff test keep their values with sigma' = sigma / sc, rc' = rc / sc, and
+// the force 24 eps s6 (2 s6 - 1) r / r^2 is c' r' with eps24' = 24 eps / sc.
+static void set_fp32_constants(LJDev& t, double sc) {
+    const double is2 = 1.0 / (sc * sc);
+    t.feps4 = (float)t.eps4;
+    t.feps24 = (float)(t.eps24 / sc);
+    t.fsigma2 = (float)(t.sigma2 * is2);
+    t.frc2 = (float)(t.rcut * t.rcut * is2);
+    t.fucut = (float)t.ucut;
+}
+
+// The 27-cell walk (k_build1) serves axes of two cells too: there the -1 and +1 neighbours are
+// the same cell seen through two images, and the box edge (2 cells of at least the list radius)
+// exceeds twice the padded list radius, so at most one image of a pair passes the distance test
+// and no pair is listed twice. Only an edge within 1e-5 of that bound is left to the generic walk,
+// which keeps the nearer image per pair. rl: the padded list radius (its FP32 square decides).
+static int walk27_valid(const SysParams& p, double rl) {
+    const double rlf = std::sqrt((double)(float)(rl * rl));
+    for (int a = 0; a < 3; ++a)
+        if (p.nc[a] < 2 || (p.nc[a] == 2 && !(p.h[a] > 2.0 * rlf * (1.0 + 1e-5)))) return 0;
+    return 1;
 }
 
 // The reference's own cell grid at the largest cutoff (Atoms::divide_into_cells,
@@ -585,18 +618,7 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
             ucut = 4.0 * e.epsilon * (cr - ca);
         }
         t.ucut = ucut;
-        t.feps4 = (float)t.eps4;
-        t.feps24 = (float)t.eps24;
-        t.fsigma2 = (float)t.sigma2;
-        t.frc2 = (float)rc2;
-        t.fucut = (float)ucut;
     }
-    // deferred placement: nothing waits for these copies, so their sources are held
-    auto src = [&](const void* q, size_t bytes) { return defer_map ? hold(q, bytes) : q; };
-    pis_status st = check(cudaMemcpyAsync(d_->tab + tab0, src(tab.data(), sizeof(LJDev) * tab.size()),
-                                          sizeof(LJDev) * tab.size(), cudaMemcpyHostToDevice, stream_),
-                          "table upload", err);
-    if (st) return -st;
 
     SysParams p;
     std::memset(&p, 0, sizeof(p));
@@ -611,22 +633,24 @@ int Engine::add_slot(const SlotDesc& d, const int32_t* type_ids, const double* p
         p.pbc[a] = 1;
     }
     // h^-1 by adjugate / determinant, the reference's 3x3 inverse (src/simulation_box.rs:13)
-    set_box(p, d.h, hinv_full);
+    const double rl = rlist * (1.0 + 1e-5);
+    set_box(p, d.h, hinv_full, rl);
     p.half_skin2 = 0.25 * d.skin * d.skin;
     p.dt = d.dt;
     p.dt2 = d.dt * d.dt;
     p.hdt = 0.5 * p.dt;
     p.hdt2 = 0.5 * p.dt2;
-    double rl = rlist * (1.0 + 1e-5);
-    p.frlist2 = (float)(rl * rl);
-    // The 27-cell walk (k_build1) serves axes of two cells too: there the -1 and +1 neighbours are
-    // the same cell seen through two images, and the box edge (2 cells of at least the list radius)
-    // exceeds twice the padded list radius, so at most one image of a pair passes the distance
-    // test and no pair is listed twice. Only an edge within 1e-5 of that bound is left to the
-    // generic walk, which keeps the nearer image per pair.
-    p.walk27 = 1;
-    for (int a = 0; a < 3; ++a)
-        if (nc[a] < 2 || (nc[a] == 2 && !(p.h[a] > 2.0 * std::sqrt((double)p.frlist2) * (1.0 + 1e-5)))) p.walk27 = 0;
+    p.walk27 = walk27_valid(p, rl);
+    // the pair table, FP32 constants in the slot's coordinate unit
+    for (auto& t : tab)
+        if (t.present) set_fp32_constants(t, p.sc);
+    slot_tab_host_[slot] = tab;
+    // deferred placement: nothing waits for these copies, so their sources are held
+    auto src = [&](const void* q, size_t bytes) { return defer_map ? hold(q, bytes) : q; };
+    pis_status st = check(cudaMemcpyAsync(d_->tab + tab0, src(tab.data(), sizeof(LJDev) * tab.size()),
+                                          sizeof(LJDev) * tab.size(), cudaMemcpyHostToDevice, stream_),
+                          "table upload", err);
+    if (st) return -st;
     // the reference's own cell grid at the largest cutoff (Atoms::divide_into_cells,
     // src/atoms/neighbour_list.rs:45-57: floor(|h column| / rcut), at least 1)
     double rc_max = 0.0;  // PairPotentialManager::max_rcut (src/potentials/potential.rs:170-179)
@@ -1811,21 +1835,26 @@ pis_status Engine::scale_box(int slot, const double* m, std::string& err) {
         h_new.m[k] = nh[k];
     }
     const int full = (p.tric || !diagonal_box(nh)) ? 1 : 0;
-    set_box(p, nh, nhi);
+    set_box(p, nh, nhi, rl * (1.0 + 1e-5));
     reference_cells(nh, slot_rcmax_[slot], p.rnc);
     if (opt_.ref_order && !reference_cells_ok(p.rnc)) {
         err = "reference-order forces need at least 3 cells of the largest cutoff per axis";
         return PIS_ERR_UNSUPPORTED;
     }
-    // the 27-cell walk's two-cell condition (add_slot) for the new edges
-    p.walk27 = 1;
-    for (int a = 0; a < 3; ++a)
-        if (p.nc[a] < 2 || (p.nc[a] == 2 && !(p.h[a] > 2.0 * std::sqrt((double)p.frlist2) * (1.0 + 1e-5)))) p.walk27 = 0;
+    // the 27-cell walk's two-cell condition for the new edges
+    p.walk27 = walk27_valid(p, rl * (1.0 + 1e-5));
+    // the FP32 pair constants follow the coordinate unit (the x cell edge)
+    std::vector<LJDev>& tab = slot_tab_host_[slot];
+    for (auto& t : tab)
+        if (t.present) set_fp32_constants(t, p.sc);
+    pis_status st = check(cudaMemcpyAsync(d_->tab + p.tab0, tab.data(), sizeof(LJDev) * tab.size(),
+                                          cudaMemcpyHostToDevice, stream_), "table upload", err);
+    if (st) return st;
     LAUNCH(k_scale_pos, (unsigned)max_chunks_, opt_.blk, *d_, slot, hi_old, h_new, full);
     if (p.tric && !any_tric_) dirty_map_ = true;  // the next launch selects the triclinic kernels
     hp_[slot] = p;
-    pis_status st = check(cudaMemcpyAsync(d_->sp + slot, &hp_[slot], sizeof(SysParams), cudaMemcpyHostToDevice, stream_),
-                          "params", err);
+    st = check(cudaMemcpyAsync(d_->sp + slot, &hp_[slot], sizeof(SysParams), cudaMemcpyHostToDevice, stream_),
+               "params", err);
     if (st) return st;
     int32_t one = 1;
     st = check(cudaMemcpyAsync(&d_->st[slot].rebuild, &one, 4, cudaMemcpyHostToDevice, stream_), "params", err);

@@ -58,9 +58,14 @@ struct SysParams {
     double half_skin2; // (skin / 2)^2
     double dt, dt2;    // dt, dt*dt
     double hdt, hdt2;  // dt/2, dt*dt/2 (mixed-path integrators)
-    float fcs[3];
-    float frlist2;     // FP32 list radius squared, padded so the FP32 test is a superset
-    float fsub[3];     // 4 / cell edge: sub-cell index scale of the in-cell atom order
+    // FP32 cell-relative coordinates (prel) are in units of sc, the x cell edge (1 for a triclinic
+    // box: Cartesian), so in a box with cubic cells an image shift is exactly +-1; the FP32 pair
+    // constants of the slot's table are scaled to match
+    double sc, isc;    // the unit and its inverse
+    float fisc_hi, fisc_lo;  // isc as the sum of two floats (FP32 scaling of small displacements)
+    float fcs[3];      // cell edges in units of sc
+    float frlist2;     // FP32 list radius squared in units of sc, padded so the FP32 test is a superset
+    float fsub[3];     // 4 sc / cell edge: sub-cell index scale of the in-cell atom order
     int32_t walk27;    // the 27-cell walk of the thread-per-atom build is valid (see add_slot)
     int32_t rnc[3];    // the reference's own cell grid at the largest cutoff (reference-order forces)
     int32_t tric;      // the box has off-diagonal elements (FP64 path only): H / HI below are used
@@ -259,6 +264,7 @@ class Engine {
     std::vector<int> slot_tab_size_;
     std::vector<double> slot_rlist_;
     std::vector<double> slot_rcmax_;  // largest cutoff of each slot's pair table
+    std::vector<std::vector<LJDev>> slot_tab_host_;  // each slot's pair table as uploaded
     // free-space bookkeeping (first fit over atom and cell index ranges)
     std::map<int64_t, int64_t> free_atoms_, free_cells_, free_clusters_;
     std::vector<int> free_tab_;
