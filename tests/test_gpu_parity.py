@@ -294,3 +294,31 @@ def test_plain_step_graphs_equal_conditional(liquid_melt, precision):
     for x, y in zip(a.get_state(), b.get_state()):
         assert np.array_equal(x, y)
     assert a.stats()["rebuilds"] == b.stats()["rebuilds"] >= 2
+
+
+@pytest.mark.parametrize("nc,stretch", [(6, (1.0, 1.1, 1.25)), (5, (1.0, 0.95, 1.2))])
+def test_mixed_orthorhombic_cells(oracle_lib, cuda_lib, nc, stretch):
+    # boxes whose cells differ between axes (3 x 3 x 4 cells; 2 x 2 x 3 cells, two-cell axes): the
+    # mixed path's FP32 coordinates are in units of the x cell edge, so the y and z image shifts
+    # are edge ratios there. Neighbour sets equal the oracle's, forces stay within the mixed bar
+    # of FP64, and a 60-step run with rebuilds stays close to the FP64 run
+    s = liquid(nc=nc, seed=12)
+    m = np.diag(stretch)
+    s["pos"] = s["pos"] @ m
+    s["h"] = s["h"] @ m
+    s = melted(s, steps=100, dt=0.004)
+    o = to_oracle(s)
+    off, idx = o.full_list()
+    g = to_gpu(s, "mixed", list_kind="full")
+    got = g.neighbour_list()
+    sets = [tuple(sorted(idx[off[i]:off[i + 1]])) for i in range(len(off) - 1)]
+    assert [tuple(got[1][got[0][i]:got[0][i + 1]]) for i in range(len(got[0]) - 1)] == sets
+    f64 = to_gpu(s, "fp64")
+    pe64, F64 = f64.compute_potential()
+    pe, f = g.compute_potential()
+    assert np.sqrt(np.sum((f - F64) ** 2) / np.sum(F64 ** 2)) <= 1e-5
+    assert abs(pe - pe64) <= 1e-6 * abs(pe64)
+    e = g.verlet_step_nve(0.004, 60)
+    e64 = f64.verlet_step_nve(0.004, 60)
+    assert np.max(np.abs(e - e64) / np.abs(e64)) <= 1e-5
+    assert g.stats()["rebuilds"] >= 2
