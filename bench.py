@@ -346,6 +346,17 @@ def main():
     force64_ms = st64[2] / k64s
     list64 = f64.stats()["list_entries"] / n  # half list
     fp64_flops = n * (list64 * FLOPS_PER_CANDIDATE + 27.6 * FLOPS_PER_PAIR_ENERGY)
+    # mixed precision on a Newton-3 half list (forces on j by FP64 atomics; a measured variant)
+    mh = GpuContext(TABLE, 1, skin=SKIN, precision="mixed", list_kind="half", mixed_kahan=True)
+    mh.set_state(melt_pos, types, [1.0], h, velocities=melt_vel)
+    mh.compute_potential(want_forces=False)
+    mh.run_timed(DT, 3)
+    msh, _ = mh.run_timed(DT, k64)
+    _, sth = mh.run_timed(DT, k64s, stages=True)
+    mixed_half = {"value": world * n * k64 / (max_over_ranks(msh, world) * 1e-3), "unit": "atom-steps/s",
+                  "steps": k64, "ms_per_step": msh / k64, "force_ms_per_step": float(sth[2]) / k64s,
+                  "list_entries_per_atom": mh.stats()["list_entries"] / n}
+    mh.close()
     f64f = GpuContext(TABLE, 1, skin=SKIN, precision="fp64", fp64_fast=True)
     f64f.set_state(melt_pos, types, [1.0], h, velocities=melt_vel)
     f64f.compute_potential(want_forces=False)
@@ -361,6 +372,13 @@ def main():
         mixf.set_state(melt_pos, types, [1.0], h, velocities=melt_vel)
         pem, Fm = mixf.compute_potential()
         errs[name] = (float(np.sqrt(np.sum((Fm - F64) ** 2) / np.sum(F64 ** 2))), abs(pem - pe64) / abs(pe64))
+        if name == "timed":
+            # atoms whose force differs by more than 1e-2 eps/sigma: a pair within ~1e-7 of the cutoff
+            # decided differently by the FP32 test (the LJ force jumps by 0.039 eps/sigma at rc = 2.5)
+            dF = np.linalg.norm(Fm - F64, axis=1)
+            edge = dF > 1e-2
+            cut_edge = {"atoms_over_1e-2": int(edge.sum()),
+                        "force_rms_rel_other_atoms": float(np.sqrt(np.sum((Fm - F64)[~edge] ** 2) / np.sum(F64 ** 2)))}
         mixf.close()
     force_rms, pe_rel = errs["timed"]
     f64.close()
@@ -447,12 +465,13 @@ def main():
             "pairs_per_s": world * pairs_per_step * args.steps / (ms * 1e-3),
             "fp64_fast": {"value": v64f, "unit": "atom-steps/s", "steps": k64, "dtype": "f64",
                           "note": "FMA / Newton-reciprocal variant, same cutoff decisions"},
+            "mixed_half_list": mixed_half,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d / k_e2e,
                     "d2h_bytes_per_step": d2h / k_e2e, "seconds": e2e_s,
                     "path": "set_state + compute_potential + verlet_step_nve(K) + get_state, pinned host buffers"},
             "roofline": roofline,
-            "error_vs_fp64": {"force_rms_rel": force_rms, "pe_rel": pe_rel,
+            "error_vs_fp64": {"force_rms_rel": force_rms, "pe_rel": pe_rel, "cutoff_edge": cut_edge,
                               "default_options": {"force_rms_rel": errs["default_options"][0],
                                                   "pe_rel": errs["default_options"][1]}},
             "batched": batched_summary,

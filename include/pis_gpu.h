@@ -65,7 +65,8 @@ typedef enum {
 
 typedef enum {
     PIS_LIST_DEFAULT = 0,    /* half list for FP64, full list for MIXED */
-    PIS_LIST_HALF = 1,       /* Newton-3 half list, forces on j scattered with FP64 atomics */
+    PIS_LIST_HALF = 1,       /* Newton-3 half list, forces on j scattered with FP64 atomics (MIXED: thread
+                              * per atom, separate force and integration kernels; a measured variant) */
     PIS_LIST_FULL = 2        /* full list, each pair evaluated from both ends, no atomics */
 } pis_list_kind;
 

@@ -1148,6 +1148,87 @@ __global__ void __launch_bounds__(256) k_force_mixed(const DP P, int step_mode) 
     if (threadIdx.x == 0) P.pe_part[blockIdx.x] = tot;
 }
 
+// Mixed precision forces on a Newton-3 half list (PIS_LIST_HALF with the mixed path; the
+// reference's own managers walk half shells, src/potentials/lennard_jones.rs:186-244): thread per
+// atom, column-major list, the same FP32 pair arithmetic as k_force_mixed. Atom i keeps its share in
+// the usual batch sums; each pair's force on j, -F_ij, is added to F_j with FP64 atomics, and so is
+// i's own total at the end (other threads add to it as their j), so forces must be zeroed before
+// (integrate-1 and every evaluation do). The order of the atomic additions varies from launch to
+// launch, so results are reproducible to FP64 rounding of the sums, not bit for bit.
+template <int ACC, bool ONE, int NB>
+__global__ void __launch_bounds__(256) k_force_mixed_half(const DP P, int step_mode) {
+    __shared__ double sh[32];
+    __shared__ float shift[12];
+    int s, i;
+    const bool live = atom_of(P, s, i);
+    if (s < 0) return;
+    if (!slot_runs(P, s, step_mode)) return;
+    const SysParams& sp = P.sp[s];
+    fill_shift_axes(shift, sp);
+    __syncthreads();
+    MixAcc<ACC> acc;
+    if (live) {
+        const float4* __restrict__ prel = P.prel;
+        const float4 pi = prel[i];
+        const LJDev* tab = P.tab + sp.tab0 + __float_as_int(pi.w) * sp.nt;
+        const MixLJ P0 = mix_lj_load(tab[0]);
+        const int nn = P.nn[i];
+        const uint32_t* __restrict__ nbp = P.nbr + i;
+        const uint32_t row32 = (uint32_t)P.npad;
+        uint32_t qoff = 0;
+        int since = 0;
+        for (int k0 = 0; k0 < nn; k0 += NB) {
+            uint32_t ent[NB];
+            float4 pj[NB];
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                ent[b] = (k0 + b < nn) ? load_list_word(nbp + qoff + (uint32_t)b * row32) : 0xffffffffu;
+                pj[b] = ent[b] != 0xffffffffu ? __ldg(prel + (ent[b] & JMASK)) : pi;
+            }
+            qoff += (uint32_t)NB * row32;
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                if (ent[b] == 0xffffffffu) continue;
+                const float3 sv = shift_of(shift, ent[b] >> JBITS);
+                const float dx = (pj[b].x - pi.x) + sv.x;
+                const float dy = (pj[b].y - pi.y) + sv.y;
+                const float dz = (pj[b].z - pi.z) + sv.z;
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                MixLJ L = P0;
+                if (!ONE) {
+                    const LJDev& T = tab[__float_as_int(pj[b].w)];
+                    L = T.present ? mix_lj_load(T) : MixLJ{-1.f, 0.f, 0.f, 0.f, 0.f};
+                }
+                if (!(r2 <= L.frc2)) continue;
+                const float inv = rcp_approx(r2);
+                const float s2 = L.fs2 * inv;
+                const float s6 = s2 * s2 * s2;
+                const float c = (s6 * fmaf(2.0f, s6, -1.0f)) * (L.fe24 * inv);
+                const float u = fmaf(L.fe4, fmaf(s6, s6, -s6), -L.fuc);
+                acc.px = fmaf(-c, dx, acc.px);
+                acc.py = fmaf(-c, dy, acc.py);
+                acc.pz = fmaf(-c, dz, acc.pz);
+                acc.pe += u;
+                double4_32a* fj = P.frc + (ent[b] & JMASK);
+                atomicAdd(&fj->x, (double)(c * dx));
+                atomicAdd(&fj->y, (double)(c * dy));
+                atomicAdd(&fj->z, (double)(c * dz));
+            }
+            since += NB;
+            if (since >= MIX_FLUSH) {
+                acc.fold();
+                since = 0;
+            }
+        }
+        acc.finish();
+        atomicAdd(&P.frc[i].x, acc.fx);
+        atomicAdd(&P.frc[i].y, acc.fy);
+        atomicAdd(&P.frc[i].z, acc.fz);
+    }
+    double tot = block_sum<256>(live ? acc.e : 0.0, sh);
+    if (threadIdx.x == 0) P.pe_part[blockIdx.x] = tot;
+}
+
 // Mixed precision forces, thread per atom, with the neighbour list streamed into shared memory by
 // bulk copies (cp.async.bulk, the TMA engine's untiled mode). In the column-major list, row k of a
 // 256-atom chunk is one contiguous run of 256 words, so the chunk's list is a stack of 1 KB rows.

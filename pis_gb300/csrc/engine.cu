@@ -107,8 +107,9 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         err = "reference-order forces need the FP64 path with a full list, one thread per atom, exact arithmetic";
         return PIS_ERR_UNSUPPORTED;
     }
-    if (opt.precision == PIS_PRECISION_MIXED && half_) {
-        err = "the mixed-precision path uses a full list";
+    if (opt.precision == PIS_PRECISION_MIXED && half_ &&
+        (opt.lpa != 1 || opt.list_tma || opt.cell_tiles || opt.cluster || opt.build_cluster > 1)) {
+        err = "the mixed-precision half list is a variant of the thread-per-atom force kernel";
         return PIS_ERR_UNSUPPORTED;
     }
     if (opt.list_tma && (opt.precision != PIS_PRECISION_MIXED || opt.lpa != 1)) {
@@ -1130,6 +1131,16 @@ void Engine::launch_force_mixed(int r) {
     }
     if (opt_.list_tma && opt_.lpa == 1) {
         launch_mixed_tma(*d_, opt_.mixed_kahan, single_type_, opt_.mix_batch, ch, stream_, r);
+        return;
+    }
+    if (half_) {  // Newton-3 half list: F_j by FP64 atomics
+        if (opt_.mixed_kahan)
+            single_type_ ? k_force_mixed_half<1, true, 4><<<ch, 256, 0, stream_>>>(*d_, r)
+                         : k_force_mixed_half<1, false, 4><<<ch, 256, 0, stream_>>>(*d_, r);
+        else
+            single_type_ ? k_force_mixed_half<0, true, 4><<<ch, 256, 0, stream_>>>(*d_, r)
+                         : k_force_mixed_half<0, false, 4><<<ch, 256, 0, stream_>>>(*d_, r);
+        g_launches.fetch_add(1);
         return;
     }
 #define PIS_CALL(L) launch_mixed_t<L>(*d_, opt_.mixed_kahan, single_type_, opt_.mix_batch, ch, stream_, r)

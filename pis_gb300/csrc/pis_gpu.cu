@@ -192,8 +192,10 @@ pis_status pis_gpu_set_options(pis_gpu_ctx* ctx, int32_t list_kind, int32_t flag
                     "the cluster list needs the mixed path, one thread per cluster or one lane per member");
     if (ctx->list_tma && (ctx->precision != PIS_PRECISION_MIXED || ctx->lpa != 1))
         return fail(ctx, PIS_ERR_UNSUPPORTED, "the bulk-copy list stream needs the mixed path, thread per atom");
-    if (ctx->precision == PIS_PRECISION_MIXED && list_kind == PIS_LIST_HALF)
-        return fail(ctx, PIS_ERR_UNSUPPORTED, "the mixed-precision path uses a full list");
+    if (ctx->precision == PIS_PRECISION_MIXED && list_kind == PIS_LIST_HALF &&
+        (ctx->lpa != 1 || ctx->list_tma || ctx->cell_tiles || ctx->cluster || ctx->build_cluster > 1))
+        return fail(ctx, PIS_ERR_UNSUPPORTED,
+                    "the mixed-precision half list is a variant of the thread-per-atom force kernel");
     ctx->list_kind = list_kind;
     return PIS_OK;
 }

@@ -73,7 +73,7 @@ def test_c1_trajectory_and_energies(c1_runs):
     # step 0: the same pair terms, so the same exact sum
     assert r["pe0"] == r["pe_ref"][0]
     assert r["ke0"] == r["ke_ref"][0]
-    # every step and the end state: the benchmark spec's 1e-12 (the trajectories differ only by the
+    # every step and the end state: the FP64 bar of 1e-12 (the trajectories differ only by the
     # order of the per-atom force sums)
     assert np.max(np.abs(r["pe"] - r["pe_ref"][1:]) / np.abs(r["pe_ref"][1:])) <= 1e-12
     assert abs(r["ke"] - r["ke_ref"][-1]) <= 1e-12 * r["ke_ref"][-1]
