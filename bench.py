@@ -73,7 +73,7 @@ def parse():
     p.add_argument("--fp64-steps", type=int, default=200)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-batch", action="store_true", help="skip the 512-replica batched measurement")
-    p.add_argument("--batch-steps", type=int, default=200)
+    p.add_argument("--batch-steps", type=int, default=2000)
     p.add_argument("--no-serve", action="store_true", help="skip the served-stream measurement")
     p.add_argument("--serve-jobs", type=int, default=128)
     p.add_argument("--serve-fp64-jobs", type=int, default=12)
@@ -513,7 +513,7 @@ def run_batched(args, rank, world):
     out["tuned_options"] = tuned
     for prec, kw in (("mixed", tuned), ("fp64", {}), ("fp64_fast", {"fp64_fast": True})):
         precision = "mixed" if prec == "mixed" else "fp64"
-        k = args.batch_steps if prec == "mixed" else max(3, args.batch_steps // 5)
+        k = args.batch_steps if prec == "mixed" else max(3, args.batch_steps // 10)
         b = Batch(atoms + 1024, len(jobs), cells + 1024, precision=precision, **kw)
         for j in jobs:
             b.admit_lj(j)
