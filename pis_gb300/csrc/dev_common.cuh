@@ -345,14 +345,23 @@ __device__ __forceinline__ float4 cell_relative(const SysParams& sp, double4_32a
         min_image_full(sp.H, sp.HI, x, y, z);
         return make_float4((float)x, (float)y, (float)z, __int_as_float(type));
     }
-    double dx = p.x - (cx + 0.5) * sp.cs[0];
-    double dy = p.y - (cy + 0.5) * sp.cs[1];
-    double dz = p.z - (cz + 0.5) * sp.cs[2];
-    dx -= sp.h[0] * rint(dx * sp.hinv[0]);
-    dy -= sp.h[1] * rint(dy * sp.hinv[1]);
-    dz -= sp.h[2] * rint(dz * sp.hinv[2]);
-    // in units of the x cell edge (SysParams::sc)
-    return make_float4((float)(dx * sp.isc), (float)(dy * sp.isc), (float)(dz * sp.isc), __int_as_float(type));
+    // the offset from the cell centre in FP64 (one fused multiply-add and one subtraction per axis),
+    // then in FP32: rounded and scaled to units of the x cell edge (SysParams::sc) by 1/sc as the
+    // sum of two floats. The minimum image applies only to a position on the upper box face binned
+    // into cell 0 (an atom binned from its own position lies within half a cell of the centre).
+    double d[3] = {p.x - fma((double)cx, sp.cs[0], 0.5 * sp.cs[0]), p.y - fma((double)cy, sp.cs[1], 0.5 * sp.cs[1]),
+                   p.z - fma((double)cz, sp.cs[2], 0.5 * sp.cs[2])};
+    float q[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float f = (float)d[a];
+        q[a] = fmaf(f, sp.fisc_lo, f * sp.fisc_hi);
+        if (fabsf(q[a]) > 0.75f * sp.fcs[a]) {
+            f = (float)(d[a] - sp.h[a] * rint(d[a] * sp.hinv[a]));
+            q[a] = fmaf(f, sp.fisc_lo, f * sp.fisc_hi);
+        }
+    }
+    return make_float4(q[0], q[1], q[2], __int_as_float(type));
 }
 
 }  // namespace pis
