@@ -13,6 +13,7 @@ constexpr int JBITS = 26;                  // atom-index bits of a neighbour ent
 constexpr uint32_t JMASK = (1u << JBITS) - 1u;
 constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_SEG = SCAN_THREADS * SCAN_ITEMS;  // cells per block of the segmented scan
 constexpr int END_THREADS = 256;
 #ifndef PIS_FUSED_LQ
 #define PIS_FUSED_LQ 8
@@ -64,6 +65,8 @@ struct Engine::DevPtrs {
     int32_t hist;
     int32_t max_slots;
     int32_t zero_forces;  // half list: integrate1 clears F for the atomic scatter
+    int2* seg_tot;        // segmented cell scan: per slot and segment, (atoms, clusters) in the segment
+    int32_t max_segs;     // segments per slot in seg_tot
     int32_t full_list;
     int32_t pe_stride;    // force-kernel blocks per chunk (lanes per atom)
     // cluster-list path (clm = atoms per cluster, 0 when the per-atom list is used)

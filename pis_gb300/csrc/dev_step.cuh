@@ -141,7 +141,8 @@ __global__ void k_bin(const DP P, int respect_steps) {
 // loads and stores stay coalesced while each thread scans SCAN_ITEMS consecutive cells.
 template <bool CL>
 __device__ __forceinline__ int scan_cells(int32_t* __restrict__ cnt_g, int32_t* __restrict__ start_g, int ncell,
-                                          int carry, int clm, int* buf, int* warp_tot, int* carry_sh) {
+                                          int carry, int clm, int* buf, int* warp_tot, int* carry_sh,
+                                          bool write_total = true) {
     const int t = threadIdx.x, l = t & 31, w = t >> 5;
     const int carry0 = carry;
     for (int base = 0; base < ncell; base += SCAN_THREADS * SCAN_ITEMS) {
@@ -200,7 +201,7 @@ __device__ __forceinline__ int scan_cells(int32_t* __restrict__ cnt_g, int32_t* 
         carry += *carry_sh;
         __syncthreads();
     }
-    if (t == 0) start_g[ncell] = carry;
+    if (t == 0 && write_total) start_g[ncell] = carry;
     return carry - carry0;
 }
 
@@ -224,6 +225,74 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(const DP P, int step_mode
     scan_cells<false>(cnt_g, P.cell_start + sp.c0, ncell, (int)sp.a0, 1, buf, warp_tot, &carry_sh);
     if (threadIdx.x == 0) {
         st.ncl = ncl;
+        st.cur ^= 1;
+    }
+}
+
+// Counting sort, pass 2 for pools with a slot of more than SCAN_SEG cells, in two kernels: each
+// block scans one segment of SCAN_SEG cells of a slot from 0 and records the segment's totals;
+// k_scan_fix then adds the slot's base and the preceding segments' totals, writes the closing
+// entries and flips the slot's buffer set. The starts equal k_scan's (integer sums).
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_seg(const DP P, int step_mode) {
+    if (!rebuild_pending(P)) return;
+    const int s = blockIdx.x, seg = blockIdx.y;
+    const SysParams& sp = P.sp[s];
+    if (!sp.active) return;
+    if (!slot_runs(P, s, step_mode)) return;
+    if (!P.st[s].rebuild) return;
+    const int ncell = sp.nc[0] * sp.nc[1] * sp.nc[2];
+    const int c0 = seg * SCAN_SEG;
+    if (c0 >= ncell) return;
+    const int m = min(SCAN_SEG, ncell - c0);
+    __shared__ int buf[SCAN_THREADS * SCAN_ITEMS];
+    __shared__ int warp_tot[SCAN_THREADS / 32];
+    __shared__ int carry_sh;
+    int32_t* __restrict__ cnt_g = P.cell_count + sp.c0 + c0;
+    int ncl = 0;
+    if (P.clm) ncl = scan_cells<true>(cnt_g, P.cl_start + sp.c0 + c0, m, 0, P.clm, buf, warp_tot, &carry_sh, false);
+    const int na = scan_cells<false>(cnt_g, P.cell_start + sp.c0 + c0, m, 0, 1, buf, warp_tot, &carry_sh, false);
+    if (threadIdx.x == 0) P.seg_tot[(int64_t)s * P.max_segs + seg] = make_int2(na, ncl);
+}
+__global__ void __launch_bounds__(256) k_scan_fix(const DP P, int step_mode) {
+    if (!rebuild_pending(P)) return;
+    const int s = blockIdx.x, seg = blockIdx.y;
+    const SysParams& sp = P.sp[s];
+    if (!sp.active) return;
+    if (!slot_runs(P, s, step_mode)) return;
+    SysState& st = P.st[s];
+    if (!st.rebuild) return;
+    const int ncell = sp.nc[0] * sp.nc[1] * sp.nc[2];
+    const int nseg = (ncell + SCAN_SEG - 1) / SCAN_SEG;
+    if (seg >= nseg) return;
+    __shared__ int2 carry_sh;
+    const int2* __restrict__ tot = P.seg_tot + (int64_t)s * P.max_segs;
+    if (threadIdx.x < 32) {
+        int a = 0, c = 0;
+        for (int k = threadIdx.x; k < seg; k += 32) {
+            const int2 t = tot[k];
+            a += t.x;
+            c += t.y;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            c += __shfl_xor_sync(0xffffffffu, c, o);
+        }
+        if (threadIdx.x == 0) carry_sh = make_int2(a, c);
+    }
+    __syncthreads();
+    const int ca = (int)sp.a0 + carry_sh.x, cc = sp.cl0 + carry_sh.y;
+    const int c0 = seg * SCAN_SEG, m = min(SCAN_SEG, ncell - c0);
+    int32_t* __restrict__ sa = P.cell_start + sp.c0 + c0;
+    for (int k = threadIdx.x; k < m; k += blockDim.x) sa[k] += ca;
+    int32_t* __restrict__ sc = P.clm ? P.cl_start + sp.c0 + c0 : nullptr;
+    if (P.clm)
+        for (int k = threadIdx.x; k < m; k += blockDim.x) sc[k] += cc;
+    if (seg == nseg - 1 && threadIdx.x == 0) {
+        const int2 t = tot[seg];
+        sa[m] = ca + t.x;
+        if (P.clm) sc[m] = cc + t.y;
+        st.ncl = carry_sh.y + t.y;
         st.cur ^= 1;
     }
 }

@@ -223,6 +223,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         {(void**)&d_->ke_hist, 8 * NS * (size_t)opt.hist}, {(void**)&d_->tr_hist, 8 * NS * (size_t)opt.hist},
         {(void**)&d_->tr_part, 8 * NCH}, {(void**)&d_->kt_part, 72 * NCH},
         {(void**)&d_->ctl, 256},
+        {(void**)&d_->seg_tot, sizeof(int2) * NS * (size_t)(NC / SCAN_SEG + 2)},
     };
     if (fused_) items.push_back({&prel_buf_[1], 16 * NA});
     const bool exact = opt.precision == PIS_PRECISION_FP64;
@@ -260,6 +261,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     d_->cap = (int32_t)cap_;
     d_->hist = opt.hist;
     d_->max_slots = opt.max_slots;
+    d_->max_segs = (int32_t)(NC / SCAN_SEG + 2);
     d_->zero_forces = half_ ? 1 : 0;
     d_->full_list = half_ ? 0 : 1;
     d_->pe_stride = opt_.lpa;
@@ -816,15 +818,21 @@ pis_status Engine::rebuild_block_map(std::string& err) {
     // the force kernel variant depends on whether every slot is single-type; captured graphs
     // bake that choice in, so they are dropped when it flips (after the stream has drained)
     bool one = true, tric = false;
+    int segs = 1;  // cell-scan segments of the largest slot (the scan kernels' grid)
     for (int s = 0; s < opt_.max_slots; ++s) {
         if (hp_[s].active && hp_[s].nt != 1) one = false;
         if (hp_[s].active && hp_[s].tric) tric = true;
+        if (hp_[s].active) {
+            const int64_t nc = (int64_t)hp_[s].nc[0] * hp_[s].nc[1] * hp_[s].nc[2];
+            segs = std::max(segs, (int)((nc + SCAN_SEG - 1) / SCAN_SEG));
+        }
     }
-    if (one != single_type_ || tric != any_tric_) {
+    if (one != single_type_ || tric != any_tric_ || segs != scan_segs_) {
         st = check(cudaStreamSynchronize(stream_), "block map", err);
         if (st) return st;
         single_type_ = one;
         any_tric_ = tric;
+        scan_segs_ = segs;
         for (auto& kv : graphs_) {
             cudaGraphExecDestroy(kv.second.exec);
             for (auto e : kv.second.ev) cudaEventDestroy(e);
@@ -883,7 +891,13 @@ void Engine::enqueue_rebuild(bool respect) {
     int r = respect ? 1 : 0;
     const unsigned ga = (unsigned)max_chunks_;
     LAUNCH(k_bin, ga, opt_.blk, P, r);
-    LAUNCH(k_scan, (unsigned)opt_.max_slots, SCAN_THREADS, P, r);
+    if (scan_segs_ <= 1) {
+        LAUNCH(k_scan, (unsigned)opt_.max_slots, SCAN_THREADS, P, r);
+    } else {  // a slot of more than SCAN_SEG cells: segmented scan, one block per segment
+        const dim3 g((unsigned)opt_.max_slots, (unsigned)scan_segs_);
+        LAUNCH(k_scan_seg, g, SCAN_THREADS, P, r);
+        LAUNCH(k_scan_fix, g, 256, P, r);
+    }
     LAUNCH(k_scatter, ga, opt_.blk, P, r);
     unsigned gcells = (unsigned)((opt_.max_cells * 32 + 255) / 256);
     if (any_tric_)

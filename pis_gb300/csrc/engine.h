@@ -293,6 +293,7 @@ class Engine {
     const void* hold(const void* src, size_t bytes);
     bool single_type_ = true;  // every active slot has one atom type (selects the force kernel)
     bool any_tric_ = false;    // some active slot has a triclinic box (selects the rebuild kernels)
+    int scan_segs_ = 1;        // cell-scan segments of the largest slot (1: one scan block per slot)
     bool fused_ = false;       // mixed steps run the fused force + kick + drift kernel
     bool list_groups_ = false; // the per-atom list is stored in groups of consecutive entries
     void* prel_buf_[2] = {nullptr, nullptr};  // the two cell-relative coordinate buffers (fused steps)

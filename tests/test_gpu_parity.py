@@ -322,3 +322,27 @@ def test_mixed_orthorhombic_cells(oracle_lib, cuda_lib, nc, stretch):
     e64 = f64.verlet_step_nve(0.004, 60)
     assert np.max(np.abs(e - e64) / np.abs(e64)) <= 1e-5
     assert g.stats()["rebuilds"] >= 2
+
+
+def test_large_cell_grid_segmented_scan(oracle_lib, cuda_lib):
+    # 171,500 atoms on 21^3 = 9,261 cells: more than one 8,192-cell segment, so the cell scan runs
+    # as one block per segment plus the carry kernel. The neighbour sets and the FP64 energy (an
+    # exact sum) must equal the oracle's on the displaced lattice.
+    s = liquid(nc=35, seed=31)
+    rng = np.random.default_rng(31)
+    L = s["h"][0, 0]
+    s["pos"] = np.mod(s["pos"] + rng.normal(0, 0.05, s["pos"].shape), L)
+    assert int(L // 2.8) ** 3 > 8192
+    o = to_oracle(s)
+    pe_exact, _ = o.compute_potential_exact()
+    off, idx = o.full_list()
+    g = to_gpu(s, "fp64", list_kind="full")
+    pe, _ = g.compute_potential()
+    assert pe == pe_exact
+    go, gi = g.neighbour_list()
+    assert np.array_equal(go, off)
+    for i in range(len(off) - 1):
+        assert np.array_equal(gi[go[i]:go[i + 1]], np.sort(idx[off[i]:off[i + 1]])), i
+    m = to_gpu(s, "mixed")
+    pem, _ = m.compute_potential()
+    assert abs(pem - pe) <= 1e-6 * abs(pe)
