@@ -325,10 +325,10 @@ def test_mixed_orthorhombic_cells(oracle_lib, cuda_lib, nc, stretch):
 
 
 def test_large_cell_grid_segmented_scan(oracle_lib, cuda_lib):
-    # 171,500 atoms on 21^3 = 9,261 cells: more than one 8,192-cell segment, so the cell scan runs
+    # 186,624 atoms on 21^3 = 9,261 cells: more than one 8,192-cell segment, so the cell scan runs
     # as one block per segment plus the carry kernel. The neighbour sets and the FP64 energy (an
     # exact sum) must equal the oracle's on the displaced lattice.
-    s = liquid(nc=35, seed=31)
+    s = liquid(nc=36, seed=31)
     rng = np.random.default_rng(31)
     L = s["h"][0, 0]
     s["pos"] = np.mod(s["pos"] + rng.normal(0, 0.05, s["pos"].shape), L)
