@@ -14,6 +14,7 @@ constexpr uint32_t JMASK = (1u << JBITS) - 1u;
 constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 8;
 constexpr int SCAN_SEG = SCAN_THREADS * SCAN_ITEMS;  // cells per block of the segmented scan
+constexpr int RING_STEPS = 64;  // longest graph of fused steps (rows of the partial ring)
 constexpr int END_THREADS = 256;
 #ifndef PIS_FUSED_LQ
 #define PIS_FUSED_LQ 8
@@ -66,6 +67,8 @@ struct Engine::DevPtrs {
     int32_t max_slots;
     int32_t zero_forces;  // half list: integrate1 clears F for the atomic scatter
     int2* seg_tot;        // segmented cell scan: per slot and segment, (atoms, clusters) in the segment
+    double* ring;         // fused steps: per step of a graph, PE, KE and trace block partials
+    int64_t ring_stride;  // partials per quantity and step (the chunk count)
     int32_t max_segs;     // segments per slot in seg_tot
     int32_t full_list;
     int32_t pe_stride;    // force-kernel blocks per chunk (lanes per atom)
@@ -326,10 +329,11 @@ __device__ __forceinline__ int64_t nbr_index(int i, int k, int64_t npad) {
     return (int64_t)(k / LPA) * (npad * LPA) + (int64_t)i * LPA + (k % LPA);
 }
 
-// Step mode (nonzero): slots with steps left take part. Evaluation mode (0): only slots the host
-// marked for a force evaluation or reduction.
+// Step mode (1 + q for step q of a graph whose step counters are updated at the graph's end, 1
+// where they are updated after every step): slots with more than q steps left take part.
+// Evaluation mode (0): only slots the host marked for a force evaluation or reduction.
 __device__ __forceinline__ bool slot_runs(const DP& P, int s, int step_mode) {
-    return step_mode ? P.st[s].steps_left > 0 : P.st[s].eval != 0;
+    return step_mode ? P.st[s].steps_left > step_mode - 1 : P.st[s].eval != 0;
 }
 
 // TRIC = false: the instantiation for pools without triclinic slots (the general branch costs the

@@ -170,14 +170,18 @@ __host__ __device__ constexpr int step_list_prefetch() {
 }
 // TRACE: the instantiation launched while some slot records its thermo (the virial trace of every
 // step); the default one carries no trace code (with it the pair loop was measured 6 % slower).
+// q: the step's index in its graph. The step counters are updated once per graph (k_ring_commit),
+// so a slot takes part while it has more than q steps left, and the step's PE, KE and trace block
+// partials go to row q of the partial ring, summed per step after the graph's last step
+// (k_ring_sums) in the order k_step_end sums them.
 template <int ACC, bool ONE, int MIX_BATCH, bool DRIFT, bool TRACE>
-__global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixed(const DP P) {
+__global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixed(const DP P, int q) {
     __shared__ double sh[32];
     __shared__ float shift[12];
     int s, i;
     const bool live = atom_of(P, s, i);
     if (s < 0) return;
-    if (!slot_runs(P, s, 1)) return;
+    if (!slot_runs(P, s, 1 + q)) return;
     const SysParams& sp = P.sp[s];
     SysState& st = P.st[s];
     fill_shift_axes(shift, sp);
@@ -185,7 +189,7 @@ __global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixe
     MixAcc<ACC> acc;
     if (live)
         mixed_atom_forces<ACC, 1, ONE, MIX_BATCH, step_list_prefetch<MIX_BATCH>(), FUSED_LQ>(P, sp, i, 0, shift, acc);
-    const bool drift = DRIFT && st.steps_left > 1;
+    const bool drift = DRIFT && st.steps_left > q + 1;
     const bool want_virial = (st.want_virial & 1) != 0;
     const bool want_trace = TRACE && st.thermo != 0;
     double ke = 0.0;
@@ -216,13 +220,14 @@ __global__ void __launch_bounds__(256, step_min_blocks<MIX_BATCH>()) k_step_mixe
             P.prel_out[i] = cell_relative_moved(P, sp, i, dx, dy, dz);
         }
     }
+    double* __restrict__ ring = P.ring + (int64_t)q * 3 * P.ring_stride;
     const double pe_tot = block_sum<256>(acc.e, sh);
-    if (threadIdx.x == 0) P.pe_part[blockIdx.x] = pe_tot;
+    if (threadIdx.x == 0) ring[blockIdx.x] = pe_tot;
     const double ke_tot = block_sum<256>(ke, sh);
-    if (threadIdx.x == 0) P.ke_part[blockIdx.x] = 0.5 * ke_tot;
+    if (threadIdx.x == 0) ring[P.ring_stride + blockIdx.x] = 0.5 * ke_tot;
     if (TRACE && want_trace) {
         const double t = block_sum<256>(live ? virial_trace(p, f) : 0.0, sh);
-        if (threadIdx.x == 0) P.tr_part[blockIdx.x] = t;
+        if (threadIdx.x == 0) ring[2 * P.ring_stride + blockIdx.x] = t;
     }
     if (want_virial) {
         double r[3] = {p.x, p.y, p.z}, g[3] = {f.x, f.y, f.z};
@@ -373,6 +378,51 @@ __global__ void __launch_bounds__(END_THREADS) k_step_end(const DP P, int mode) 
             st.steps_left -= 1;
         }
     }
+}
+
+// End of a graph of fused steps, pass 1: block (slot, q) sums step q's partials from the ring (the
+// thread-strided sums and block tree of k_step_end, so every value equals the per-step reduction's)
+// into the slot's energy history, and flags a NaN. The counters are still the graph's start values.
+__global__ void __launch_bounds__(END_THREADS) k_ring_sums(const DP P) {
+    __shared__ double sh[32];
+    const int s = blockIdx.x, q = blockIdx.y;
+    const SysParams& sp = P.sp[s];
+    if (!sp.active) return;
+    SysState& st = P.st[s];
+    if (st.steps_left <= q) return;
+    const double* __restrict__ r = P.ring + (int64_t)q * 3 * P.ring_stride;
+    double pe = 0.0, ke = 0.0, tr = 0.0;
+    for (int c = threadIdx.x; c < sp.nch; c += END_THREADS) pe += r[sp.ch0 + c];
+    for (int c = threadIdx.x; c < sp.nch; c += END_THREADS) ke += r[P.ring_stride + sp.ch0 + c];
+    pe = block_sum<END_THREADS>(pe, sh);
+    ke = block_sum<END_THREADS>(ke, sh);
+    if (st.thermo) {
+        for (int c = threadIdx.x; c < sp.nch; c += END_THREADS) tr += r[2 * P.ring_stride + sp.ch0 + c];
+        tr = block_sum<END_THREADS>(tr, sh);
+    }
+    if (threadIdx.x == 0) {
+        if (P.full_list) pe *= 0.5;
+        const int64_t h = (int64_t)s * P.hist + (st.steps_done + q) % P.hist;
+        P.pe_hist[h] = pe;
+        P.ke_hist[h] = ke;
+        if (st.thermo) P.tr_hist[h] = tr;
+        if (pe != pe || ke != ke) atomicOr(&st.flags, FLAG_NAN);
+    }
+}
+// Pass 2, thread per slot: the last step's energies into the state, and the counters advanced by
+// the steps the slot took in the graph (g steps, or fewer if its run ended inside the graph).
+__global__ void k_ring_commit(const DP P, int g) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= P.max_slots || !P.sp[s].active) return;
+    SysState& st = P.st[s];
+    const int64_t left = st.steps_left;
+    if (left <= 0) return;
+    const int64_t n = left < g ? left : g;
+    const int64_t h = (int64_t)s * P.hist + (st.steps_done + n - 1) % P.hist;
+    st.pe = P.pe_hist[h];
+    st.ke = P.ke_hist[h];
+    st.steps_done += n;
+    st.steps_left -= n;
 }
 
 // End of a rebuild phase (its last kernel, so every rebuild kernel has read the request flags):

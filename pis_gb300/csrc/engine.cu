@@ -225,7 +225,10 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         {(void**)&d_->ctl, 256},
         {(void**)&d_->seg_tot, sizeof(int2) * NS * (size_t)(NC / SCAN_SEG + 2)},
     };
-    if (fused_) items.push_back({&prel_buf_[1], 16 * NA});
+    if (fused_) {
+        items.push_back({&prel_buf_[1], 16 * NA});
+        items.push_back({(void**)&d_->ring, 8 * 3 * (size_t)RING_STEPS * NCH});
+    }
     const bool exact = opt.precision == PIS_PRECISION_FP64;
     if (exact) {
         items.push_back({(void**)&d_->xpe_part, 8 * XS_WORDS * NCH * 32});
@@ -262,6 +265,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     d_->hist = opt.hist;
     d_->max_slots = opt.max_slots;
     d_->max_segs = (int32_t)(NC / SCAN_SEG + 2);
+    d_->ring_stride = (int64_t)NCH;
     d_->zero_forces = half_ ? 1 : 0;
     d_->full_list = half_ ? 0 : 1;
     d_->pe_stride = opt_.lpa;
@@ -886,9 +890,9 @@ pis_status Engine::set_steps(int slot, int64_t steps, std::string& err) {
     return sync(err);
 }
 
-void Engine::enqueue_rebuild(bool respect) {
+void Engine::enqueue_rebuild(bool respect, int q) {
     const DP& P = *d_;
-    int r = respect ? 1 : 0;
+    int r = respect ? 1 + q : 0;
     const unsigned ga = (unsigned)max_chunks_;
     LAUNCH(k_bin, ga, opt_.blk, P, r);
     if (scan_segs_ <= 1) {
@@ -1195,13 +1199,16 @@ void Engine::enqueue_step(bool respect, cudaEvent_t* ev, int64_t q, int64_t g) {
         d_->prel = (float4*)prel_buf_[q & 1];
         d_->prel_out = (float4*)prel_buf_[(q + 1) & 1];
     }
+    // fused steps keep the step counters fixed through the graph: the rebuild kernels of step q
+    // see the slots with more than q steps left
+    const int qs = fused ? (int)q : 0;
     if (cond_step_)
-        cond_error_ = cond_error_ ? cond_error_ : enqueue_rebuild_conditional(respect);
+        cond_error_ = cond_error_ ? cond_error_ : enqueue_rebuild_conditional(respect, qs);
     else
-        enqueue_rebuild(respect);
+        enqueue_rebuild(respect, qs);
     if (ev) cudaEventRecordWithFlags(ev[2], stream_, cudaEventRecordExternal);
     if (fused)
-        launch_step_mixed(q + 1 < g);
+        launch_step_mixed(q + 1 < g, (int)q);
     else if (mixed)
         launch_force_mixed(r);
     else
@@ -1214,7 +1221,7 @@ void Engine::enqueue_step(bool respect, cudaEvent_t* ev, int64_t q, int64_t g) {
             LAUNCH((k_integrate2<true, true>), (unsigned)max_chunks_, opt_.blk, P, r);
     }
     if (ev) cudaEventRecordWithFlags(ev[4], stream_, cudaEventRecordExternal);
-    launch_step_end(0);
+    if (!fused) launch_step_end(0);  // fused steps: k_ring_sums / k_ring_commit after the graph's last step
     if (ev) cudaEventRecordWithFlags(ev[5], stream_, cudaEventRecordExternal);
     if (fused) {
         d_->prel = (float4*)prel_buf_[0];
@@ -1223,18 +1230,18 @@ void Engine::enqueue_step(bool respect, cudaEvent_t* ev, int64_t q, int64_t g) {
 }
 
 template <int ACC, bool ONE, int B, bool TRACE>
-static void launch_step_mixed_tt(const DP& P, bool drift, unsigned chunks, cudaStream_t st) {
+static void launch_step_mixed_tt(const DP& P, bool drift, int q, unsigned chunks, cudaStream_t st) {
     if (drift)
-        k_step_mixed<ACC, ONE, B, true, TRACE><<<chunks, 256, 0, st>>>(P);
+        k_step_mixed<ACC, ONE, B, true, TRACE><<<chunks, 256, 0, st>>>(P, q);
     else
-        k_step_mixed<ACC, ONE, B, false, TRACE><<<chunks, 256, 0, st>>>(P);
+        k_step_mixed<ACC, ONE, B, false, TRACE><<<chunks, 256, 0, st>>>(P, q);
 }
 template <int ACC, bool ONE, int B>
-static void launch_step_mixed_t(const DP& P, bool drift, bool trace, unsigned chunks, cudaStream_t st) {
+static void launch_step_mixed_t(const DP& P, bool drift, bool trace, int q, unsigned chunks, cudaStream_t st) {
     if (trace)
-        launch_step_mixed_tt<ACC, ONE, B, true>(P, drift, chunks, st);
+        launch_step_mixed_tt<ACC, ONE, B, true>(P, drift, q, chunks, st);
     else
-        launch_step_mixed_tt<ACC, ONE, B, false>(P, drift, chunks, st);
+        launch_step_mixed_tt<ACC, ONE, B, false>(P, drift, q, chunks, st);
 }
 
 void Engine::launch_step_end(int mode) {
@@ -1244,24 +1251,24 @@ void Engine::launch_step_end(int mode) {
         LAUNCH(k_step_end<false>, (unsigned)opt_.max_slots, END_THREADS, *d_, mode);
 }
 
-void Engine::launch_step_mixed(bool drift) {
+void Engine::launch_step_mixed(bool drift, int q) {
     const unsigned ch = (unsigned)max_chunks_;
     const bool b8 = opt_.mix_batch == 8;
     const bool tr = thermo_slots_ > 0;
     if (opt_.mixed_kahan) {
         if (single_type_)
-            b8 ? launch_step_mixed_t<1, true, 8>(*d_, drift, tr, ch, stream_)
-               : launch_step_mixed_t<1, true, 4>(*d_, drift, tr, ch, stream_);
+            b8 ? launch_step_mixed_t<1, true, 8>(*d_, drift, tr, q, ch, stream_)
+               : launch_step_mixed_t<1, true, 4>(*d_, drift, tr, q, ch, stream_);
         else
-            b8 ? launch_step_mixed_t<1, false, 8>(*d_, drift, tr, ch, stream_)
-               : launch_step_mixed_t<1, false, 4>(*d_, drift, tr, ch, stream_);
+            b8 ? launch_step_mixed_t<1, false, 8>(*d_, drift, tr, q, ch, stream_)
+               : launch_step_mixed_t<1, false, 4>(*d_, drift, tr, q, ch, stream_);
     } else {
         if (single_type_)
-            b8 ? launch_step_mixed_t<0, true, 8>(*d_, drift, tr, ch, stream_)
-               : launch_step_mixed_t<0, true, 4>(*d_, drift, tr, ch, stream_);
+            b8 ? launch_step_mixed_t<0, true, 8>(*d_, drift, tr, q, ch, stream_)
+               : launch_step_mixed_t<0, true, 4>(*d_, drift, tr, q, ch, stream_);
         else
-            b8 ? launch_step_mixed_t<0, false, 8>(*d_, drift, tr, ch, stream_)
-               : launch_step_mixed_t<0, false, 4>(*d_, drift, tr, ch, stream_);
+            b8 ? launch_step_mixed_t<0, false, 8>(*d_, drift, tr, q, ch, stream_)
+               : launch_step_mixed_t<0, false, 4>(*d_, drift, tr, q, ch, stream_);
     }
     g_launches.fetch_add(1);
 }
@@ -1283,7 +1290,7 @@ void Engine::enqueue_potential(int only) {
 // then a conditional IF node whose body (the rebuild kernels, captured on side_) runs only when
 // some slot rebuilds. On the ~8 steps in 9 without a rebuild the step then launches no rebuild
 // kernel at all.
-pis_status Engine::enqueue_rebuild_conditional(bool respect) {
+pis_status Engine::enqueue_rebuild_conditional(bool respect, int q) {
     cudaStreamCaptureStatus cs;
     unsigned long long id = 0;
     cudaGraph_t g = nullptr;
@@ -1311,7 +1318,7 @@ pis_status Engine::enqueue_rebuild_conditional(bool respect) {
         return PIS_ERR_CUDA;
     const int64_t before = g_launches.load();
     ls_ = side_;
-    enqueue_rebuild(respect);
+    enqueue_rebuild(respect, q);
     ls_ = stream_;
     const int64_t n_body = g_launches.load() - before;
     g_launches.fetch_sub(n_body);  // counted when a body actually runs (account_body_launches)
@@ -1396,7 +1403,8 @@ void Engine::reset_stage_times() {
 pis_status Engine::run(int64_t k, std::string& err) {
     pis_status st = rebuild_block_map(err);
     if (st) return st;
-    const int64_t G = graph_steps_;
+    // fused steps: a graph holds at most RING_STEPS steps (the rows of the partial ring)
+    const int64_t G = (fused_ && graph_steps_ > RING_STEPS) ? RING_STEPS : graph_steps_;
     while (k > 0) {
         int64_t g = k >= G ? G : k;
         // graphs differ by length, instrumentation and whether the fused step records thermo
@@ -1405,7 +1413,7 @@ pis_status Engine::run(int64_t k, std::string& err) {
         if (it == graphs_.end()) {
             GraphRec rec;
             if (instrument_) {
-                rec.ev.resize((size_t)(6 * g));
+                rec.ev.resize((size_t)(6 * g + 1));  // + the end of the graph's ring kernels
                 for (auto& e : rec.ev) {
                     st = check(cudaEventCreate(&e), "event", err);
                     if (st) return st;
@@ -1421,6 +1429,12 @@ pis_status Engine::run(int64_t k, std::string& err) {
                 for (int64_t q = 0; q < g; ++q)
                     enqueue_step(true, instrument_ ? rec.ev.data() + 6 * q : nullptr, q, g);
                 cond_step_ = false;
+                if (fused_ && opt_.precision == PIS_PRECISION_MIXED) {
+                    // the step ends of the graph's fused steps: energies per step, then counters
+                    LAUNCH(k_ring_sums, dim3((unsigned)opt_.max_slots, (unsigned)g), END_THREADS, *d_);
+                    LAUNCH(k_ring_commit, (unsigned)((opt_.max_slots + 127) / 128), 128, *d_, (int)g);
+                }
+                if (instrument_) cudaEventRecordWithFlags(rec.ev[6 * g], stream_, cudaEventRecordExternal);
                 int64_t captured = g_launches.load() - before;
                 g_launches.fetch_sub(captured);
                 rec.kernels = captured;
@@ -1456,6 +1470,11 @@ pis_status Engine::run(int64_t k, std::string& err) {
                     if (st) return st;
                     stage_ms_[t] += ms;
                 }
+            // the ring kernels (fused steps) belong to the step-end stage
+            float ms = 0.f;
+            st = check(cudaEventElapsedTime(&ms, it->second.ev[6 * g - 1], it->second.ev[6 * g]), "event timing", err);
+            if (st) return st;
+            stage_ms_[4] += ms;
             stage_steps_ += g;
         }
         k -= g;

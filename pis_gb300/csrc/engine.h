@@ -227,16 +227,16 @@ class Engine {
     pis_status rebuild_block_map(std::string& err);
     // Step q of a g-step graph.
     void enqueue_step(bool respect_steps, cudaEvent_t* ev, int64_t q, int64_t g);
-    void enqueue_rebuild(bool respect_steps);
+    void enqueue_rebuild(bool respect_steps, int q = 0);
     // The rebuild kernels of a captured step inside a conditional graph node that runs only when
     // some slot rebuilds in that step (the condition is set on the device).
-    pis_status enqueue_rebuild_conditional(bool respect_steps);
+    pis_status enqueue_rebuild_conditional(bool respect_steps, int q = 0);
     // Conditional rebuild bodies executed since the last call, counted on the device.
     void account_body_launches();
     void enqueue_potential(int only);
     void launch_force_fp64(int respect_steps);
     void launch_force_mixed(int respect_steps);
-    void launch_step_mixed(bool drift);
+    void launch_step_mixed(bool drift, int q);
     void launch_step_end(int mode);
     void launch_build(int respect_steps);
     void launch_force_cluster(int respect_steps);
