@@ -577,12 +577,14 @@ def job_errors(jobs, pick, steps, tuned, chunk=500, melt=300):
     for q, (r, j) in enumerate(zip(pick, sel)):
         n = 4 * j.k ** 3
         f64, fm = res["fp64"][0][q], res["mixed"][0][q]
-        d64 = drift_stats(np.array(res["fp64"][1][q]), n, chunk)["drift_per_atom_per_1e4_steps"]
-        dm = drift_stats(np.array(res["mixed"][1][q]), n, chunk)["drift_per_atom_per_1e4_steps"]
+        s64 = drift_stats(np.array(res["fp64"][1][q]), n, chunk)
+        sm = drift_stats(np.array(res["mixed"][1][q]), n, chunk)
         reps.append({"job": r, "atoms": n, "rho": j.rho, "t_star": j.t_star,
                      "force_rms_rel": float(np.sqrt(np.sum((fm["force"] - f64["force"]) ** 2) / np.sum(f64["force"] ** 2))),
                      "pe_rel": abs(fm["pe"] - f64["pe"]) / abs(f64["pe"]),
-                     "drift_fp64": d64, "drift_mixed": dm})
+                     "drift_fp64": s64["drift_per_atom_per_1e4_steps"], "drift_mixed": sm["drift_per_atom_per_1e4_steps"],
+                     "drift_fit_stderr_fp64": s64["fit_stderr_per_atom_per_1e4_steps"],
+                     "drift_fit_stderr_mixed": sm["fit_stderr_per_atom_per_1e4_steps"]})
     summary = {"jobs": len(reps), "steps": steps, "melt_steps": melt,
                "max_force_rms_rel": max(x["force_rms_rel"] for x in reps),
                "max_pe_rel": max(x["pe_rel"] for x in reps),
@@ -610,9 +612,15 @@ def energy_series(ctx, steps, chunk):
 
 
 def drift_stats(e, n, chunk):
+    """Slope of a linear fit of E(t) per atom per 10^4 steps, with the fit's standard error (the
+    residuals are the energy's own fluctuation, which per atom grows as N shrinks; being
+    correlated in time they make this a lower bound on the slope's uncertainty)."""
     t = np.arange(len(e)) * chunk
-    slope = np.polyfit(t, e, 1)[0]
-    return {"drift_per_atom_per_1e4_steps": float(slope * 1e4 / n), "max_abs_dev_per_atom": float(np.abs(e - e[0]).max() / n)}
+    slope, icpt = np.polyfit(t, e, 1)
+    res = e - (slope * t + icpt)
+    se = np.sqrt(np.sum(res ** 2) / max(len(e) - 2, 1) / np.sum((t - t.mean()) ** 2)) if len(e) > 2 else 0.0
+    return {"drift_per_atom_per_1e4_steps": float(slope * 1e4 / n), "fit_stderr_per_atom_per_1e4_steps": float(se * 1e4 / n),
+            "max_abs_dev_per_atom": float(np.abs(e - e[0]).max() / n)}
 
 
 def run_drift(args, melt_pos, melt_vel, types, h, tuned):
