@@ -821,22 +821,24 @@ pis_status Engine::rebuild_block_map(std::string& err) {
     dirty_map_ = false;
     // the force kernel variant depends on whether every slot is single-type; captured graphs
     // bake that choice in, so they are dropped when it flips (after the stream has drained)
-    bool one = true, tric = false;
+    bool one = true, tric = false, gen = false;
     int segs = 1;  // cell-scan segments of the largest slot (the scan kernels' grid)
     for (int s = 0; s < opt_.max_slots; ++s) {
         if (hp_[s].active && hp_[s].nt != 1) one = false;
         if (hp_[s].active && hp_[s].tric) tric = true;
+        if (hp_[s].active && !hp_[s].walk27) gen = true;
         if (hp_[s].active) {
             const int64_t nc = (int64_t)hp_[s].nc[0] * hp_[s].nc[1] * hp_[s].nc[2];
             segs = std::max(segs, (int)((nc + SCAN_SEG - 1) / SCAN_SEG));
         }
     }
-    if (one != single_type_ || tric != any_tric_ || segs != scan_segs_) {
+    if (one != single_type_ || tric != any_tric_ || segs != scan_segs_ || gen != any_generic_) {
         st = check(cudaStreamSynchronize(stream_), "block map", err);
         if (st) return st;
         single_type_ = one;
         any_tric_ = tric;
         scan_segs_ = segs;
+        any_generic_ = gen;
         for (auto& kv : graphs_) {
             cudaGraphExecDestroy(kv.second.exec);
             for (auto e : kv.second.ev) cudaEventDestroy(e);
@@ -923,19 +925,20 @@ static void launch_build1(const DP& P, bool tric, unsigned g, cudaStream_t st, i
         k_build1<HALF, false><<<g, 256, 0, st>>>(P, r, only_two_cell);
 }
 
+// generic: some slot needs the generic walk (its kernel is launched only then).
 template <int L>
-static void launch_build_t(const DP& P, bool half, bool tric, unsigned chunks, cudaStream_t st, int r) {
+static void launch_build_t(const DP& P, bool half, bool tric, unsigned chunks, cudaStream_t st, int r, bool generic) {
     const unsigned g = chunks * L;
     if (L == 1) {
-        // lean kernel for slots with >= 3 cells per axis, generic kernel for the rest
+        // lean kernel for the 27-cell walk, generic kernel for the other slots
         if (half) {
             launch_build1<true>(P, tric, g, st, r, 0);
-            k_build1_generic<true><<<g, 256, 0, st>>>(P, r);
+            if (generic) k_build1_generic<true><<<g, 256, 0, st>>>(P, r);
         } else {
             launch_build1<false>(P, tric, g, st, r, 0);
-            k_build1_generic<false><<<g, 256, 0, st>>>(P, r);
+            if (generic) k_build1_generic<false><<<g, 256, 0, st>>>(P, r);
         }
-        g_launches.fetch_add(2);
+        g_launches.fetch_add(generic ? 2 : 1);
         return;
     }
     if (half)
@@ -1083,7 +1086,7 @@ void Engine::launch_build(int r) {
         g_launches.fetch_add(4);
         return;
     }
-#define PIS_CALL(L) launch_build_t<L>(*d_, half_, any_tric_, ch, ls_, r)
+#define PIS_CALL(L) launch_build_t<L>(*d_, half_, any_tric_, ch, ls_, r, any_generic_)
     PIS_LPA_DISPATCH(opt_.lpa, PIS_CALL)
 #undef PIS_CALL
 }
@@ -1896,6 +1899,7 @@ pis_status Engine::scale_box(int slot, const double* m, std::string& err) {
     if (st) return st;
     LAUNCH(k_scale_pos, (unsigned)max_chunks_, opt_.blk, *d_, slot, hi_old, h_new, full);
     if (p.tric && !any_tric_) dirty_map_ = true;  // the next launch selects the triclinic kernels
+    if (!p.walk27 && !any_generic_) dirty_map_ = true;  // ... or launches the generic list walk
     hp_[slot] = p;
     st = check(cudaMemcpyAsync(d_->sp + slot, &hp_[slot], sizeof(SysParams), cudaMemcpyHostToDevice, stream_),
                "params", err);

@@ -294,6 +294,7 @@ class Engine {
     bool single_type_ = true;  // every active slot has one atom type (selects the force kernel)
     bool any_tric_ = false;    // some active slot has a triclinic box (selects the rebuild kernels)
     int scan_segs_ = 1;        // cell-scan segments of the largest slot (1: one scan block per slot)
+    bool any_generic_ = false; // some active slot needs the generic list walk (not the 27-cell walk)
     bool fused_ = false;       // mixed steps run the fused force + kick + drift kernel
     bool list_groups_ = false; // the per-atom list is stored in groups of consecutive entries
     void* prel_buf_[2] = {nullptr, nullptr};  // the two cell-relative coordinate buffers (fused steps)
