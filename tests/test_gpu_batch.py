@@ -109,6 +109,23 @@ def test_served_stream_results_match_alone(cuda_lib):
     b.close()
 
 
+def test_serve_graphs_longer_than_the_partial_ring(cuda_lib):
+    # 150 steps per serving iteration run as fused graphs of at most 64 steps (the rows of the
+    # per-step partial ring whose sums end each graph): results equal the jobs run alone
+    from pis_gb300.batch import lj_job
+    reqs = [(0.0, lj_job(5, 0.85, 0.9, 170, 41)), (0.0, lj_job(6, 0.8, 1.1, 130, 42)),
+            (0.0, lj_job(5, 0.9, 0.7, 64, 43))]
+    b = _batch(atoms=3000, slots=3)
+    res, _ = b.serve(reqs, graph_steps=150)
+    st = b.serve_stats()
+    b.close()
+    assert st["atom_steps"] == sum(4 * job.k ** 3 * job.steps for _, job in reqs)
+    for (_, job), r in zip(reqs, res):
+        assert r["status"] == 0 and r["steps"] == job.steps
+        alone = _run_alone(job.k, job.rho, job.t_star, job.seed, job.steps)
+        assert r["pe"] == alone["pe"] and r["ke"] == alone["ke"]
+
+
 def test_serve_accounting_at_saturation(cuda_lib):
     # six jobs at once on two slots: the first graphs run while requests wait for a slot
     from pis_gb300.batch import lj_job
