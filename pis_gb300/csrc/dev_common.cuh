@@ -87,7 +87,10 @@ struct Engine::DevPtrs {
     int32_t lq;           // list layout: entry k of atom i at (k / lq) * npad * lq + i * lq + k % lq
                           // (lq = lanes per atom for lanes-per-atom pools, FUSED_LQ for the fused
                           // step's pools, whose kernels read 4 entries of a batch as one 16-byte word)
-    int32_t* ctl;         // ctl[0]: some slot rebuilds its list in the current step or evaluation
+    int32_t* ctl;         // ctl[0]: some slot rebuilds its list in the current step or evaluation;
+                          // ctl[8], ctl[9]: listed chunks and cells of the rebuilding slots
+    int32_t* rb_list;     // listed rebuild: chunk ids, then (from rb_cells_off) cell entries
+    int64_t rb_cells_off;
     // fused step: cell-relative coordinates of the drifted atoms go to prel_out (the buffer the next
     // step reads)
     float4* prel_out;

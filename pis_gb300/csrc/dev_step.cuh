@@ -134,6 +134,56 @@ __global__ void k_bin(const DP P, int respect_steps) {
     if (!rebuild_block(P, P.blk_sys, blockIdx.x)) return;
     bin_chunk(P, blockIdx.x, respect_steps);
 }
+// Replica pools: the first kernel of a rebuild lists the chunks and cells of the rebuilding slots
+// (block per slot), and the rebuild kernels run a grid sized to the GPU that strides over the
+// list, instead of a block per chunk (per cell for the sort) of the whole pool: in a replica mix a
+// few slots rebuild per step, and the blocks of the others only exit. A slot's place in the list
+// is the count of rebuilding slots' chunks (cells) placed before it in the pool's chunk order, so
+// the list keeps that order (slots with the most atoms per cell first); every chunk and cell is
+// processed on its own, so results do not depend on the grid. k_rebuild_done clears the counts.
+__global__ void __launch_bounds__(256) k_rebuild_list(const DP P, int step_mode) {
+    __shared__ int part[2][8];
+    const int s = blockIdx.x;
+    if (!rebuild_pending(P)) return;
+    const SysParams& sp = P.sp[s];
+    if (!sp.active || !slot_runs(P, s, step_mode) || !P.st[s].rebuild) return;  // uniform per block
+    int bc = 0, bg = 0;
+    for (int t = threadIdx.x; t < P.max_slots; t += blockDim.x) {
+        const SysParams& o = P.sp[t];
+        if (o.active && o.ch0 < sp.ch0 && slot_runs(P, t, step_mode) && P.st[t].rebuild) {
+            bc += o.nch;
+            bg += o.nc[0] * o.nc[1] * o.nc[2];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        bc += __shfl_xor_sync(0xffffffffu, bc, o);
+        bg += __shfl_xor_sync(0xffffffffu, bg, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        part[0][threadIdx.x >> 5] = bc;
+        part[1][threadIdx.x >> 5] = bg;
+    }
+    __syncthreads();
+    bc = 0;
+    bg = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        bc += part[0][w];
+        bg += part[1][w];
+    }
+    const int ncell = sp.nc[0] * sp.nc[1] * sp.nc[2];
+    if (threadIdx.x == 0) {
+        atomicAdd(&P.ctl[8], sp.nch);
+        atomicAdd(&P.ctl[9], ncell);
+    }
+    for (int k = threadIdx.x; k < sp.nch; k += blockDim.x) P.rb_list[bc + k] = sp.ch0 + k;
+    int32_t* __restrict__ cells = P.rb_list + P.rb_cells_off;
+    for (int k = threadIdx.x; k < ncell; k += blockDim.x) cells[bg + k] = (int32_t)(sp.c0 + k);
+}
+__global__ void k_bin_list(const DP P, int respect_steps) {
+    const int n = P.ctl[8];
+    for (int q = blockIdx.x; q < n; q += gridDim.x) bin_chunk(P, P.rb_list[q], respect_steps);
+}
 
 // One exclusive scan over a slot's cells: of the atom counts (CL = 0, the last pass, which also
 // clears the counts) or of the cluster counts ceil(count / clm) (CL = 1). Writes absolute indices
@@ -311,6 +361,10 @@ __global__ void k_scatter(const DP P, int respect_steps) {
     if (!rebuild_block(P, P.blk_sys, blockIdx.x)) return;
     scatter_chunk(P, blockIdx.x, respect_steps);
 }
+__global__ void k_scatter_list(const DP P, int respect_steps) {
+    const int n = P.ctl[8];
+    for (int q = blockIdx.x; q < n; q += gridDim.x) scatter_chunk(P, P.rb_list[q], respect_steps);
+}
 
 // Order key of an atom inside its cell: the Morton index of its sub-cell on a 4 x 4 x 4 grid over
 // the cell (6 bits, coarse bits high) above its original id (26 bits). Atoms that are consecutive
@@ -435,6 +489,14 @@ __global__ void k_gather(const DP P, int64_t max_cells, int respect_steps) {
     __shared__ uint32_t keybuf[256 / 32][GATHER_SMEM_KEYS];
     const int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (g < max_cells && rebuild_block(P, P.cell_sys, g)) gather_cell<TRIC>(P, g, respect_steps, keybuf[threadIdx.x >> 5]);
+}
+template <bool TRIC>
+__global__ void k_gather_list(const DP P, int respect_steps) {
+    __shared__ uint32_t keybuf[256 / 32][GATHER_SMEM_KEYS];
+    const int n = P.ctl[9];
+    const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), nw = (int)((gridDim.x * blockDim.x) >> 5);
+    const int32_t* __restrict__ cells = P.rb_list + P.rb_cells_off;
+    for (int q = w; q < n; q += nw) gather_cell<TRIC>(P, cells[q], respect_steps, keybuf[threadIdx.x >> 5]);
 }
 
 // Neighbour-list build at rcut + skin. LPA lanes share one home atom (atoms in cell order, so
@@ -688,6 +750,20 @@ __global__ void __launch_bounds__(256) k_build1_generic(const DP P, int step_mod
     const SysParams& sp = P.sp[s];
     if (sp.walk27) return;
     k_build_body<HALF, 1>(P, blockIdx.x, step_mode);
+}
+// The two list builds over the listed chunks of a replica pool's rebuilding slots.
+template <bool HALF, bool TRIC>
+__global__ void __launch_bounds__(256) k_build1_list(const DP P, int step_mode) {
+    const int n = P.ctl[8];
+    for (int q = blockIdx.x; q < n; q += gridDim.x) build1_chunk<HALF, TRIC>(P, P.rb_list[q], step_mode);
+}
+template <bool HALF>
+__global__ void __launch_bounds__(256) k_build1_generic_list(const DP P, int step_mode) {
+    const int n = P.ctl[8];
+    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+        const int blk = P.rb_list[q];
+        if (!P.sp[P.blk_sys[blk]].walk27) k_build_body<HALF, 1>(P, blk, step_mode);
+    }
 }
 
 // FP64 forces: the pair evaluation of LJVOffsetManager (src/potentials/lennard_jones.rs:214-235),

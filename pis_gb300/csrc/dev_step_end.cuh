@@ -430,7 +430,11 @@ __global__ void k_ring_commit(const DP P, int g) {
 // runs later in the same step (the fused step kernel) may raise them again for the next step.
 __global__ void k_rebuild_done(const DP P, int step_mode) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s == 0) P.ctl[0] = 0;
+    if (s == 0) {
+        P.ctl[0] = 0;
+        P.ctl[8] = 0;  // the listed rebuild's counts
+        P.ctl[9] = 0;
+    }
     if (s >= P.max_slots || !P.sp[s].active) return;
     if (!slot_runs(P, s, step_mode)) return;
     SysState& st = P.st[s];

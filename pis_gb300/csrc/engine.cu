@@ -229,6 +229,18 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         items.push_back({&prel_buf_[1], 16 * NA});
         items.push_back({(void**)&d_->ring, 8 * 3 * (size_t)RING_STEPS * NCH});
     }
+    // replica pools: the rebuild kernels stride over a list of the rebuilding slots' chunks and
+    // cells (1.054 vs 1.078 ms per step of the 512-replica mix)
+    listed_ = opt.max_slots > 1 && opt.lpa == 1 && !opt.cluster && !clm_;
+    if (listed_) {
+        items.push_back({(void**)&d_->rb_list, 4 * (NCH + NC)});
+        int dev = 0, sms = 0;
+        st = check(cudaGetDevice(&dev), "device query", err);
+        if (st) return st;
+        st = check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device query", err);
+        if (st) return st;
+        listed_grid_ = 4 * sms;  // resident blocks of the 64-register build and gather kernels
+    }
     const bool exact = opt.precision == PIS_PRECISION_FP64;
     if (exact) {
         items.push_back({(void**)&d_->xpe_part, 8 * XS_WORDS * NCH * 32});
@@ -266,6 +278,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
     d_->max_slots = opt.max_slots;
     d_->max_segs = (int32_t)(NC / SCAN_SEG + 2);
     d_->ring_stride = (int64_t)NCH;
+    d_->rb_cells_off = (int64_t)NCH;
     d_->zero_forces = half_ ? 1 : 0;
     d_->full_list = half_ ? 0 : 1;
     d_->pe_stride = opt_.lpa;
@@ -896,7 +909,13 @@ void Engine::enqueue_rebuild(bool respect, int q) {
     const DP& P = *d_;
     int r = respect ? 1 + q : 0;
     const unsigned ga = (unsigned)max_chunks_;
-    LAUNCH(k_bin, ga, opt_.blk, P, r);
+    const unsigned gl = (unsigned)listed_grid_;
+    if (listed_) {
+        LAUNCH(k_rebuild_list, (unsigned)opt_.max_slots, 256, P, r);
+        LAUNCH(k_bin_list, gl, opt_.blk, P, r);
+    } else {
+        LAUNCH(k_bin, ga, opt_.blk, P, r);
+    }
     if (scan_segs_ <= 1) {
         LAUNCH(k_scan, (unsigned)opt_.max_slots, SCAN_THREADS, P, r);
     } else {  // a slot of more than SCAN_SEG cells: segmented scan, one block per segment
@@ -904,12 +923,20 @@ void Engine::enqueue_rebuild(bool respect, int q) {
         LAUNCH(k_scan_seg, g, SCAN_THREADS, P, r);
         LAUNCH(k_scan_fix, g, 256, P, r);
     }
-    LAUNCH(k_scatter, ga, opt_.blk, P, r);
     unsigned gcells = (unsigned)((opt_.max_cells * 32 + 255) / 256);
-    if (any_tric_)
-        LAUNCH(k_gather<true>, gcells, 256, P, (int64_t)opt_.max_cells, r);
-    else
-        LAUNCH(k_gather<false>, gcells, 256, P, (int64_t)opt_.max_cells, r);
+    if (listed_) {
+        LAUNCH(k_scatter_list, gl, opt_.blk, P, r);
+        if (any_tric_)
+            LAUNCH(k_gather_list<true>, gl, 256, P, r);
+        else
+            LAUNCH(k_gather_list<false>, gl, 256, P, r);
+    } else {
+        LAUNCH(k_scatter, ga, opt_.blk, P, r);
+        if (any_tric_)
+            LAUNCH(k_gather<true>, gcells, 256, P, (int64_t)opt_.max_cells, r);
+        else
+            LAUNCH(k_gather<false>, gcells, 256, P, (int64_t)opt_.max_cells, r);
+    }
     launch_build(r);
     LAUNCH(k_rebuild_done, (unsigned)((opt_.max_slots + 127) / 128), 128, P, r);
 }
@@ -925,10 +952,26 @@ static void launch_build1(const DP& P, bool tric, unsigned g, cudaStream_t st, i
         k_build1<HALF, false><<<g, 256, 0, st>>>(P, r, only_two_cell);
 }
 
-// generic: some slot needs the generic walk (its kernel is launched only then).
+// generic: some slot needs the generic walk (its kernel is launched only then). listed > 0: the
+// grid of the listed rebuild of a replica pool.
 template <int L>
-static void launch_build_t(const DP& P, bool half, bool tric, unsigned chunks, cudaStream_t st, int r, bool generic) {
+static void launch_build_t(const DP& P, bool half, bool tric, unsigned chunks, cudaStream_t st, int r, bool generic,
+                           unsigned listed) {
     const unsigned g = chunks * L;
+    if (L == 1 && listed) {
+        if (half)
+            tric ? k_build1_list<true, true><<<listed, 256, 0, st>>>(P, r) : k_build1_list<true, false><<<listed, 256, 0, st>>>(P, r);
+        else
+            tric ? k_build1_list<false, true><<<listed, 256, 0, st>>>(P, r) : k_build1_list<false, false><<<listed, 256, 0, st>>>(P, r);
+        if (generic) {
+            if (half)
+                k_build1_generic_list<true><<<listed, 256, 0, st>>>(P, r);
+            else
+                k_build1_generic_list<false><<<listed, 256, 0, st>>>(P, r);
+        }
+        g_launches.fetch_add(generic ? 2 : 1);
+        return;
+    }
     if (L == 1) {
         // lean kernel for the 27-cell walk, generic kernel for the other slots
         if (half) {
@@ -1086,7 +1129,7 @@ void Engine::launch_build(int r) {
         g_launches.fetch_add(4);
         return;
     }
-#define PIS_CALL(L) launch_build_t<L>(*d_, half_, any_tric_, ch, ls_, r, any_generic_)
+#define PIS_CALL(L) launch_build_t<L>(*d_, half_, any_tric_, ch, ls_, r, any_generic_, listed_ ? (unsigned)listed_grid_ : 0u)
     PIS_LPA_DISPATCH(opt_.lpa, PIS_CALL)
 #undef PIS_CALL
 }

@@ -295,6 +295,10 @@ class Engine {
     bool any_tric_ = false;    // some active slot has a triclinic box (selects the rebuild kernels)
     int scan_segs_ = 1;        // cell-scan segments of the largest slot (1: one scan block per slot)
     bool any_generic_ = false; // some active slot needs the generic list walk (not the 27-cell walk)
+    // replica pools with the thread-per-atom list: the rebuild kernels run a grid of listed_grid_
+    // blocks over a list of the rebuilding slots' chunks and cells
+    bool listed_ = false;
+    int listed_grid_ = 0;
     bool fused_ = false;       // mixed steps run the fused force + kick + drift kernel
     bool list_groups_ = false; // the per-atom list is stored in groups of consecutive entries
     void* prel_buf_[2] = {nullptr, nullptr};  // the two cell-relative coordinate buffers (fused steps)
