@@ -1449,8 +1449,10 @@ void Engine::reset_stage_times() {
 pis_status Engine::run(int64_t k, std::string& err) {
     pis_status st = rebuild_block_map(err);
     if (st) return st;
-    // fused steps: a graph holds at most RING_STEPS steps (the rows of the partial ring)
-    const int64_t G = (fused_ && graph_steps_ > RING_STEPS) ? RING_STEPS : graph_steps_;
+    // fused steps: a graph holds at most RING_STEPS steps (the rows of the partial ring), and no
+    // more than the energy history holds (its entries are written by parallel blocks at the end)
+    int64_t G = graph_steps_;
+    if (fused_) G = std::min<int64_t>(G, std::min<int64_t>(RING_STEPS, opt_.hist));
     while (k > 0) {
         int64_t g = k >= G ? G : k;
         // graphs differ by length, instrumentation and whether the fused step records thermo
