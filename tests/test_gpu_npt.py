@@ -67,6 +67,28 @@ def test_sheared_box_trajectory_bit_identical(state):
     assert np.array_equal(pos, o.pos) and np.array_equal(vel, o.vel)
 
 
+def test_sheared_slot_in_a_replica_pool(state):
+    # a sheared slot beside a cubic one in an FP64 replica pool, whose rebuild kernels stride over
+    # the listed chunks and cells with the triclinic instantiations: each slot's 40 steps match
+    # the oracle's run (energies at the FP64 bar, positions within 1e-9 sigma)
+    from pis_gb300.batch import Batch
+    cubic = melted(liquid(nc=6, seed=31), steps=50, dt=0.005)
+    systems = (state, cubic)
+    b = Batch(4000, 3, 0, precision="fp64")
+    slots = [b.admit(s["pos"], s["types"], s["masses"], s["h"], s["table"], 40, velocities=s["vel"]) for s in systems]
+    b.advance(40)
+    for s, slot in zip(systems, slots):
+        o = to_oracle(s)
+        pe_ref, _, _ = o.run_nve_exact(0.005, 40)
+        hist = b.pe_history(slot, 40)
+        assert np.max(np.abs(hist - pe_ref[1:]) / np.abs(pe_ref[1:])) <= 1e-11
+        r = b.result(slot, len(s["pos"]))
+        f = (r["pos"] - o.pos) @ np.linalg.inv(s["h"]).T  # fractional difference, minimum image
+        f -= np.round(f)
+        assert np.abs(f @ s["h"].T).max() <= 1e-9
+    b.close()
+
+
 def test_symmetric_box_scaling(state):
     # Atoms::scale_box with a symmetric matrix (the barostat's form): box, positions and the
     # next evaluation against the oracle
