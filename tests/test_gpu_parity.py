@@ -223,6 +223,32 @@ def test_two_cell_box_walks(oracle_lib, cuda_lib, edge_margin):
         assert np.all(np.isfinite(e))
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_two_cell_generic_walk_in_a_replica_pool(oracle_lib, cuda_lib, prec):
+    # a generic-walk box as in the test above (4 lattice cells per edge, so that its ~134 list
+    # entries per atom fit a replica pool's fixed capacity) beside an ordinary liquid in one
+    # replica pool, whose rebuild kernels stride over the listed chunks (the generic walk's list
+    # form included): the first evaluation of each slot gives the all-pairs forces
+    import oracle
+    from pis_gb300.batch import Batch
+    s = displaced(liquid(nc=4, rho=0.95), 0.02, 4)
+    L = s["h"][0, 0]
+    other = displaced(liquid(nc=6, seed=12), 0.02, 5)
+    b = Batch(2000, 2, 0, precision=prec)
+    slots = [b.admit(x["pos"], x["types"], x["masses"], x["h"], x["table"], 20, velocities=x["vel"], skin=sk)
+             for x, sk in ((s, L / 2 * (1 - 2e-6) - 2.5), (other, 0.3))]
+    tol = FP64_TOL if prec == "fp64" else 1e-5
+    for x, slot in zip((s, other), slots):
+        o = to_oracle(x)
+        pe_ref = o.compute_potential(manager=oracle.ALLPAIRS)
+        r = b.result(slot, len(x["pos"]))
+        assert abs(r["pe"] - pe_ref) <= tol * abs(pe_ref)
+        assert rel_norm(r["force"], o.force) <= tol
+    b.advance(20)
+    assert all(np.isfinite(b.result(sl, len(x["pos"]))["pe"]) for sl, x in zip(slots, (s, other)))
+    b.close()
+
+
 def test_errors_are_reported(oracle_lib, cuda_lib):
     from pis_gb300 import PisError
     s = liquid(nc=2)  # L = 3.36 < 2 (rc + skin)
