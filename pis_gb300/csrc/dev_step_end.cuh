@@ -428,9 +428,12 @@ __global__ void k_ring_commit(const DP P, int g) {
 // End of a rebuild phase (its last kernel, so every rebuild kernel has read the request flags):
 // count and clear the rebuilt slots' flags and lower the device-wide request word. A drift that
 // runs later in the same step (the fused step kernel) may raise them again for the next step.
-__global__ void k_rebuild_done(const DP P, int step_mode) {
+// body_kernels > 0 (the last kernel of a conditional rebuild body): the body's kernel count is
+// added to ctl[2..3] (64 bits), which the host folds into its launch counter.
+__global__ void k_rebuild_done(const DP P, int step_mode, int body_kernels) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s == 0) {
+        if (body_kernels > 0) *reinterpret_cast<unsigned long long*>(P.ctl + 2) += (unsigned long long)body_kernels;
         P.ctl[0] = 0;
         P.ctl[8] = 0;  // the listed rebuild's counts
         P.ctl[9] = 0;
@@ -529,11 +532,8 @@ __global__ void k_scale_pos(const DP P, int slot, const Mat3Arg HI_old, const Ma
 }
 
 // Condition of a step's rebuild node: some slot rebuilds in this step (the device-wide word).
-// Also counts executed rebuild bodies (ctl[2..3], 64 bits) for the launch counter.
 __global__ void k_set_rebuild_cond(const DP P, cudaGraphConditionalHandle h) {
-    const bool go = P.ctl[0] != 0;
-    cudaGraphSetConditional(h, go ? 1u : 0u);
-    if (go) ++*reinterpret_cast<unsigned long long*>(P.ctl + 2);
+    cudaGraphSetConditional(h, P.ctl[0] != 0 ? 1u : 0u);
 }
 
 // Upload of one slot's state. The caller's arrays (x,y,z per atom, 1-based types) are copied as

@@ -832,8 +832,9 @@ pis_status Engine::rebuild_block_map(std::string& err) {
     // No synchronisation here (the sources are held), so a host loop can change the map while
     // earlier graphs still run: the copies are ordered after them on the stream.
     dirty_map_ = false;
-    // the force kernel variant depends on whether every slot is single-type; captured graphs
-    // bake that choice in, so they are dropped when it flips (after the stream has drained)
+    // kernel choices that follow the active slots (the force kernel for single-type pools, the
+    // triclinic rebuild kernels, the generic walk, the cell-scan grid); step graphs are kept per
+    // combination (Engine::run)
     bool one = true, tric = false, gen = false;
     int segs = 1;  // cell-scan segments of the largest slot (the scan kernels' grid)
     for (int s = 0; s < opt_.max_slots; ++s) {
@@ -845,19 +846,10 @@ pis_status Engine::rebuild_block_map(std::string& err) {
             segs = std::max(segs, (int)((nc + SCAN_SEG - 1) / SCAN_SEG));
         }
     }
-    if (one != single_type_ || tric != any_tric_ || segs != scan_segs_ || gen != any_generic_) {
-        st = check(cudaStreamSynchronize(stream_), "block map", err);
-        if (st) return st;
-        single_type_ = one;
-        any_tric_ = tric;
-        scan_segs_ = segs;
-        any_generic_ = gen;
-        for (auto& kv : graphs_) {
-            cudaGraphExecDestroy(kv.second.exec);
-            for (auto e : kv.second.ev) cudaEventDestroy(e);
-        }
-        graphs_.clear();
-    }
+    single_type_ = one;
+    any_tric_ = tric;
+    scan_segs_ = segs;
+    any_generic_ = gen;
     return st;
 }
 
@@ -908,6 +900,7 @@ pis_status Engine::set_steps(int slot, int64_t steps, std::string& err) {
 void Engine::enqueue_rebuild(bool respect, int q) {
     const DP& P = *d_;
     int r = respect ? 1 + q : 0;
+    const int64_t start = g_launches.load();
     const unsigned ga = (unsigned)max_chunks_;
     const unsigned gl = (unsigned)listed_grid_;
     if (listed_) {
@@ -938,7 +931,9 @@ void Engine::enqueue_rebuild(bool respect, int q) {
             LAUNCH(k_gather<false>, gcells, 256, P, (int64_t)opt_.max_cells, r);
     }
     launch_build(r);
-    LAUNCH(k_rebuild_done, (unsigned)((opt_.max_slots + 127) / 128), 128, P, r);
+    // inside a conditional body the last kernel adds the body's kernel count on the device
+    const int body = ls_ == side_ ? (int)(g_launches.load() - start + 1) : 0;
+    LAUNCH(k_rebuild_done, (unsigned)((opt_.max_slots + 127) / 128), 128, P, r, body);
 }
 
 // Lanes-per-atom kernels are templates; these dispatch on the pool's runtime choice. Their grid
@@ -1368,18 +1363,18 @@ pis_status Engine::enqueue_rebuild_conditional(bool respect, int q) {
     ls_ = stream_;
     const int64_t n_body = g_launches.load() - before;
     g_launches.fetch_sub(n_body);  // counted when a body actually runs (account_body_launches)
-    body_kernels_ = n_body;
+    body_counting_ = true;
     cudaGraph_t out = nullptr;
     if (cudaStreamEndCapture(side_, &out) != cudaSuccess) return PIS_ERR_CUDA;
     return PIS_OK;
 }
 
 void Engine::account_body_launches() {
-    if (!body_kernels_ || !d_) return;
+    if (!body_counting_ || !d_) return;
     unsigned long long n = 0;
     if (cudaMemcpy(&n, d_->ctl + 2, sizeof(n), cudaMemcpyDeviceToHost) != cudaSuccess) return;
     if (n > body_seen_) {
-        g_launches.fetch_add((int64_t)(n - body_seen_) * body_kernels_);
+        g_launches.fetch_add((int64_t)(n - body_seen_));
         body_seen_ = n;
     }
 }
@@ -1455,8 +1450,13 @@ pis_status Engine::run(int64_t k, std::string& err) {
     if (fused_) G = std::min<int64_t>(G, std::min<int64_t>(RING_STEPS, opt_.hist));
     while (k > 0) {
         int64_t g = k >= G ? G : k;
-        // graphs differ by length, instrumentation and whether the fused step records thermo
+        // graphs differ by length, instrumentation, whether the fused step records thermo, and
+        // the kernel choices the pool's slots imply (one type, a triclinic slot, a slot on the
+        // generic walk, the cell-scan segments): a pool whose slots come and go keeps one graph
+        // per combination instead of recapturing at every change
         int64_t key = 4 * g + (instrument_ ? 1 : 0) + (thermo_slots_ > 0 ? 2 : 0);
+        key = key * 8 + (single_type_ ? 4 : 0) + (any_tric_ ? 2 : 0) + (any_generic_ ? 1 : 0);
+        key = key * 4096 + std::min(scan_segs_, 4095);
         auto it = graphs_.find(key);
         if (it == graphs_.end()) {
             GraphRec rec;
@@ -1500,7 +1500,7 @@ pis_status Engine::run(int64_t k, std::string& err) {
                 if (!cond_rebuild_) return check(ce == cudaSuccess ? cudaErrorUnknown : ce, "capture", err);
                 // conditional nodes unavailable: capture the plain step sequence instead
                 cond_rebuild_ = false;
-                body_kernels_ = 0;
+                body_counting_ = false;
             }
             it = graphs_.emplace(key, rec).first;
         }

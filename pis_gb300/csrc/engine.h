@@ -255,8 +255,8 @@ class Engine {
                                    // conditional body is captured)
     cudaStream_t side_ = nullptr;  // capture stream of conditional bodies
     bool cond_rebuild_ = true;     // step graphs skip the rebuild kernels through a conditional node
-    int64_t body_kernels_ = 0;     // kernels in one conditional rebuild body
-    uint64_t body_seen_ = 0;       // bodies already counted into the launch counter
+    bool body_counting_ = false;   // conditional rebuild bodies count their kernels on the device
+    uint64_t body_seen_ = 0;       // body kernels already counted into the launch counter
     bool cond_step_ = false;       // a capture with conditional rebuild nodes is in progress
     pis_status cond_error_ = PIS_OK;
     cudaStream_t stream_ = nullptr;
