@@ -398,6 +398,12 @@ def main():
     e2e_vel[:] = melt_vel
     e2e_types[:] = types
     e2e_out = (pinned((n, 3), torch.float64), pinned((n, 3), torch.float64), pinned((n, 3), torch.float64))
+    # one untimed pass of the same calls first (W steps): the step graphs of this entry point are
+    # captured there, as the timed steps of `value` follow their own warm-up
+    mix.set_state(e2e_pos, e2e_types, [1.0], h, velocities=e2e_vel)
+    mix.compute_potential(want_forces=False)
+    mix.verlet_step_nve(DT, max(args.warmup, 3))
+    mix.get_state(out=e2e_out)
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
@@ -469,7 +475,8 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d / k_e2e,
                     "d2h_bytes_per_step": d2h / k_e2e, "seconds": e2e_s,
-                    "path": "set_state + compute_potential + verlet_step_nve(K) + get_state, pinned host buffers"},
+                    "path": "set_state + compute_potential + verlet_step_nve(K) + get_state, pinned host buffers, "
+                            "after one untimed pass of the same calls"},
             "roofline": roofline,
             "error_vs_fp64": {"force_rms_rel": force_rms, "pe_rel": pe_rel, "cutoff_edge": cut_edge,
                               "default_options": {"force_rms_rel": errs["default_options"][0],
