@@ -634,44 +634,62 @@ __global__ void __launch_bounds__(256) k_build(const DP P, int step_mode) {
 // cells whose nearest face is beyond the list radius for this atom are skipped.
 //
 // Candidates of one neighbour cell [j, jend), tested against the padded list radius and written
-// in candidate order. Two phases per run of up to 32 candidates: a branch-free pass that shifts one
-// bit per candidate into a mask (candidate k ends at bit m - 1 - k; shifting the mask instead of
-// setting bit k cut the rebuild by 6 %), then the accepted ones written from the highest bit down,
-// so the lanes of a warp diverge only in how many candidates and entries they have (a loop that
-// branched on every candidate to store it made rebuilds 2 % slower). The tests against atom i
-// itself (half list: above i; full list: not i) are one mask operation per run.
-template <bool HALF>
+// in candidate order. Two phases per run of up to 32 candidates: a branch-free pass that records one
+// bit per candidate in a mask, then the accepted ones written in order, so the lanes of a warp
+// diverge only in how many candidates and entries they have (a loop that branched on every
+// candidate to store it made rebuilds 2 % slower).
+// SHIFT: the mask is shifted one bit per candidate (candidate k ends at bit m - 1 - k) and the
+// tests against atom i itself (half list: above i; full list: not i) are one mask operation per
+// run: the single-system build (every chunk rebuilds at once) runs 6 % faster so. Otherwise bit k
+// is set with the self tests per candidate: the listed build of replica pools, where few chunks
+// rebuild at once, ran 6 % slower with the other form.
+template <bool HALF, bool SHIFT>
 __device__ __forceinline__ void scan_cell_mask(const float4* __restrict__ prel, int j, int jend, float sx, float sy,
                                                float sz, float rl2, uint32_t codebits, int i, bool home,
                                                uint32_t*& out, int& cnt, int64_t jump, int qmask, int cap) {
     for (int j0 = j; j0 < jend; j0 += 32) {
         const int m = min(32, jend - j0);
         const float4* __restrict__ pp = prel + j0;
-        uint32_t mask = 0;  // candidate k at bit m - 1 - k
+        uint32_t mask = 0;  // SHIFT: candidate k at bit m - 1 - k; otherwise at bit k
 #pragma unroll 4
         for (int k = 0; k < m; ++k) {
             const float4 pj = pp[k];
             const float dx = pj.x + sx, dy = pj.y + sy, dz = pj.z + sz;
-            const bool take = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= rl2;
-            mask = (mask << 1) | (uint32_t)take;
+            bool take = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= rl2;
+            if (SHIFT) {
+                mask = (mask << 1) | (uint32_t)take;
+            } else {
+                if (HALF)
+                    take = take && j0 + k > i;
+                else if (home)
+                    take = take && j0 + k != i;
+                mask |= (uint32_t)take << k;
+            }
         }
-        // the run's candidates j0 + k against atom i, once per run: above i (half list) or not i
-        const int t = i - j0;
-        if (HALF)
-            mask = t >= m - 1 ? 0u : (t >= 0 ? mask & ((1u << (m - 1 - t)) - 1u) : mask);
-        else if (home && t >= 0 && t < m)
-            mask &= ~(1u << (m - 1 - t));
+        if (SHIFT) {  // the run's candidates j0 + k against atom i: above i (half list) or not i
+            const int t = i - j0;
+            if (HALF)
+                mask = t >= m - 1 ? 0u : (t >= 0 ? mask & ((1u << (m - 1 - t)) - 1u) : mask);
+            else if (home && t >= 0 && t < m)
+                mask &= ~(1u << (m - 1 - t));
+        }
         while (mask) {
-            const int b = 31 - __clz(mask);
-            const int k = m - 1 - b;
-            mask ^= 1u << b;
+            int k;
+            if (SHIFT) {
+                const int b = 31 - __clz(mask);
+                k = m - 1 - b;
+                mask ^= 1u << b;
+            } else {
+                k = __ffs(mask) - 1;
+                mask &= mask - 1;
+            }
             if (cnt < cap) *out = (uint32_t)(j0 + k) | codebits;
             ++cnt;
             out += ((cnt & qmask) == 0) ? jump : 1;
         }
     }
 }
-template <bool HALF, bool TRIC>
+template <bool HALF, bool TRIC, bool SHIFT = true>
 __device__ __forceinline__ void build1_chunk(const DP& P, int blk, int step_mode) {
     int s, i;
     if (!atom_of_blk(P, blk, s, i)) return;
@@ -724,7 +742,7 @@ __device__ __forceinline__ void build1_chunk(const DP& P, int blk, int step_mode
                     shy = (float)ox * sp.fcv[1] + (float)oy * sp.fcv[4] + (float)oz * sp.fcv[7];
                     shz = (float)ox * sp.fcv[2] + (float)oy * sp.fcv[5] + (float)oz * sp.fcv[8];
                 }
-                scan_cell_mask<HALF>(prel, b0, b1, shx - pi.x, shy - pi.y, shz - pi.z, rl2, codebits, i, home, out,
+                scan_cell_mask<HALF, SHIFT>(prel, b0, b1, shx - pi.x, shy - pi.y, shz - pi.z, rl2, codebits, i, home, out,
                                 cnt, jump, qmask, cap);
             }
         }
@@ -760,7 +778,7 @@ __global__ void __launch_bounds__(256) k_build1_generic(const DP P, int step_mod
 template <bool HALF, bool TRIC>
 __global__ void __launch_bounds__(256) k_build1_list(const DP P, int step_mode) {
     const int n = P.ctl[8];
-    for (int q = blockIdx.x; q < n; q += gridDim.x) build1_chunk<HALF, TRIC>(P, P.rb_list[q], step_mode);
+    for (int q = blockIdx.x; q < n; q += gridDim.x) build1_chunk<HALF, TRIC, false>(P, P.rb_list[q], step_mode);
 }
 template <bool HALF>
 __global__ void __launch_bounds__(256) k_build1_generic_list(const DP P, int step_mode) {
