@@ -230,7 +230,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         items.push_back({(void**)&d_->ring, 8 * 3 * (size_t)RING_STEPS * NCH});
     }
     // replica pools: the rebuild kernels stride over a list of the rebuilding slots' chunks and
-    // cells (1.054 vs 1.078 ms per step of the 512-replica mix)
+    // cells (1.028 vs 1.078 ms per step of the 512-replica mix)
     listed_ = opt.max_slots > 1 && opt.lpa == 1 && !opt.cluster && !clm_;
     if (listed_) {
         items.push_back({(void**)&d_->rb_list, 4 * (NCH + NC)});
@@ -239,7 +239,7 @@ pis_status Engine::init(const PoolOptions& opt, std::string& err) {
         if (st) return st;
         st = check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device query", err);
         if (st) return st;
-        listed_grid_ = 4 * sms;  // resident blocks of the 64-register build and gather kernels
+        listed_grid_ = 8 * sms;  // twice the resident blocks of the 64-register build and gather kernels
     }
     const bool exact = opt.precision == PIS_PRECISION_FP64;
     if (exact) {
